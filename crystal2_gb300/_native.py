@@ -1,0 +1,125 @@
+"""ctypes binding of ``libc2g.so`` (the C ABI declared in ``include/c2g.h``).
+
+The library is built in-tree (``crystal2_gb300/build.py``).  There is no CPU fallback: when the
+shared library is missing, or a call needs a GPU and none is present, the call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libc2g.so")
+
+C2G_OK = 0
+C2G_ERR_INVALID = 1
+C2G_ERR_IO = 2
+C2G_ERR_PARSE = 3
+C2G_ERR_CUDA = 4
+C2G_ERR_OOM = 5
+C2G_ERR_DEVICE = 6
+C2G_ERR_STATE = 7
+C2G_ERR_UNSUPPORTED = 8
+
+ACCEL_BVH = 0
+ACCEL_BRUTE = 1
+TREE_REF_EQUAL_COUNT = 0
+TREE_SAH = 1
+INTEGRATOR_PATH = 0
+INTEGRATOR_DIRECT = 1
+INTEGRATOR_GUIDED = 2
+
+STATUS_NAMES = {
+    C2G_ERR_INVALID: "invalid argument", C2G_ERR_IO: "i/o error", C2G_ERR_PARSE: "parse error",
+    C2G_ERR_CUDA: "CUDA error", C2G_ERR_OOM: "out of device memory", C2G_ERR_DEVICE: "device error",
+    C2G_ERR_STATE: "bad state", C2G_ERR_UNSUPPORTED: "unsupported",
+}
+
+
+class C2GError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, 'error')} ({code}): {msg}")
+        self.code = code
+
+
+class DeviceOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("mem_limit_bytes", C.c_size_t), ("verbose", C.c_int)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("spp", C.c_int), ("max_depth", C.c_int),
+                ("integrator", C.c_int), ("accel", C.c_int), ("sample_begin", C.c_int), ("sample_count", C.c_int),
+                ("wave_paths", C.c_int), ("seed", C.c_uint64)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("seconds", C.c_double), ("paths", C.c_double), ("rays_closest", C.c_double),
+                ("rays_shadow", C.c_double), ("nodes_visited", C.c_double), ("prims_tested", C.c_double),
+                ("kernel_ms", C.c_double * 8), ("kernel_launches", C.c_int), ("waves", C.c_int)]
+
+
+_P = C.c_void_p
+_I = C.c_int
+_FP = C.POINTER(C.c_float)
+_IP = C.POINTER(C.c_int)
+
+# name -> (restype, argtypes); this table is also the list of symbols include/c2g.h declares
+SIGNATURES = {
+    "c2g_create": (_I, [C.POINTER(_P), C.POINTER(DeviceOpts)]),
+    "c2g_destroy": (None, [_P]),
+    "c2g_last_error": (C.c_char_p, [_P]),
+    "c2g_version": (C.c_char_p, []),
+    "c2g_load_json": (_I, [_P, C.c_char_p, C.c_char_p, _I]),
+    "c2g_load_json_text": (_I, [_P, C.c_char_p, C.c_char_p, _I]),
+    "c2g_bvh_build": (_I, [_P, _I]),
+    "c2g_get_render_params": (_I, [_P, C.POINTER(RenderParams)]),
+    "c2g_num_objects": (_I, [_P]),
+    "c2g_num_lights": (_I, [_P]),
+    "c2g_bvh_order": (_I, [_P, _IP, _I]),
+    "c2g_bvh_nodes": (_I, [_P, _FP, _IP, _IP, _I]),
+    "c2g_render": (_I, [_P, C.POINTER(RenderParams), _P]),
+    "c2g_film_clear": (_I, [_P, _P]),
+    "c2g_film_download": (_I, [_P, _FP, _FP]),
+    "c2g_film_image": (_I, [_P, _FP]),
+    "c2g_film_download_m2": (_I, [_P, _FP]),
+    "c2g_get_stats": (_I, [_P, C.POINTER(Stats)]),
+    "c2g_set_counting": (_I, [_P, _I]),
+    "c2g_trace_rays": (_I, [_P, _I, _FP, _FP, _FP, _FP, _IP, _I, _IP, _FP]),
+    "c2g_trace_rays_dev": (_I, [_P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
+    "c2g_halton": (_I, [_P, _I, _I, _I, _IP, _IP, _IP, _I, _FP]),
+    "c2g_camera_rays": (_I, [_P, _I, _FP, _FP, _FP]),
+}
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load ``libc2g.so`` (raises FileNotFoundError when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: build it with `python crystal2_gb300/build.py`")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def fptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_FP)
+
+
+def iptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_IP)

@@ -1,0 +1,61 @@
+// Host-side scene: the reference's JSON/OBJ inputs parsed and flattened into the POD arrays of
+// c2g_types.h.  Mirrors RayTracer's construction (src/Core/RayTracer.cpp:11-22):
+// ConfigLoader::LoadConfigInfo, Scene::CreateScene, Camera::CreateCamera, Integrator and
+// Sampler factories.
+#pragma once
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../c2g_types.h"
+#include "fmath.h"
+#include "json.h"
+
+namespace c2g {
+
+struct SceneError : std::runtime_error {
+    int code;
+    SceneError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+struct HostConfig {
+    int width = 0, height = 0, spp = 0, threads = 1;
+    std::string accel;            // "BVH" | "Brute" | "KDTree"
+    std::string integrator;       // "PathTracer" | "DirectLight" | "GuidedPathTracer"
+    int depth = 0;
+    std::string sampler;          // "Halton" (others: Default, Stratified)
+    long long seed = 0;
+};
+
+struct HostScene {
+    HostConfig cfg;
+    Camera cam{};
+    std::vector<ObjInfo> objs;         // scene order
+    std::vector<fm::V3> tri_pos;       // 3 per triangle
+    std::vector<TriShade> tri_shade;   // per triangle
+    std::vector<Quadric> quads;        // spheres and disks
+    std::vector<float> quad_box;       // 6 per quadric (GetBoundingBox)
+    std::vector<Material> mats;
+    std::vector<Light> lights;         // Scene::_lights order
+
+    size_t num_objects() const { return objs.size(); }
+    // Object bounding box (IIntersectable::GetBoundingBox) as min xyz, max xyz.
+    void object_box(int obj, float out[6]) const;
+};
+
+// Parse config + scene JSON (already loaded as text).  Throws SceneError / JsonError.
+void load_scene(HostScene& s, const std::string& config_text, const std::string& scene_text);
+std::string read_text_file(const std::string& path);  // throws SceneError(C2G_ERR_IO)
+
+// Halton sampler tables (HaltonSampler.cpp:164-229).
+HaltonParams halton_params(int width, int height);
+// 100 permutation tables from one default-seeded std::mt19937 and std::shuffle, concatenated in
+// prime order (24133 entries), plus each table's start offset.
+void halton_perm_tables(std::vector<uint16_t>& perm, std::vector<int>& offset);
+// Radical-inverse primes of dims 0..99.
+const int* halton_primes();
+// GetVectorIndexForSample for a pixel and sample (HaltonSampler.cpp:251-270).
+int halton_vector_index(const HaltonParams& hp, int px, int py, int sample);
+
+}  // namespace c2g

@@ -1,0 +1,854 @@
+// Wavefront path tracer for sm_103a: kernels and their host orchestration.
+//
+// One wave = a fixed set of camera paths (all pixels x a range of samples).  Per bounce:
+//   extend     closest hit of every queued path ray                      (BVH::Intersect)
+//   shade      hit record -> emission, NEE rays, BSDF continuation, RR   (Evaluate + EsimateDirect)
+//   shadow     any-hit of the NEE light-sample rays                      (BVH::IntersectTest)
+//   mis        closest hit of the NEE BSDF-sample rays + emitter check   (EsimateDirect, BSDF half)
+//   accumulate direct lighting added to the path radiance; finished paths written out
+// and at the end of the wave `film` adds every sample to its pixel in sample order
+// (FrameBuffer::AddSample).  Path state is SoA in float4 arrays and is compacted into the
+// next queue with warp ballot/popc appends, so every kernel reads its inputs coalesced.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../host/bvh.h"
+#include "../host/scene.h"
+#include "render.h"
+#include "shade.cuh"
+
+namespace c2g {
+
+// ---- arena -----------------------------------------------------------------------------------
+DeviceArena::~DeviceArena() { free_all(); }
+
+void* DeviceArena::alloc(size_t bytes, std::string& err) {
+    if (bytes == 0) bytes = 16;
+    bytes = (bytes + 255) & ~size_t(255);
+    if (cap_ && used_ + bytes > cap_) {
+        err = "device memory cap exceeded (" + std::to_string(used_ + bytes) + " > " + std::to_string(cap_) + " bytes)";
+        return nullptr;
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        err = std::string("cudaMalloc failed: ") + cudaGetErrorString(e);
+        return nullptr;
+    }
+    blocks_.push_back({p, bytes});
+    used_ += bytes;
+    return p;
+}
+
+void DeviceArena::free(void* p) {
+    if (!p) return;
+    for (size_t i = 0; i < blocks_.size(); i++) {
+        if (blocks_[i].p == p) {
+            cudaFree(p);
+            used_ -= blocks_[i].n;
+            blocks_.erase(blocks_.begin() + i);
+            return;
+        }
+    }
+}
+
+void DeviceArena::free_all() {
+    for (auto& b : blocks_) cudaFree(b.p);
+    blocks_.clear();
+    used_ = 0;
+}
+
+// ---- buffers -----------------------------------------------------------------------------------
+struct DeviceSceneBuffers {
+    DevScene S{};
+    std::vector<void*> owned;
+    int* err = nullptr;
+    unsigned long long* counts = nullptr;  // nodes/prims counters (closest, any)
+    float4* film = nullptr;                // rgb sum, weight
+    float4* film_m2 = nullptr;             // rgb sum of squares
+    int n_lights = 0;
+};
+
+struct WaveBuffers {
+    size_t P = 0;     // path capacity
+    int K = 0;        // NEE slots per path
+    float4* o[2] = {nullptr, nullptr};
+    float4* d[2] = {nullptr, nullptr};
+    float4* beta[2] = {nullptr, nullptr};
+    float4* L[2] = {nullptr, nullptr};
+    float4* hit = nullptr;
+    int2* acc = nullptr;
+    float4* out_L = nullptr;
+    float4* sh_o = nullptr;
+    float4* sh_d = nullptr;
+    float4* sh_c = nullptr;
+    float4* mis_o = nullptr;
+    float4* mis_d = nullptr;
+    float4* mis_c = nullptr;
+    int* sh_list = nullptr;
+    int* mis_list = nullptr;
+    int* counters = nullptr;  // [0],[1] path queues, [2] shadow, [3] mis
+    std::vector<void*> owned;
+};
+
+GpuScene::GpuScene() : sb_(new DeviceSceneBuffers()), wb_(new WaveBuffers()) {}
+GpuScene::~GpuScene() {
+    delete sb_;
+    delete wb_;
+}
+
+// ---- small device helpers ------------------------------------------------------------------------
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// Warp-aggregated append: one atomic per warp, lanes with pred get consecutive slots in lane order.
+// Must be called by all 32 lanes of the warp.
+__device__ __forceinline__ int warp_append(int* counter, bool pred) {
+    unsigned m = __ballot_sync(0xffffffffu, pred);
+    int base = 0;
+    if (lane_id() == 0 && m) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return pred ? base + __popc(m & ((1u << lane_id()) - 1u)) : -1;
+}
+
+__device__ __forceinline__ void warp_count(unsigned long long* dst, unsigned v) {
+    unsigned long long s = v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane_id() == 0 && s) atomicAdd(dst, s);
+}
+
+struct WaveArgs {
+    int W, H;
+    int tiles_x;
+    int nslots;          // pixel slots (8x8 tiles)
+    int wave_samples;    // samples of this wave
+    int sample0;         // first sample index of the wave
+    int max_depth;
+    int K;               // NEE slots per path
+    int integrator;
+};
+
+__device__ __forceinline__ void slot_pixel(const WaveArgs& a, int slot, int& x, int& y) {
+    int tile = slot >> 6, w = slot & 63;
+    x = (tile % a.tiles_x) * 8 + (w & 7);
+    y = (tile / a.tiles_x) * 8 + (w >> 3);
+}
+
+__device__ __forceinline__ int pack_state(int dim, int bounce, int light_path) {
+    return (dim & 0xffff) | ((bounce & 0xff) << 16) | (light_path << 24);
+}
+
+struct PathRefs {
+    float4 *o, *d, *beta, *L;
+};
+
+// ---- raygen (SamplerIntegrator.cpp:42-55 + PerspCamera::GenerateRay) -----------------------------
+__global__ void k_raygen(DevScene S, WaveArgs a, PathRefs out, float4* out_L, int* qcount) {
+    const int total = a.nslots * a.wave_samples;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < total; base += stride) {
+        int pid = base + threadIdx.x;
+        bool valid = pid < total;
+        int x = 0, y = 0, s_local = 0;
+        if (valid) {
+            s_local = pid / a.nslots;
+            slot_pixel(a, pid - s_local * a.nslots, x, y);
+            valid = x < a.W && y < a.H;
+            out_L[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        int j = warp_append(qcount, valid);
+        if (valid) {
+            int sample = a.sample0 + s_local;
+            int vidx = halton_vector_index(S.hp, x, y, sample);
+            float sx = halton_dim0(vidx, S.hp);
+            float sy = halton_dim1(vidx, S.hp);
+            float nx, ny;
+            pixel_ndc(x, y, sx, sy, a.W, a.H, nx, ny);
+            float3 o, d;
+            camera_ray(S.cam, nx, ny, o, d);
+            out.o[j] = make_float4(o.x, o.y, o.z, __int_as_float(pid));
+            out.d[j] = make_float4(d.x, d.y, d.z, __int_as_float(pack_state(2, 0, 1)));
+            out.beta[j] = make_float4(1.f, 1.f, 1.f, __int_as_float(vidx));
+            out.L[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+}
+
+// ---- extend: closest hit of each queued path ray ------------------------------------------------
+template <bool COUNT>
+__global__ void k_extend(DevScene S, const float4* __restrict__ qo, const float4* __restrict__ qd, float4* hit,
+                         const int* qcount, int* zero_a, int* zero_b, int* zero_c, unsigned long long* cnt) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) { *zero_a = 0; *zero_b = 0; *zero_c = 0; }
+    const int n = *qcount;
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        float4 o = qo[i], d = qd[i];
+        TraceCounters tc{0, 0};
+        Hit h = trace_closest<COUNT>(S, f3(o), f3(d), &tc);
+        hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.obj));
+        if (COUNT) { atomicAdd(cnt + 0, (unsigned long long)tc.nodes); atomicAdd(cnt + 1, (unsigned long long)tc.prims); }
+    }
+}
+
+// ---- shade ---------------------------------------------------------------------------------------
+struct ShadeOut {
+    PathRefs nxt;
+    int* nxt_count;
+    float4 *sh_o, *sh_d, *sh_c;
+    float4 *mis_o, *mis_d, *mis_c;
+    int *sh_list, *mis_list;
+    int *sh_count, *mis_count;
+    int2* acc;
+};
+
+__global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs cur, const float4* __restrict__ hits,
+                                                const int* qcount, ShadeOut out) {
+    const int n = *qcount;
+    const int stride = gridDim.x * blockDim.x;
+    const int K = a.K;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int i = base + threadIdx.x;
+        const bool valid = i < n;
+        // ---- load path state
+        float4 o4 = make_float4(0, 0, 0, 0), d4 = o4, b4 = o4, L4 = o4, h4 = make_float4(0, 0, 0, __int_as_float(-1));
+        if (valid) { o4 = cur.o[i]; d4 = cur.d[i]; b4 = cur.beta[i]; L4 = cur.L[i]; h4 = hits[i]; }
+        const int pid = __float_as_int(o4.w);
+        const int packed = __float_as_int(d4.w);
+        int dim = packed & 0xffff;
+        int bounce = (packed >> 16) & 0xff;
+        int light_path = (packed >> 24) & 1;
+        const int vidx = __float_as_int(b4.w);
+        int s_local = valid ? pid / a.nslots : 0;
+        int px = 0, py = 0;
+        if (valid) slot_pixel(a, pid - s_local * a.nslots, px, py);
+        const uint32_t pixel = (uint32_t)(py * a.W + px);
+        const uint32_t sample = (uint32_t)(a.sample0 + s_local);
+        float3 ro = f3(o4), rd = f3(d4);
+        float3 beta = f3(b4), L = f3(L4);
+        Hit h{h4.x, h4.y, h4.z, __float_as_int(h4.w)};
+
+        bool alive = valid && h.obj >= 0;       // miss: the path ends (no skybox)
+        bool do_nee = false;
+        bool cont = false;
+        float3 next_o = ro, next_d = rd;
+        Surface s;
+        BxDF bx;
+        Frame fr;
+        float3 wo = -rd;
+        if (alive) {
+            make_surface(S, ro, rd, h, s);
+            if (light_path && s.light >= 0) {
+                const Light& Lg = S.lights[s.light];
+                float3 n_actual = s.front ? s.N : -s.N;
+                L = L + beta * area_Le(Lg, n_actual, -rd);
+            }
+            if (s.mat < 0) {
+                // no BSDF: continue straight through (PathTracingIntegrator.cpp:64-68)
+                next_o = spawn_origin(s, rd);
+                next_d = rd;
+                cont = true;
+            } else {
+                bx = make_bxdf(S.mats[s.mat], s.front);
+                fr.T = s.dpdu; fr.N = s.N; fr.B = s.dpdv;
+                do_nee = true;
+            }
+        }
+        // ---- next-event estimation: UniformSampleAllLights (PathTracingIntegrator.cpp:175-186)
+        float2 uL = make_float2(0, 0), uB = make_float2(0, 0);
+        if (do_nee) {
+            uL = make_float2(halton_sample(S, vidx, dim, pixel, sample), halton_sample(S, vidx, dim + 1, pixel, sample));
+            uB = make_float2(halton_sample(S, vidx, dim + 2, pixel, sample), halton_sample(S, vidx, dim + 3, pixel, sample));
+            dim += 4;
+        }
+        const int nsflags = BXDF_ALL & ~BXDF_SPECULAR;
+        for (int l = 0; l < K; l++) {
+            bool sh_valid = false, mis_valid = false;
+            float4 sh_o4, sh_d4, sh_c4 = make_float4(0, 0, 0, 0), mis_o4, mis_d4, mis_c4 = make_float4(0, 0, 0, 0);
+            if (do_nee && l < S.n_lights) {
+                const Light Lg = S.lights[l];
+                bool eligible = !(Lg.flux_zero != 0.f) && l != s.light;
+                if (eligible) {
+                    // light-sampling half (EsimateDirect, :195-227)
+                    float3 lpos;
+                    float pdf_l;
+                    float3 Li = light_sample_li(S, Lg, s.pos, s.N, uL, lpos, pdf_l);
+                    float3 wi = normalize(lpos - s.pos);
+                    if (pdf_l != 0.f && !is_zero(Li)) {
+                        float3 f = bsdf_f(bx, fr, wo, wi) * fmaxf(0.f, dot(s.N, wi));
+                        float pdf_b = bsdf_pdf(bx, fr, wo, wi, nsflags);
+                        if (!is_zero(f)) {
+                            bool back = dot(lpos - s.pos, s.N) < 0;
+                            float3 org = s.pos + (back ? -s.N : s.N) * kSpawnEps;
+                            float3 dir = lpos - org;
+                            float3 c;
+                            if (Lg.type == LIGHT_POINT) c = f * Li / pdf_l;
+                            else c = f * Li * power_heuristic(pdf_l, pdf_b) / pdf_l;
+                            c = beta * c;
+                            sh_valid = true;
+                            sh_o4 = make_float4(org.x, org.y, org.z, __int_as_float(Lg.type == LIGHT_AREA ? Lg.obj : -1));
+                            sh_d4 = make_float4(dir.x, dir.y, dir.z, 1.f - kEpsTri);
+                            sh_c4 = make_float4(c.x, c.y, c.z, 0.f);
+                        }
+                    }
+                    // BSDF-sampling half (:229-270)
+                    if (Lg.type != LIGHT_POINT) {
+                        float u1 = halton_sample(S, vidx, dim, pixel, sample);
+                        dim += 1;
+                        float3 wi2 = f3(0.f, 0.f, 0.f);
+                        float pdf_b2 = 0.f;
+                        int stype = 0;
+                        bool ok;
+                        float3 f = bsdf_sample(bx, fr, u1, uB, wo, wi2, pdf_b2, nsflags, stype, ok);
+                        if (ok) {
+                            float weight = 1.f;
+                            bool good = true;
+                            if (!(stype & BXDF_SPECULAR)) {
+                                f = f * fmaxf(0.f, dot(s.N, wi2));
+                                float pdf_l2 = light_pdf(S, Lg, s.pos, s.N, wi2);
+                                if (pdf_l2 == 0.f) good = false;
+                                else weight = power_heuristic(pdf_b2, pdf_l2);
+                            }
+                            if (good) {
+                                float3 org = spawn_origin(s, wi2);
+                                float3 m = beta * (f * weight / pdf_b2);
+                                mis_valid = true;
+                                mis_o4 = make_float4(org.x, org.y, org.z, __int_as_float(l));
+                                mis_d4 = make_float4(wi2.x, wi2.y, wi2.z, 0.f);
+                                mis_c4 = make_float4(m.x, m.y, m.z, 0.f);
+                            }
+                        }
+                    }
+                }
+            }
+            const int e = i * K + l;
+            if (do_nee) {
+                out.sh_c[e] = sh_c4;
+                out.mis_c[e] = mis_c4;
+                if (sh_valid) { out.sh_o[e] = sh_o4; out.sh_d[e] = sh_d4; }
+                if (mis_valid) { out.mis_o[e] = mis_o4; out.mis_d[e] = mis_d4; }
+            }
+            int js = warp_append(out.sh_count, sh_valid);
+            if (sh_valid) out.sh_list[js] = e;
+            int jm = warp_append(out.mis_count, mis_valid);
+            if (mis_valid) out.mis_list[jm] = e;
+        }
+        // ---- continuation: BSDF sample (PathTracingIntegrator.cpp:73-102)
+        if (do_nee) {
+            // GCC evaluates SampleDirection(Get1D(), Get2D(), ...) right to left: Get2D first.
+            float2 u2 = make_float2(halton_sample(S, vidx, dim, pixel, sample), halton_sample(S, vidx, dim + 1, pixel, sample));
+            float u1 = halton_sample(S, vidx, dim + 2, pixel, sample);
+            dim += 3;
+            float3 wi = f3(0.f, 0.f, 0.f);
+            float pdf = 0.f;
+            int stype = 0;
+            bool ok;
+            float3 f = bsdf_sample(bx, fr, u1, u2, wo, wi, pdf, BXDF_ALL, stype, ok);
+            if (ok && fabsf(pdf) != 0.f) {
+                bool specular = (stype & BXDF_SPECULAR) != 0;
+                float cosine = specular ? 1.0f : fmaxf(0.f, (stype & BXDF_TRANSMISSION) ? dot(-s.N, wi) : dot(s.N, wi));
+                light_path = (specular || (stype & BXDF_TRANSMISSION)) ? 1 : 0;
+                next_o = spawn_origin(s, wi);
+                next_d = wi;
+                beta = beta * (f * cosine / pdf);
+                cont = true;
+                if (bounce > 3) {
+                    float q = fmaxf(.05f, 1.f - length(beta));
+                    float u = halton_sample(S, vidx, dim, pixel, sample);
+                    dim += 1;
+                    if (u < q) cont = false;
+                    else beta = beta / (1 - q);
+                }
+            }
+        }
+        if (cont && bounce + 1 >= a.max_depth) cont = false;
+        // ---- enqueue the continuation; finished paths keep L in place for `accumulate`
+        int j = warp_append(out.nxt_count, cont);
+        if (valid) {
+            if (cont) {
+                out.nxt.o[j] = make_float4(next_o.x, next_o.y, next_o.z, __int_as_float(pid));
+                out.nxt.d[j] = make_float4(next_d.x, next_d.y, next_d.z, __int_as_float(pack_state(dim, bounce + 1, light_path)));
+                out.nxt.beta[j] = make_float4(beta.x, beta.y, beta.z, __int_as_float(vidx));
+                out.nxt.L[j] = make_float4(L.x, L.y, L.z, 0.f);
+            } else {
+                cur.L[i] = make_float4(L.x, L.y, L.z, 0.f);
+            }
+            out.acc[i] = make_int2(cont ? j : -1, do_nee ? 1 : 0);
+        }
+    }
+}
+
+// ---- shadow: any-hit of NEE light samples (BVH::IntersectTest) ------------------------------------
+template <bool COUNT>
+__global__ void k_shadow(DevScene S, const int* __restrict__ list, const int* count, const float4* __restrict__ so,
+                         const float4* __restrict__ sd, float4* sc, unsigned long long* cnt) {
+    const int n = *count;
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        int e = list[i];
+        float4 o = so[e], d = sd[e];
+        TraceCounters tc{0, 0};
+        bool occ = trace_any<COUNT>(S, f3(o), f3(d), 0.f, d.w, __float_as_int(o.w), &tc);
+        if (occ) sc[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (COUNT) { atomicAdd(cnt + 2, (unsigned long long)tc.nodes); atomicAdd(cnt + 3, (unsigned long long)tc.prims); }
+    }
+}
+
+// ---- mis: closest hit of NEE BSDF samples; radiance only if the hit emitter is the sampled light --
+template <bool COUNT>
+__global__ void k_mis(DevScene S, const int* __restrict__ list, const int* count, const float4* __restrict__ mo,
+                      const float4* __restrict__ md, float4* mc, unsigned long long* cnt) {
+    const int n = *count;
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        int e = list[i];
+        float4 o = mo[e], d = md[e];
+        int l = __float_as_int(o.w);
+        TraceCounters tc{0, 0};
+        Hit h = trace_closest<COUNT>(S, f3(o), f3(d), &tc);
+        float3 res = f3(0.f, 0.f, 0.f);
+        if (h.obj >= 0) {
+            const ObjInfo oi = S.objs[h.obj];
+            if (oi.light == l) {
+                Surface s;
+                make_surface(S, f3(o), f3(d), h, s);
+                float3 n_actual = s.front ? s.N : -s.N;
+                float3 Le = area_Le(S.lights[l], n_actual, -f3(d));
+                float4 m = mc[e];
+                res = f3(m) * Le;
+            }
+        }
+        // no hit: Light::Le of an area light is zero (Light.h:52)
+        mc[e] = make_float4(res.x, res.y, res.z, 0.f);
+        if (COUNT) { atomicAdd(cnt + 0, (unsigned long long)tc.nodes); atomicAdd(cnt + 1, (unsigned long long)tc.prims); }
+    }
+}
+
+// ---- accumulate ------------------------------------------------------------------------------------
+__global__ void k_accumulate(WaveArgs a, PathRefs cur, PathRefs nxt, const int2* __restrict__ acc, const float4* __restrict__ sc,
+                             const float4* __restrict__ mc, float4* out_L, const int* qcount) {
+    const int n = *qcount;
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        int2 ac = acc[i];
+        float3 direct = f3(0.f, 0.f, 0.f);
+        if (ac.y) {
+            for (int l = 0; l < a.K; l++) {
+                float4 s = sc[i * a.K + l], m = mc[i * a.K + l];
+                direct = direct + (f3(s) + f3(m));
+            }
+        }
+        if (ac.x >= 0) {
+            if (ac.y) {
+                float4 L = nxt.L[ac.x];
+                nxt.L[ac.x] = make_float4(L.x + direct.x, L.y + direct.y, L.z + direct.z, 0.f);
+            }
+        } else {
+            float4 L = cur.L[i];
+            int pid = __float_as_int(cur.o[i].w);
+            out_L[pid] = make_float4(L.x + direct.x, L.y + direct.y, L.z + direct.z, 0.f);
+        }
+    }
+}
+
+// ---- film: FrameBuffer::AddSample for every sample of the wave, in sample order ------------------
+__global__ void k_film(WaveArgs a, const float4* __restrict__ out_L, float4* film, float4* film_m2) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < a.nslots; slot += stride) {
+        int x, y;
+        slot_pixel(a, slot, x, y);
+        if (x >= a.W || y >= a.H) continue;
+        int p = y * a.W + x;
+        float4 f = film[p];
+        float4 m2 = film_m2[p];
+        for (int s = 0; s < a.wave_samples; s++) {
+            float4 c = out_L[(size_t)s * a.nslots + slot];
+            if (!isfinite(c.x) || !isfinite(c.y) || !isfinite(c.z)) c = make_float4(0.f, 0.f, 0.f, 0.f);
+            f.x += c.x; f.y += c.y; f.z += c.z; f.w += 1.f;
+            m2.x += c.x * c.x; m2.y += c.y * c.y; m2.z += c.z * c.z;
+        }
+        film[p] = f;
+        film_m2[p] = m2;
+    }
+}
+
+// ---- ray queries ----------------------------------------------------------------------------------
+__global__ void k_trace_rays(DevScene S, int n, const float* o, const float* d, const float* tmin, const float* tmax,
+                             const int* ignore, int any_hit, int* obj, float* t) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float3 ro = f3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
+    float3 rd = f3(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
+    if (any_hit) {
+        float a = tmin ? tmin[i] : 0.f, b = tmax ? tmax[i] : INFINITY;
+        int ig = ignore ? ignore[i] : -1;
+        obj[i] = trace_any<false>(S, ro, rd, a, b, ig, nullptr) ? 1 : 0;
+    } else {
+        Hit h = trace_closest<false>(S, ro, rd, nullptr);
+        obj[i] = h.obj;
+        if (t) t[i] = h.obj >= 0 ? h.t : INFINITY;
+    }
+}
+
+__global__ void k_halton(DevScene S, HaltonParams hp, int W, int n, const int* px, const int* py, const int* sample, int ndim, float* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int vidx = halton_vector_index(hp, px[i], py[i], sample[i]);
+    for (int dd = 0; dd < ndim; dd++) {
+        float v;
+        if (dd == 0) v = halton_dim0(vidx, hp);
+        else if (dd == 1) v = halton_dim1(vidx, hp);
+        else v = halton_sample(S, vidx, dd, (uint32_t)(py[i] * W + px[i]), (uint32_t)sample[i]);
+        out[(size_t)i * ndim + dd] = v;
+    }
+}
+
+__global__ void k_camera(Camera c, int n, const float* pos2, float* o, float* d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float3 ro, rd;
+    camera_ray(c, pos2[2 * i], pos2[2 * i + 1], ro, rd);
+    o[3 * i] = ro.x; o[3 * i + 1] = ro.y; o[3 * i + 2] = ro.z;
+    d[3 * i] = rd.x; d[3 * i + 1] = rd.y; d[3 * i + 2] = rd.z;
+}
+
+// ---- host side -------------------------------------------------------------------------------------
+namespace {
+
+#define C2G_CUDA(call)                                                                       \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            err = std::string(#call) + ": " + cudaGetErrorString(e_);                       \
+            return C2G_ERR_CUDA;                                                             \
+        }                                                                                    \
+    } while (0)
+
+template <typename T>
+T* upload_vec(const std::vector<T>& v, DeviceArena& arena, std::vector<void*>& owned, std::string& err, int& rc) {
+    size_t bytes = std::max<size_t>(sizeof(T), v.size() * sizeof(T));
+    T* p = (T*)arena.alloc(bytes, err);
+    if (!p) { rc = C2G_ERR_OOM; return nullptr; }
+    owned.push_back(p);
+    if (!v.empty()) {
+        cudaError_t e = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { err = cudaGetErrorString(e); rc = C2G_ERR_CUDA; return nullptr; }
+    }
+    return p;
+}
+
+int grid_for(const void* kernel, int block, size_t smem = 0) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, smem);
+    if (per <= 0) per = 1;
+    return sms * per;
+}
+
+}  // namespace
+
+int GpuScene::upload(const HostScene& s, int tree, const RefTree* ref, const SahTree* sah, DeviceArena& arena, std::string& err) {
+    // release previous scene buffers
+    for (void* p : sb_->owned) arena.free(p);
+    sb_->owned.clear();
+    int rc = C2G_OK;
+    DevScene& S = sb_->S;
+    S = DevScene{};
+    S.objs = upload_vec(s.objs, arena, sb_->owned, err, rc);
+    if (rc) return rc;
+    S.tri_shade = upload_vec(s.tri_shade, arena, sb_->owned, err, rc);
+    if (rc) return rc;
+    std::vector<float4> tp(s.tri_pos.size());
+    for (size_t i = 0; i < tp.size(); i++) tp[i] = make_float4(s.tri_pos[i].x, s.tri_pos[i].y, s.tri_pos[i].z, 0.f);
+    S.tri_pos = upload_vec(tp, arena, sb_->owned, err, rc);
+    if (rc) return rc;
+    S.quads = upload_vec(s.quads, arena, sb_->owned, err, rc);
+    if (rc) return rc;
+    S.mats = upload_vec(s.mats, arena, sb_->owned, err, rc);
+    if (rc) return rc;
+    S.lights = upload_vec(s.lights, arena, sb_->owned, err, rc);
+    if (rc) return rc;
+    S.n_lights = (int)s.lights.size();
+    S.n_objs = (int)s.objs.size();
+    std::vector<Prim> prims;
+    S.tree = tree;
+    if (tree == C2G_TREE_SAH) {
+        make_prims(s, sah->order, prims);
+        S.wide_nodes = upload_vec(sah->nodes, arena, sb_->owned, err, rc);
+        if (rc) return rc;
+    } else {
+        make_prims(s, ref->order, prims);
+        S.ref_nodes = upload_vec(ref->nodes, arena, sb_->owned, err, rc);
+        if (rc) return rc;
+    }
+    S.prims = upload_vec(prims, arena, sb_->owned, err, rc);
+    if (rc) return rc;
+    S.n_prims = (int)prims.size();
+    S.anyhit_clip = s.cfg.accel == "BVH" ? 1 : 0;
+    S.closest_box = s.cfg.accel == "Brute" ? 0 : 1;
+    S.cam = s.cam;
+    S.hp = halton_params(s.cfg.width, s.cfg.height);
+    std::vector<uint16_t> perm;
+    std::vector<int> off;
+    halton_perm_tables(perm, off);
+    S.perm = upload_vec(perm, arena, sb_->owned, err, rc);
+    if (rc) return rc;
+    S.perm_off = upload_vec(off, arena, sb_->owned, err, rc);
+    if (rc) return rc;
+    S.seed = (uint64_t)s.cfg.seed;
+    const int* primes = halton_primes();
+    uint64_t magic[kHaltonDims];
+    for (int i = 0; i < kHaltonDims; i++) magic[i] = UINT64_MAX / (uint64_t)primes[i] + 1;
+    C2G_CUDA(cudaMemcpyToSymbol(c_primes, primes, sizeof(int) * kHaltonDims));
+    C2G_CUDA(cudaMemcpyToSymbol(c_divmagic, magic, sizeof(magic)));
+    sb_->err = (int*)arena.alloc(sizeof(int) * 4, err);
+    if (!sb_->err) return C2G_ERR_OOM;
+    sb_->owned.push_back(sb_->err);
+    C2G_CUDA(cudaMemset(sb_->err, 0, sizeof(int) * 4));
+    S.err = sb_->err;
+    sb_->counts = (unsigned long long*)arena.alloc(sizeof(unsigned long long) * 8, err);
+    if (!sb_->counts) return C2G_ERR_OOM;
+    sb_->owned.push_back(sb_->counts);
+    C2G_CUDA(cudaMemset(sb_->counts, 0, sizeof(unsigned long long) * 8));
+    // film
+    film_w_ = s.cfg.width;
+    film_h_ = s.cfg.height;
+    size_t npx = (size_t)film_w_ * film_h_;
+    sb_->film = (float4*)arena.alloc(npx * sizeof(float4), err);
+    if (!sb_->film) return C2G_ERR_OOM;
+    sb_->owned.push_back(sb_->film);
+    sb_->film_m2 = (float4*)arena.alloc(npx * sizeof(float4), err);
+    if (!sb_->film_m2) return C2G_ERR_OOM;
+    sb_->owned.push_back(sb_->film_m2);
+    C2G_CUDA(cudaMemset(sb_->film, 0, npx * sizeof(float4)));
+    C2G_CUDA(cudaMemset(sb_->film_m2, 0, npx * sizeof(float4)));
+    sb_->n_lights = S.n_lights;
+    // wave buffers depend on the light count: drop them
+    for (void* p : wb_->owned) arena.free(p);
+    wb_->owned.clear();
+    *wb_ = WaveBuffers();
+    return C2G_OK;
+}
+
+int GpuScene::film_clear(cudaStream_t st) {
+    size_t npx = (size_t)film_w_ * film_h_;
+    if (!sb_->film) return C2G_ERR_STATE;
+    if (cudaMemsetAsync(sb_->film, 0, npx * sizeof(float4), st) != cudaSuccess) return C2G_ERR_CUDA;
+    if (cudaMemsetAsync(sb_->film_m2, 0, npx * sizeof(float4), st) != cudaSuccess) return C2G_ERR_CUDA;
+    return C2G_OK;
+}
+
+int GpuScene::check_device_error(std::string& err) {
+    int h[4] = {0, 0, 0, 0};
+    if (!sb_->err) return C2G_OK;
+    C2G_CUDA(cudaMemcpy(h, sb_->err, sizeof(h), cudaMemcpyDeviceToHost));
+    if (h[0]) {
+        err = "device error word " + std::to_string(h[0]) + ((h[0] & DEVERR_STACK) ? " (traversal stack overflow)" : "") +
+              ((h[0] & DEVERR_QUEUE) ? " (queue overflow)" : "");
+        cudaMemset(sb_->err, 0, sizeof(int));
+        return C2G_ERR_DEVICE;
+    }
+    return C2G_OK;
+}
+
+int GpuScene::film_download(float* rgb_sum, float* weight, float* rgb_sumsq, std::string& err) {
+    size_t npx = (size_t)film_w_ * film_h_;
+    if (!sb_->film) { err = "no scene loaded"; return C2G_ERR_STATE; }
+    std::vector<float4> f(npx), m(npx);
+    C2G_CUDA(cudaMemcpy(f.data(), sb_->film, npx * sizeof(float4), cudaMemcpyDeviceToHost));
+    if (rgb_sumsq) C2G_CUDA(cudaMemcpy(m.data(), sb_->film_m2, npx * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < npx; i++) {
+        if (rgb_sum) { rgb_sum[3 * i] = f[i].x; rgb_sum[3 * i + 1] = f[i].y; rgb_sum[3 * i + 2] = f[i].z; }
+        if (weight) weight[i] = f[i].w;
+        if (rgb_sumsq) { rgb_sumsq[3 * i] = m[i].x; rgb_sumsq[3 * i + 1] = m[i].y; rgb_sumsq[3 * i + 2] = m[i].z; }
+    }
+    return C2G_OK;
+}
+
+int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_t st, DeviceArena& arena, std::string& err) {
+    if (!sb_->film) { err = "no scene loaded"; return C2G_ERR_STATE; }
+    if (p.width != film_w_ || p.height != film_h_) { err = "render size differs from the loaded film size"; return C2G_ERR_INVALID; }
+    if (p.max_depth <= 0 || p.sample_count < 0 || p.sample_begin < 0) { err = "invalid render parameters"; return C2G_ERR_INVALID; }
+    if (p.integrator != C2G_INTEGRATOR_PATH) { err = "integrator not available in this build"; return C2G_ERR_UNSUPPORTED; }
+    if (p.max_depth > 255) { err = "max_depth above 255"; return C2G_ERR_INVALID; }
+    DevScene S = sb_->S;
+    S.anyhit_clip = p.accel == C2G_ACCEL_BVH ? 1 : 0;
+    S.closest_box = p.accel == C2G_ACCEL_BVH ? 1 : 0;
+    S.seed = p.seed;
+    WaveArgs a{};
+    a.W = p.width;
+    a.H = p.height;
+    a.tiles_x = (p.width + 7) / 8;
+    int tiles_y = (p.height + 7) / 8;
+    a.nslots = a.tiles_x * tiles_y * 64;
+    a.max_depth = p.max_depth;
+    a.K = std::max(1, S.n_lights);
+    a.integrator = p.integrator;
+    // wave capacity: default 2^21 paths, at least one sample of every pixel
+    size_t want = p.wave_paths > 0 ? (size_t)p.wave_paths : (size_t)(1u << 21);
+    int spw = (int)std::max<size_t>(1, want / (size_t)a.nslots);
+    spw = std::min(spw, std::max(1, p.sample_count));
+    size_t P = (size_t)spw * a.nslots;
+    if (wb_->P < P || wb_->K != a.K) {
+        for (void* q : wb_->owned) arena.free(q);
+        wb_->owned.clear();
+        *wb_ = WaveBuffers();
+        auto A = [&](size_t bytes) -> void* {
+            void* q = arena.alloc(bytes, err);
+            if (q) wb_->owned.push_back(q);
+            return q;
+        };
+        size_t PK = P * (size_t)a.K;
+        bool ok = true;
+        for (int b = 0; b < 2 && ok; b++) {
+            ok = ok && (wb_->o[b] = (float4*)A(P * 16)) && (wb_->d[b] = (float4*)A(P * 16)) &&
+                 (wb_->beta[b] = (float4*)A(P * 16)) && (wb_->L[b] = (float4*)A(P * 16));
+        }
+        ok = ok && (wb_->hit = (float4*)A(P * 16)) && (wb_->acc = (int2*)A(P * 8)) && (wb_->out_L = (float4*)A(P * 16)) &&
+             (wb_->sh_o = (float4*)A(PK * 16)) && (wb_->sh_d = (float4*)A(PK * 16)) && (wb_->sh_c = (float4*)A(PK * 16)) &&
+             (wb_->mis_o = (float4*)A(PK * 16)) && (wb_->mis_d = (float4*)A(PK * 16)) && (wb_->mis_c = (float4*)A(PK * 16)) &&
+             (wb_->sh_list = (int*)A(PK * 4)) && (wb_->mis_list = (int*)A(PK * 4)) && (wb_->counters = (int*)A(64));
+        if (!ok) {
+            for (void* q : wb_->owned) arena.free(q);
+            wb_->owned.clear();
+            *wb_ = WaveBuffers();
+            return C2G_ERR_OOM;
+        }
+        wb_->P = P;
+        wb_->K = a.K;
+    }
+    WaveBuffers& w = *wb_;
+    const bool count = counting_;
+    unsigned long long* cnt = sb_->counts;
+    if (count) C2G_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 8, st));
+
+    static int g_raygen = 0, g_ext = 0, g_ext_c = 0, g_shade = 0, g_sh = 0, g_sh_c = 0, g_mis = 0, g_mis_c = 0, g_acc = 0, g_film = 0;
+    if (!g_raygen) {
+        g_raygen = grid_for((const void*)k_raygen, 256);
+        g_ext = grid_for((const void*)k_extend<false>, 128);
+        g_ext_c = grid_for((const void*)k_extend<true>, 128);
+        g_shade = grid_for((const void*)k_shade, 128);
+        g_sh = grid_for((const void*)k_shadow<false>, 128);
+        g_sh_c = grid_for((const void*)k_shadow<true>, 128);
+        g_mis = grid_for((const void*)k_mis<false>, 128);
+        g_mis_c = grid_for((const void*)k_mis<true>, 128);
+        g_acc = grid_for((const void*)k_accumulate, 256);
+        g_film = grid_for((const void*)k_film, 256);
+    }
+    cudaEvent_t ev0, ev1;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    cudaEventRecord(ev0, st);
+    int launches = 0, waves = 0;
+    int* C = w.counters;
+    for (int s0 = 0; s0 < p.sample_count; s0 += spw) {
+        a.wave_samples = std::min(spw, p.sample_count - s0);
+        a.sample0 = p.sample_begin + s0;
+        C2G_CUDA(cudaMemsetAsync(C, 0, 64, st));
+        PathRefs buf[2] = {{w.o[0], w.d[0], w.beta[0], w.L[0]}, {w.o[1], w.d[1], w.beta[1], w.L[1]}};
+        k_raygen<<<g_raygen, 256, 0, st>>>(S, a, buf[0], w.out_L, C + 0);
+        launches++;
+        int cur = 0;
+        for (int b = 0; b < p.max_depth; b++) {
+            int nxt = cur ^ 1;
+            if (count)
+                k_extend<true><<<g_ext_c, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3, cnt);
+            else
+                k_extend<false><<<g_ext, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3, cnt);
+            ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc};
+            k_shade<<<g_shade, 128, 0, st>>>(S, a, buf[cur], w.hit, C + cur, so);
+            if (count) {
+                k_shadow<true><<<g_sh_c, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
+                k_mis<true><<<g_mis_c, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_c, cnt);
+            } else {
+                k_shadow<false><<<g_sh, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
+                k_mis<false><<<g_mis, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_c, cnt);
+            }
+            k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.out_L, C + cur);
+            launches += 5;
+            cur = nxt;
+        }
+        k_film<<<g_film, 256, 0, st>>>(a, w.out_L, sb_->film, sb_->film_m2);
+        launches++;
+        waves++;
+    }
+    cudaEventRecord(ev1, st);
+    C2G_CUDA(cudaGetLastError());
+    C2G_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    stats_ = c2g_stats{};
+    stats_.seconds = ms * 1e-3;
+    stats_.paths = (double)p.width * p.height * p.sample_count;
+    stats_.kernel_launches = launches;
+    stats_.waves = waves;
+    if (count) {
+        unsigned long long h[8];
+        C2G_CUDA(cudaMemcpy(h, cnt, sizeof(h), cudaMemcpyDeviceToHost));
+        stats_.nodes_visited = (double)(h[0] + h[2]);
+        stats_.prims_tested = (double)(h[1] + h[3]);
+    }
+    return check_device_error(err);
+}
+
+int GpuScene::trace_rays_dev(int n, const float* o, const float* d, const float* tmin, const float* tmax, const int* ignore,
+                             int any_hit, int* obj, float* t, cudaStream_t st, std::string& err) {
+    if (!sb_->film) { err = "no scene loaded"; return C2G_ERR_STATE; }
+    if (n <= 0) return C2G_OK;
+    k_trace_rays<<<(n + 127) / 128, 128, 0, st>>>(sb_->S, n, o, d, tmin, tmax, ignore, any_hit, obj, t);
+    C2G_CUDA(cudaGetLastError());
+    return C2G_OK;
+}
+
+int GpuScene::halton(int width, int height, int n, const int* px, const int* py, const int* sample, int ndim, float* out,
+                     DeviceArena& arena, std::string& err) {
+    if (!sb_->S.perm) { err = "no scene loaded"; return C2G_ERR_STATE; }
+    if (n <= 0 || ndim <= 0) return C2G_OK;
+    HaltonParams hp = halton_params(width, height);
+    size_t bytes_i = (size_t)n * 4, bytes_o = (size_t)n * ndim * 4;
+    int* dpx = (int*)arena.alloc(bytes_i * 3, err);
+    float* dout = (float*)arena.alloc(bytes_o, err);
+    if (!dpx || !dout) { arena.free(dpx); arena.free(dout); return C2G_ERR_OOM; }
+    int rc = C2G_OK;
+    do {
+        if (cudaMemcpy(dpx, px, bytes_i, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(dpx + n, py, bytes_i, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(dpx + 2 * n, sample, bytes_i, cudaMemcpyHostToDevice) != cudaSuccess) { rc = C2G_ERR_CUDA; break; }
+        k_halton<<<(n + 127) / 128, 128>>>(sb_->S, hp, width, n, dpx, dpx + n, dpx + 2 * n, ndim, dout);
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(out, dout, bytes_o, cudaMemcpyDeviceToHost) != cudaSuccess) rc = C2G_ERR_CUDA;
+    } while (0);
+    if (rc) err = "halton query failed";
+    arena.free(dpx);
+    arena.free(dout);
+    return rc;
+}
+
+int GpuScene::camera_rays(int n, const float* pos2, float* o, float* d, DeviceArena& arena, std::string& err) {
+    if (!sb_->film) { err = "no scene loaded"; return C2G_ERR_STATE; }
+    if (n <= 0) return C2G_OK;
+    float* buf = (float*)arena.alloc((size_t)n * 8 * 4, err);
+    if (!buf) return C2G_ERR_OOM;
+    int rc = C2G_OK;
+    if (cudaMemcpy(buf, pos2, (size_t)n * 8, cudaMemcpyHostToDevice) != cudaSuccess) rc = C2G_ERR_CUDA;
+    if (!rc) {
+        k_camera<<<(n + 127) / 128, 128>>>(sb_->S.cam, n, buf, buf + 2 * n, buf + 5 * n);
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(o, buf + 2 * n, (size_t)n * 12, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(d, buf + 5 * n, (size_t)n * 12, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = C2G_ERR_CUDA;
+    }
+    if (rc) err = "camera query failed";
+    arena.free(buf);
+    return rc;
+}
+
+}  // namespace c2g

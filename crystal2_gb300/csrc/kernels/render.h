@@ -1,0 +1,67 @@
+// Host interface of the CUDA side: device scene upload, the wavefront renderer and the ray-query
+// kernels.  Implemented in render.cu; called by the C ABI (capi.cpp).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../c2g_types.h"
+#include "../../../include/c2g.h"
+
+namespace c2g {
+
+struct HostScene;
+struct RefTree;
+struct SahTree;
+
+// Device allocations owned by a context, with an optional cap.
+class DeviceArena {
+public:
+    explicit DeviceArena(size_t cap = 0) : cap_(cap) {}
+    ~DeviceArena();
+    // Returns nullptr (and sets err) when the cap would be exceeded or cudaMalloc fails.
+    void* alloc(size_t bytes, std::string& err);
+    void free(void* p);
+    void free_all();
+    size_t used() const { return used_; }
+    void set_cap(size_t c) { cap_ = c; }
+
+private:
+    struct Block { void* p; size_t n; };
+    std::vector<Block> blocks_;
+    size_t cap_ = 0, used_ = 0;
+};
+
+struct DeviceSceneBuffers;
+struct WaveBuffers;
+
+// Everything the kernels need for one loaded scene + its film.
+class GpuScene {
+public:
+    GpuScene();
+    ~GpuScene();
+    // Upload scene, tree and sampler tables.  Returns a C2G status; err holds the message.
+    int upload(const HostScene& s, int tree, const RefTree* ref, const SahTree* sah, DeviceArena& arena, std::string& err);
+    int render(const HostScene& s, const c2g_render_params& p, cudaStream_t st, DeviceArena& arena, std::string& err);
+    int film_clear(cudaStream_t st);
+    int film_download(float* rgb_sum, float* weight, float* rgb_sumsq, std::string& err);
+    int trace_rays_dev(int n, const float* o, const float* d, const float* tmin, const float* tmax, const int* ignore,
+                       int any_hit, int* obj, float* t, cudaStream_t st, std::string& err);
+    int halton(int width, int height, int n, const int* px, const int* py, const int* sample, int ndim, float* out,
+               DeviceArena& arena, std::string& err);
+    int camera_rays(int n, const float* pos2, float* o, float* d, DeviceArena& arena, std::string& err);
+    void set_counting(bool on) { counting_ = on; }
+    const c2g_stats& stats() const { return stats_; }
+    int check_device_error(std::string& err);
+
+private:
+    DeviceSceneBuffers* sb_;
+    WaveBuffers* wb_;
+    bool counting_ = false;
+    c2g_stats stats_{};
+    int film_w_ = 0, film_h_ = 0;
+};
+
+}  // namespace c2g

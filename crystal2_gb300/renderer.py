@@ -1,0 +1,235 @@
+"""Python mirror of the reference's render driver and integrator plug-in surface.
+
+``RayTracer(config, scene)`` follows ``RayTracer`` (src/Core/RayTracer.cpp:11-43): it loads the
+two JSON files, builds the scene, camera and integrator, renders into a frame buffer and writes
+``result.hdr``.  ``Integrator.load`` mirrors the string factory ``Integrator::LoadIntegrator``
+(src/Integrators/Integrator.cpp:14-47): "PathTracer" and "DirectLight" map to the GPU kernels,
+anything else raises ``ValueError`` like the reference's ``std::invalid_argument``.
+Every computation happens in ``libc2g.so`` on the GPU; nothing here computes pixels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import struct
+
+import numpy as np
+
+from . import _native as N
+
+
+class Context:
+    """Owns one ``c2g_ctx`` (device memory, stream, loaded scene)."""
+
+    def __init__(self, device: int = 0, mem_limit_bytes: int = 0, verbose: bool = False):
+        self._lib = N.load_library()
+        self._h = C.c_void_p()
+        opts = N.DeviceOpts(device, mem_limit_bytes, 1 if verbose else 0)
+        rc = self._lib.c2g_create(C.byref(self._h), C.byref(opts))
+        if rc != N.C2G_OK:
+            msg = self._lib.c2g_last_error(self._h).decode() if self._h else "create failed"
+            if self._h:
+                self._lib.c2g_destroy(self._h)
+                self._h = C.c_void_p()
+            raise N.C2GError(rc, msg)
+        self.host_only = device < 0
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self, rc: int) -> None:
+        if rc != N.C2G_OK:
+            raise N.C2GError(rc, self._lib.c2g_last_error(self._h).decode())
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.c2g_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- scene
+    def load(self, config_path: str, scene_path: str, tree: int = N.TREE_SAH) -> None:
+        self.check(self._lib.c2g_load_json(self._h, config_path.encode(), scene_path.encode(), tree))
+
+    def load_text(self, config_json: str, scene_json: str, tree: int = N.TREE_SAH) -> None:
+        self.check(self._lib.c2g_load_json_text(self._h, config_json.encode(), scene_json.encode(), tree))
+
+    def build_tree(self, tree: int) -> None:
+        self.check(self._lib.c2g_bvh_build(self._h, tree))
+
+    def render_params(self) -> N.RenderParams:
+        p = N.RenderParams()
+        self.check(self._lib.c2g_get_render_params(self._h, C.byref(p)))
+        return p
+
+    def num_objects(self) -> int:
+        return self._lib.c2g_num_objects(self._h)
+
+    def num_lights(self) -> int:
+        return self._lib.c2g_num_lights(self._h)
+
+    def bvh_order(self) -> np.ndarray:
+        n = self.num_objects()
+        out = np.zeros(n, np.int32)
+        m = self._lib.c2g_bvh_order(self._h, N.iptr(out), n)
+        if m < 0:
+            self.check(-m if m < 0 else m)
+        return out
+
+    def bvh_nodes(self):
+        tot = self._lib.c2g_bvh_nodes(self._h, None, None, None, 0)
+        if tot < 0:
+            self.check(-tot)
+        b = np.zeros((tot, 6), np.float32)
+        a = np.zeros((tot, 2), np.int32)
+        ax = np.zeros(tot, np.int32)
+        self._lib.c2g_bvh_nodes(self._h, N.fptr(b), N.iptr(a), N.iptr(ax), tot)
+        return b, a, ax
+
+    # ---- rendering
+    def render(self, params: N.RenderParams, stream: int | None = None) -> None:
+        self.check(self._lib.c2g_render(self._h, C.byref(params), C.c_void_p(stream) if stream else None))
+
+    def film_clear(self) -> None:
+        self.check(self._lib.c2g_film_clear(self._h, None))
+
+    def film(self):
+        p = self.render_params()
+        s = np.zeros((p.height, p.width, 3), np.float32)
+        w = np.zeros((p.height, p.width), np.float32)
+        self.check(self._lib.c2g_film_download(self._h, N.fptr(s), N.fptr(w)))
+        return s, w
+
+    def film_m2(self) -> np.ndarray:
+        p = self.render_params()
+        m = np.zeros((p.height, p.width, 3), np.float32)
+        self.check(self._lib.c2g_film_download_m2(self._h, N.fptr(m)))
+        return m
+
+    def image(self) -> np.ndarray:
+        p = self.render_params()
+        img = np.zeros((p.height, p.width, 3), np.float32)
+        self.check(self._lib.c2g_film_image(self._h, N.fptr(img)))
+        return img
+
+    def stats(self) -> N.Stats:
+        s = N.Stats()
+        self.check(self._lib.c2g_get_stats(self._h, C.byref(s)))
+        return s
+
+    def set_counting(self, on: bool) -> None:
+        self.check(self._lib.c2g_set_counting(self._h, 1 if on else 0))
+
+    # ---- ray queries
+    def trace_rays(self, o: np.ndarray, d: np.ndarray, any_hit: bool = False, tmin=None, tmax=None, ignore=None):
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        n = o.shape[0]
+        obj = np.zeros(n, np.int32)
+        t = None if any_hit else np.zeros(n, np.float32)
+        tmin = None if tmin is None else np.ascontiguousarray(tmin, np.float32)
+        tmax = None if tmax is None else np.ascontiguousarray(tmax, np.float32)
+        ignore = None if ignore is None else np.ascontiguousarray(ignore, np.int32)
+        self.check(self._lib.c2g_trace_rays(self._h, n, N.fptr(o), N.fptr(d), N.fptr(tmin), N.fptr(tmax),
+                                            N.iptr(ignore), 1 if any_hit else 0, N.iptr(obj), N.fptr(t)))
+        return (obj.astype(bool) if any_hit else (obj, t))
+
+    def halton(self, width, height, px, py, sample, ndim) -> np.ndarray:
+        px = np.ascontiguousarray(px, np.int32)
+        py = np.ascontiguousarray(py, np.int32)
+        sample = np.ascontiguousarray(sample, np.int32)
+        out = np.zeros((px.shape[0], ndim), np.float32)
+        self.check(self._lib.c2g_halton(self._h, width, height, px.shape[0], N.iptr(px), N.iptr(py), N.iptr(sample), ndim, N.fptr(out)))
+        return out
+
+    def camera_rays(self, pos2: np.ndarray):
+        pos2 = np.ascontiguousarray(pos2, np.float32)
+        n = pos2.shape[0]
+        o = np.zeros((n, 3), np.float32)
+        d = np.zeros((n, 3), np.float32)
+        self.check(self._lib.c2g_camera_rays(self._h, n, N.fptr(pos2), N.fptr(o), N.fptr(d)))
+        return o, d
+
+
+class Integrator:
+    """String factory of the integrators (Integrator::LoadIntegrator)."""
+
+    TYPES = {"PathTracer": N.INTEGRATOR_PATH, "DirectLight": N.INTEGRATOR_DIRECT, "GuidedPathTracer": N.INTEGRATOR_GUIDED}
+
+    def __init__(self, kind: int, depth: int):
+        self.kind = kind
+        self.depth = depth
+
+    @classmethod
+    def load(cls, config: dict) -> "Integrator":
+        node = config["Integrator"]
+        t = node["Type"]
+        if t not in cls.TYPES:
+            raise ValueError("Invalid Integrator Type!")
+        if node["Sampler"]["Type"] != "Halton":
+            raise ValueError(f"sampler {node['Sampler']['Type']} is not supported (Halton only)")
+        return cls(cls.TYPES[t], int(node["Depth"]))
+
+    def render(self, ctx: Context, sample_begin: int = 0, sample_count: int | None = None, wave_paths: int = 0) -> None:
+        """Integrator::Render(Scene*, Camera*, FrameBuffer*) on the context's loaded scene."""
+        p = ctx.render_params()
+        p.integrator = self.kind
+        p.max_depth = self.depth
+        p.sample_begin = sample_begin
+        p.sample_count = p.spp - sample_begin if sample_count is None else sample_count
+        p.wave_paths = wave_paths
+        ctx.render(p)
+
+
+class RayTracer:
+    """``RayTracer(config, scene)`` then ``trace()``; ``image()`` is GetImageDataRGB32F."""
+
+    def __init__(self, config_path: str, scene_path: str, device: int = 0, tree: int = N.TREE_SAH):
+        with open(config_path) as fh:
+            self.config = json.load(fh)
+        self.ctx = Context(device)
+        self.ctx.load(config_path, scene_path, tree)
+        self.integrator = Integrator.load(self.config)
+
+    def trace(self) -> float:
+        self.ctx.film_clear()
+        self.integrator.render(self.ctx)
+        return self.ctx.stats().seconds
+
+    def image(self) -> np.ndarray:
+        return self.ctx.image()
+
+    def write_hdr(self, path: str = "result.hdr") -> None:
+        write_hdr(path, self.image())
+
+
+def write_hdr(path: str, rgb: np.ndarray) -> None:
+    """Radiance RGBE file (flat, uncompressed scanlines) of an (H, W, 3) float image, top row first."""
+    rgb = np.nan_to_num(np.asarray(rgb, np.float32), nan=0.0, posinf=0.0, neginf=0.0)
+    h, w, _ = rgb.shape
+    m = rgb.max(axis=2)
+    e = np.zeros_like(m, dtype=np.int32)
+    mant, ex = np.frexp(m)
+    nz = m > 1e-32
+    e[nz] = ex[nz]
+    scale = np.where(nz, 256.0 / np.ldexp(1.0, e), 0.0)
+    out = np.zeros((h, w, 4), np.uint8)
+    out[..., :3] = np.clip(rgb * scale[..., None], 0, 255).astype(np.uint8)
+    out[..., 3] = np.where(nz, e + 128, 0).astype(np.uint8)
+    with open(path, "wb") as fh:
+        fh.write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n")
+        fh.write(f"-Y {h} +X {w}\n".encode())
+        fh.write(out.tobytes())

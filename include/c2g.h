@@ -1,0 +1,158 @@
+/*
+ * c2g.h - C ABI of the GB300 path-tracing hot path for Crystal2.
+ *
+ * The library replaces the subtree under crystal::Integrator::Render(Scene*, Camera*, FrameBuffer*)
+ * (src/Integrators/Integrator.h:8-18) of the reference renderer: the per-sample loop of
+ * SamplerIntegrator::Render (src/Integrators/SamplerIntegrator.cpp:17-72), the MIS path tracer
+ * PathTracingIntegrator::Evaluate (src/Integrators/PathTracingIntegrator.cpp:28-278), BVH traversal
+ * (src/Accelerators/BVH.cpp:56-154), shape intersection (src/Shapes/*.cpp), BSDF sampling and
+ * evaluation (src/BSDFs/**), light sampling (src/Lights/*.cpp) and film accumulation
+ * (src/Core/FrameBuffer.cpp:20-32).
+ *
+ * Conventions
+ *  - Every entry point returns an int status (C2G_OK == 0); no C++ exception crosses the ABI.
+ *    c2g_last_error() gives the message of the last failure on that context.
+ *  - The context owns all device memory. Caller buffers are borrowed for the duration of a call.
+ *  - Arrays are plain host pointers unless a name says `_dev` (device pointers, e.g. from
+ *    cudaMalloc or torch). Streams are `cudaStream_t` passed as void* (NULL = the context stream).
+ *  - One context per host thread; different contexts may be used concurrently.
+ */
+#ifndef C2G_H
+#define C2G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------- */
+#define C2G_OK 0
+#define C2G_ERR_INVALID 1   /* bad argument (std::invalid_argument in the reference factories) */
+#define C2G_ERR_IO 2        /* file missing or unreadable (JsonLoader.cpp:6-58, ObjLoader.cpp:96-116) */
+#define C2G_ERR_PARSE 3     /* malformed JSON / OBJ (SJson ParseError family) */
+#define C2G_ERR_CUDA 4      /* a CUDA runtime call failed */
+#define C2G_ERR_OOM 5       /* device allocation failed or exceeded the context's memory cap */
+#define C2G_ERR_DEVICE 6    /* a kernel reported an error word (stack/queue overflow, bounded-wait timeout) */
+#define C2G_ERR_STATE 7     /* call out of order (e.g. render before a scene is loaded) */
+#define C2G_ERR_UNSUPPORTED 8 /* feature the reference has but this library leaves out (textures, skybox) */
+
+/* ---- enumerations ------------------------------------------------------------------------ */
+/* Accelerator semantics (the reference's "Acceleration" key, Accelerator.cpp:6-25). */
+#define C2G_ACCEL_BVH 0     /* BVH semantics: per-object box test; shadow test clipped to the object box (BVH.cpp:110-154) */
+#define C2G_ACCEL_BRUTE 1   /* Brute semantics: no box tests; shadow test over [tMin, tMax] (Brute.cpp:19-55) */
+
+/* Tree actually traversed on the GPU (either gives BVH semantics). */
+#define C2G_TREE_REF_EQUAL_COUNT 0  /* bit-exact replica of BVH::_build with equal-count splits (BVH.cpp:156-188,269-279) */
+#define C2G_TREE_SAH 1              /* binned-SAH tree, compact node layout (performance) */
+
+/* Integrators (the reference's Integrator.Type, Integrator.cpp:14-47). */
+#define C2G_INTEGRATOR_PATH 0    /* "PathTracer" */
+#define C2G_INTEGRATOR_DIRECT 1  /* "DirectLight" */
+#define C2G_INTEGRATOR_GUIDED 2  /* "GuidedPathTracer": path tracer plus the learned directional proposal */
+
+/* Shape kinds of c2g_trace_rays outputs / scene objects. */
+#define C2G_SHAPE_TRIANGLE 0
+#define C2G_SHAPE_SPHERE 1
+#define C2G_SHAPE_DISK 2
+
+/* ---- plain structs ----------------------------------------------------------------------- */
+typedef struct c2g_ctx c2g_ctx;
+
+typedef struct {
+    int device;                 /* CUDA device ordinal; -1 = host-only context (scene parsing and tree
+                                   builds only; every device call returns C2G_ERR_STATE) */
+    size_t mem_limit_bytes;     /* 0 = no cap; else allocations beyond this fail with C2G_ERR_OOM */
+    int verbose;                /* print timings to stderr */
+} c2g_device_opts;
+
+typedef struct {
+    int width, height;          /* film size (ConfigInfo.Width/Height) */
+    int spp;                    /* samples per pixel (ConfigInfo.SamplesPerPixel) */
+    int max_depth;              /* Integrator.Depth */
+    int integrator;             /* C2G_INTEGRATOR_* */
+    int accel;                  /* C2G_ACCEL_* */
+    int sample_begin;           /* first sample index rendered by this call (progressive rendering) */
+    int sample_count;           /* number of samples rendered by this call (<= spp - sample_begin) */
+    int wave_paths;             /* paths in flight per wave (0 = automatic) */
+    uint64_t seed;              /* seed of the hash RNG used for Halton dims >= 100 */
+} c2g_render_params;
+
+typedef struct {
+    double seconds;             /* wall time of the last c2g_render (device, CUDA events) */
+    double paths;               /* camera paths traced by the last c2g_render */
+    double rays_closest;        /* closest-hit queries issued */
+    double rays_shadow;         /* any-hit queries issued */
+    double nodes_visited;       /* filled only when counting is enabled */
+    double prims_tested;        /* filled only when counting is enabled */
+    double kernel_ms[8];        /* per-kernel-kind device time: raygen, extend, shade, shadow, mis, accum, film, guide */
+    int kernel_launches;        /* kernels launched by the last c2g_render */
+    int waves;                  /* waves of the last c2g_render */
+} c2g_stats;
+
+/* ---- lifecycle ------------------------------------------------------------------------------ */
+int c2g_create(c2g_ctx** out, const c2g_device_opts* opts);
+void c2g_destroy(c2g_ctx* ctx);
+const char* c2g_last_error(const c2g_ctx* ctx);
+const char* c2g_version(void);
+
+/* ---- scene ---------------------------------------------------------------------------------- */
+/* Load the reference's two JSON files (config + scene) exactly as RayTracer's constructor does
+ * (src/Core/RayTracer.cpp:11-22): ConfigLoader keys, Scene::CreateScene (Scene.cpp:23-45),
+ * Camera::CreateCamera (Camera.cpp:7-22), Integrator/Sampler factories. The tree is built with
+ * `tree` (C2G_TREE_*). Relative OBJ paths resolve against the current directory, as fopen does
+ * in ObjLoader::load (ObjLoader.cpp:96-116). */
+int c2g_load_json(c2g_ctx* ctx, const char* config_path, const char* scene_path, int tree);
+/* Same, from in-memory JSON text. */
+int c2g_load_json_text(c2g_ctx* ctx, const char* config_json, const char* scene_json, int tree);
+/* Rebuild the acceleration structure of the loaded scene (BVH::Build, BVH.cpp:45-54). */
+int c2g_bvh_build(c2g_ctx* ctx, int tree);
+/* Render parameters implied by the loaded config (Width, Height, SamplesPerPixel, Depth ...). */
+int c2g_get_render_params(c2g_ctx* ctx, c2g_render_params* out);
+int c2g_num_objects(c2g_ctx* ctx);
+int c2g_num_lights(c2g_ctx* ctx);
+/* Object order after the reference equal-count build (BVH::_objects), as scene indices. */
+int c2g_bvh_order(c2g_ctx* ctx, int* order, int n);
+/* Reference-tree nodes 1..n (n returned): bounds (6 floats), ch0/ch1 or start/count, axis (-1 leaf). */
+int c2g_bvh_nodes(c2g_ctx* ctx, float* bounds, int* a, int* axis, int cap);
+
+/* ---- rendering ------------------------------------------------------------------------------ */
+/* Integrator::Render: trace samples [sample_begin, sample_begin + sample_count) of every pixel
+ * and add them to the device film (FrameBuffer::AddSample semantics: NaN/Inf -> 0, weight 1). */
+int c2g_render(c2g_ctx* ctx, const c2g_render_params* params, void* stream);
+int c2g_film_clear(c2g_ctx* ctx, void* stream);
+/* Per-pixel sums and weights, row y = sample-loop pixel y (not flipped). Either may be NULL. */
+int c2g_film_download(c2g_ctx* ctx, float* rgb_sum, float* weight);
+/* FrameBuffer::GetImageDataRGB32F (FrameBuffer.cpp:58-75): sum/weight, rows flipped. */
+int c2g_film_image(c2g_ctx* ctx, float* rgb);
+/* Per-pixel sum of squares of the samples (variance estimates for parity tests). */
+int c2g_film_download_m2(c2g_ctx* ctx, float* rgb_sumsq);
+int c2g_get_stats(c2g_ctx* ctx, c2g_stats* out);
+/* Count nodes visited / prims tested in the traversal kernels (slower; 0 = off). */
+int c2g_set_counting(c2g_ctx* ctx, int enable);
+
+/* ---- ray queries (Scene::Intersect / Scene::IntersectTest, Scene.cpp:50-59) ---------------- */
+/* Closest hit (any_hit = 0): obj = scene index of the hit object or -1, t = distance.
+ * Any hit (any_hit = 1): obj = 1 if occluded else 0 over [tmin, tmax], ignoring object ignore[i]
+ * (scene index or -1; the reference's ignoreShape). tmin/tmax/ignore may be NULL (0, inf, -1).
+ * Host pointers; the copies are part of the call. */
+int c2g_trace_rays(c2g_ctx* ctx, int n, const float* o, const float* d, const float* tmin,
+                   const float* tmax, const int* ignore, int any_hit, int* obj, float* t);
+/* Same over device pointers, on `stream`, without host synchronisation. */
+int c2g_trace_rays_dev(c2g_ctx* ctx, int n, const float* o_dev, const float* d_dev,
+                       const float* tmin_dev, const float* tmax_dev, const int* ignore_dev,
+                       int any_hit, int* obj_dev, float* t_dev, void* stream);
+
+/* ---- sampler / camera (HaltonSampler.cpp:118-291, PerspCamera.cpp:23-29) -------------------- */
+/* SampleValue(GetVectorIndexForSample(sample), dim) for n (pixel, sample) pairs and dims
+ * [0, ndim); film size width x height. Dims >= 100 come from the hash RNG. out: n * ndim. */
+int c2g_halton(c2g_ctx* ctx, int width, int height, int n, const int* px, const int* py,
+               const int* sample, int ndim, float* out);
+/* PerspCamera::GenerateRay for NDC points pos2 (n x 2) of the loaded camera. */
+int c2g_camera_rays(c2g_ctx* ctx, int n, const float* pos2, float* o, float* d);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* C2G_H */
