@@ -1,0 +1,357 @@
+#!/usr/bin/env python3
+"""Benchmark: Mpaths/s of the GPU MIS path tracer at 1080p on the many-material scene.
+
+Workload (the configuration the headline metric is quoted on): 400 subdivision-4 icospheres
+(2,048,000 triangles) on a jittered 20 x 20 grid over a 40 x 40 ground quad, five material families
+(GGX, anisotropic GGX, rough glass, mirror, diffuse), two area quads of radiance 20 plus a point light
+of intensity 50; 1920 x 1080, max depth 16, Halton sampler, BVH semantics, SAH tree.  The full
+render is 256 spp; one bench step renders `--spp-per-step` samples of every pixel (default 4, i.e.
+8.29 M camera paths), so 64 steps make the full render.
+
+Timing: W untimed warm-up steps, then K steps bracketed by a barrier and device synchronisation,
+timed with CUDA events on the stream the kernels run on (max over ranks).  The scene (~200 MB of
+BVH/prims) and the wave state (~1.7 GB) are far larger than the 129 MB L2, so no L2 flush is added.
+`e2e` is the same metric through the public C ABI per step: c2g_render (render parameters from the
+host) plus the film read back to host memory (c2g_film_download), wall-clock timed.
+
+Multi-GPU: the path does not exchange data; `--gpus N` runs N independent replicas (weak scaling),
+one process per GPU, rendering the same frame; value = all paths / max time.
+
+`--impl reference` times the reference renderer's own CPU code (compiled from its sources by
+oracle/build_ref.py; the oracle port when that library cannot be built) on the host cores, on a
+bounded sample of the same workload: rows of the 1080p frame at 1 spp per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {
+    "workload": "many_material_1080p",
+    "scene": "400 icospheres (subdiv 4, 5120 tris each) + 40x40 ground quad, 2,048,002 triangles",
+    "materials": "GGX U(0.05,0.8), aniso GGX U(0.05,0.6)^2, glass IOR 1.5 a=0.1, mirror, diffuse U(0.2,0.9)",
+    "lights": "2 area quads Le=20 (4 triangle lights) + point light flux 50*4pi",
+    "resolution": "1920x1080", "spp_full_render": 256, "max_depth": 16, "sampler": "Halton",
+    "tree": "SAH (binned, 2-wide compact nodes)", "accel_semantics": "BVH",
+}
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def make_scene(out_dir: str, spp: int, scale: float = 1.0):
+    from crystal2_gb300 import scenes
+    w, h = int(1920 * scale), int(1080 * scale)
+    return scenes.many_material(out_dir, width=w, height=h, spp=spp, depth=16, seed=2)
+
+
+def load_peaks() -> tuple[dict, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return json.load(fh), "of measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "of fallback"
+
+
+def load_traffic(kernel: str) -> float | None:
+    """DRAM bytes per launch of `kernel` on this workload from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "traffic_many_material_1080p.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        for ln in fh:
+            parts = ln.split()
+            if len(parts) >= 2 and parts[0] == kernel:
+                try:
+                    return float(parts[1])
+                except ValueError:
+                    return None
+    return None
+
+
+def cpu_baseline(cfg_dir: str, budget_s: float = 12.0, rows: int | None = None) -> dict:
+    """Reference CPU path on a bounded sample: rows of the 1080p frame at 1 spp."""
+    from oracle import bindings as B
+    cp, sp = make_scene(cfg_dir, spp=1)
+    kind = "reference"
+    try:
+        sc = B.ref_open(cp, sp)
+    except Exception:
+        kind = "port"
+        sc = B.oracle_open(cp, sp)
+    threads = min(16, os.cpu_count() or 1)
+    W, H = sc.W, sc.H
+    if rows is None:
+        y0 = H // 2 - 2
+        _, _, t = sc.render_region(0, y0, W, y0 + 4, threads=threads) if kind == "reference" else sc.render_region(0, y0, W, y0 + 4, threads=threads)
+        rows = int(max(4, min(H, budget_s / max(t, 1e-3) * 4)))
+    y0 = max(0, H // 2 - rows // 2)
+    y1 = min(H, y0 + rows)
+    _, _, t = sc.render_region(0, y0, W, y1, threads=threads)
+    paths = W * (y1 - y0)
+    return {"value": paths / t / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": kind, "seconds": t,
+            "sample": f"rows {y0}..{y1 - 1} of the 1920x1080 frame at 1 spp ({paths} paths), "
+                      f"{'reference PathTracingIntegrator::Evaluate compiled from source' if kind == 'reference' else 'oracle port'}, "
+                      f"{threads} threads", "rows": rows}
+
+
+def run_reference(args) -> None:
+    rank = _env_int("RANK", 0)
+    if rank != 0:
+        return
+    wdir = tempfile.mkdtemp(prefix="c2g_bench_ref_")
+    # calibrate the per-step sample so the whole run stays within a few minutes
+    steps, warm = args.steps, args.warmup
+    per_step = max(2.0, min(10.0, 150.0 / max(1, steps + warm)))
+    cal = cpu_baseline(wdir, budget_s=per_step)
+    vals = []
+    for i in range(warm + steps):
+        r = cpu_baseline(wdir, rows=cal["rows"])
+        if i >= warm:
+            vals.append(r["value"])
+    v = statistics.mean(vals)
+    line = {"metric": "Mpaths/s at 1080p (many-material scene, MIS path tracer)", "value": v, "unit": "Mpaths/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": 1e3 * cal["rows"] * 1920 / (v * 1e6),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scene generator)", "config": dict(WORKLOAD, parallelism="cpu threads"),
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "Mpaths/s", "cores": cal["cores"], "kind": cal["kind"], "sample": cal["sample"]},
+            "e2e": {"value": v, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    world = _env_int("WORLD_SIZE", 1)
+    rank = _env_int("RANK", 0)
+    local = _env_int("LOCAL_RANK", 0)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    from crystal2_gb300 import Context
+    from crystal2_gb300 import _native as N
+
+    wdir = tempfile.mkdtemp(prefix=f"c2g_bench_{rank}_")
+    spp_full = 256
+    cp, sp = make_scene(wdir, spp=spp_full, scale=args.scale)
+    ctx = Context(local)
+    t0 = time.time()
+    ctx.load(cp, sp, tree=N.TREE_SAH)
+    load_s = time.time() - t0
+    p = ctx.render_params()
+    sps = args.spp_per_step
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+
+    def step(i: int) -> None:
+        q = N.RenderParams()
+        C.memmove(C.addressof(q), C.addressof(p), C.sizeof(p))
+        q.sample_begin = (i * sps) % spp_full
+        q.sample_count = sps
+        ctx.render(q, stream=sh)
+
+    for i in range(args.warmup):
+        step(i)
+    # traversal counters (untimed): rays, nodes and prims per traversal kernel
+    ctx.set_counting(N.COUNT_TRAVERSAL)
+    step(0)
+    cst = ctx.stats()
+    counts = {k: (cst.rays[i], cst.nodes[i], cst.prims[i]) for i, k in ((N.K_EXTEND, "extend"), (N.K_SHADOW, "shadow"), (N.K_MIS, "mis"))}
+    # timed region (per-launch CUDA events on for the roofline)
+    ctx.set_counting(N.COUNT_TIMING)
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    kernel_ms = np.zeros(8)
+    kernel_n = np.zeros(8)
+    launches = 0
+    ev0.record(stream)
+    for i in range(args.steps):
+        step(args.warmup + i)
+        st = ctx.stats()
+        kernel_ms += np.array(st.kernel_ms[:])
+        kernel_n += np.array(st.kernel_count[:])
+        launches += st.kernel_launches
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    ctx.set_counting(0)
+    t_local = ms / 1e3
+    if dist:
+        tt = torch.tensor([t_local], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    else:
+        t_max = t_local
+    paths_rank = p.width * p.height * sps * args.steps
+    value = paths_rank * world / t_max / 1e6
+    # end to end through the C ABI with host buffers
+    film = np.zeros((p.height, p.width, 3), np.float32)
+    wgt = np.zeros((p.height, p.width), np.float32)
+    e2e_steps = max(2, min(args.steps, 4))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        q = N.RenderParams()
+        C.memmove(C.addressof(q), C.addressof(p), C.sizeof(p))
+        q.sample_begin = (i * sps) % spp_full
+        q.sample_count = sps
+        ctx.render(q)
+        ctx.check(ctx._lib.c2g_film_download(ctx.handle, N.fptr(film), N.fptr(wgt)))
+    e2e_t = time.perf_counter() - t0
+    if dist:
+        tt = torch.tensor([e2e_t], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+    e2e = paths_rank / args.steps * e2e_steps * world / e2e_t / 1e6
+    # roofline of the dominant kernel
+    peaks, peak_src = load_peaks()
+    names = N.KERNEL_NAMES
+    top = int(np.argmax(kernel_ms))
+    roof = None
+    trav = {N.K_EXTEND: "extend", N.K_SHADOW: "shadow", N.K_MIS: "mis"}
+    top_trav = max(trav, key=lambda k: kernel_ms[k])
+    rays, nodes, prims = counts[trav[top_trav]]
+    # algorithmic bytes: 32 B ray + 8 B hit + 32 B per node visited + 36 B per triangle tested
+    alg_bytes_per_step = 40.0 * rays + 32.0 * nodes + 36.0 * prims
+    launches_per_step = kernel_n[top_trav] / args.steps
+    avg_launch_s = kernel_ms[top_trav] / 1e3 / max(1, kernel_n[top_trav])
+    bytes_per_launch = alg_bytes_per_step / max(1, launches_per_step)
+    achieved = bytes_per_launch / max(avg_launch_s, 1e-12) / 1e9
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = load_traffic(names[top_trav])
+    roof = {"kernel": names[top_trav], "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+            "alg_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
+            "per_ray": {"nodes": nodes / max(1, rays), "prims": prims / max(1, rays)}}
+    share = {names[k]: float(kernel_ms[k] / max(1e-9, kernel_ms.sum())) for k in range(8) if kernel_n[k] > 0}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            cpu = cpu_baseline(tempfile.mkdtemp(prefix="c2g_cpu_"), budget_s=args.cpu_seconds)
+            cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "Mpaths/s", "cores": 0, "kind": "unavailable", "sample": str(e)[:200]}
+    if rank == 0:
+        line = {"metric": "Mpaths/s at 1080p (many-material scene, MIS path tracer)", "value": value, "unit": "Mpaths/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded scene generator; no dataset)",
+                "config": dict(WORKLOAD, spp_per_step=sps, paths_per_step=p.width * p.height * sps,
+                               parallelism=f"replicas x{world}" if world > 1 else "single GPU",
+                               l2="inputs larger than L2 (scene + wave state >> 129 MB); no flush",
+                               scene_load_s=round(load_s, 2), scale=args.scale),
+                "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": C.sizeof(p),
+                        "d2h_bytes_per_step": int(p.width * p.height * 16)},
+                "gpu_launches": int(launches), "roofline": roof, "kernel_share": share,
+                "traversal_per_step": {k: {"rays": v[0], "nodes": v[1], "prims": v[2]} for k, v in counts.items()},
+                "clocks": clk, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--spp-per-step", type=int, default=4)
+    ap.add_argument("--scale", type=float, default=1.0, help="film scale (1.0 = 1920x1080)")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -54,10 +54,16 @@ class RenderParams(C.Structure):
                 ("wave_paths", C.c_int), ("seed", C.c_uint64)]
 
 
+K_RAYGEN, K_EXTEND, K_SHADE, K_SHADOW, K_MIS, K_ACCUM, K_FILM, K_GUIDE = range(8)
+KERNEL_NAMES = ["raygen", "extend", "shade", "shadow", "mis", "accumulate", "film", "guide"]
+COUNT_TRAVERSAL = 1
+COUNT_TIMING = 2
+
+
 class Stats(C.Structure):
-    _fields_ = [("seconds", C.c_double), ("paths", C.c_double), ("rays_closest", C.c_double),
-                ("rays_shadow", C.c_double), ("nodes_visited", C.c_double), ("prims_tested", C.c_double),
-                ("kernel_ms", C.c_double * 8), ("kernel_launches", C.c_int), ("waves", C.c_int)]
+    _fields_ = [("seconds", C.c_double), ("paths", C.c_double), ("rays", C.c_double * 8), ("nodes", C.c_double * 8),
+                ("prims", C.c_double * 8), ("kernel_ms", C.c_double * 8), ("kernel_count", C.c_int * 8),
+                ("kernel_launches", C.c_int), ("waves", C.c_int)]
 
 
 _P = C.c_void_p

@@ -282,9 +282,9 @@ int c2g_get_stats(c2g_ctx* ctx, c2g_stats* out) {
     return C2G_OK;
 }
 
-int c2g_set_counting(c2g_ctx* ctx, int enable) {
+int c2g_set_counting(c2g_ctx* ctx, int flags) {
     if (!ctx) return C2G_ERR_INVALID;
-    ctx->gpu->set_counting(enable != 0);
+    ctx->gpu->set_counting(flags);
     return C2G_OK;
 }
 

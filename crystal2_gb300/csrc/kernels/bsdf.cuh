@@ -267,6 +267,57 @@ __device__ __forceinline__ float bxdf_pdf(const BxDF& b, float3 wo, float3 wi) {
     return 0.f;
 }
 
+// f and pdf of the BxDF at one (wo, wi) pair, sharing the half vector and D() between them.
+// Same values as bxdf_f / bxdf_pdf.
+__device__ __forceinline__ float3 mf_refl_f_pdf(const BxDF& b, float3 wo, float3 wi, float& pdf) {
+    float3 H = normalize(wo + wi);
+    float D = ndf_D(b, H);
+    pdf = D * fabsf(H.y) / (4 * dot(wo, H));
+    if (wo.y * wi.y < 0) return f3(0.f, 0.f, 0.f);
+    float F = bxdf_fresnel(b, fmaxf(0.f, dot(wo, H)));
+    float G = ndf_G(b, wo, wi);
+    return b.R * D * G * F / (4 * fmaxf(0.f, wi.y) * fmaxf(0.f, wo.y));
+}
+__device__ __forceinline__ float3 mf_trans_f_pdf(const BxDF& b, float3 wo, float3 wi, float& pdf) {
+    const float3 zero = f3(0.f, 0.f, 0.f);
+    if (wo.y * wi.y > 0) { pdf = 0.f; return zero; }
+    float eta = b.etaB / b.etaA;
+    float3 H = normalize(wo + wi * eta);
+    float D = ndf_D(b, H);  // D is even in H
+    float s = dot(wo, H) + eta * dot(wi, H);
+    pdf = D * fabsf(H.y) * (eta * eta * fabsf(dot(H, wi)) / sq(s));
+    if (wo.y == 0.f) return zero;
+    if (H.y < 0) H = -H;
+    float bot = sq(dot(wo, H) + eta * dot(wi, H));
+    float F = 1.f - bxdf_fresnel(b, fmaxf(0.f, dot(wo, H)));
+    float G = ndf_G(b, wo, wi);
+    return b.R * D * G * F * fabsf(dot(H, wo)) * fabsf(dot(H, wi)) / (bot * fmaxf(0.f, -wi.y) * fmaxf(0.f, wo.y));
+}
+__device__ __forceinline__ float3 fb_f_pdf(const BxDF& b, float3 wo, float3 wi, float& pdf) {
+    float3 H = normalize(wo + wi);
+    float D = ndf_D(b, H);
+    pdf = 0.5f * (fmaxf(0.f, wi.y) / kPiF + D * fabsf(H.y) / (4 * dot(wo, H)));
+    float cosI = fmaxf(0.f, wi.y), cosO = fmaxf(0.f, wo.y);
+    float k = (28.f / (23.f * kPiF));
+    float3 diffuse = k * b.R * (f3(1.f, 1.f, 1.f) - b.S) * (1.f - powf(1.f - 0.5f * cosO, 5.f)) * (1.f - powf(1.f - 0.5f * cosI, 5.f));
+    float cwh = dot(wi, H);
+    float sp = D / (4 * cwh * fmaxf(cosI, cosO));
+    float3 schlick = b.S + (f3(1.f, 1.f, 1.f) - b.S) * powf(1.f - cwh, 5.f);
+    return diffuse + sp * schlick;
+}
+__device__ __forceinline__ float3 bxdf_f_pdf(const BxDF& b, float3 wo, float3 wi, float& pdf) {
+    switch (b.mtype) {
+        case MAT_DIFFUSE: pdf = fmaxf(0.f, wi.y) / kPiF; return b.R / kPiF;
+        case MAT_MICRO_GGX:
+        case MAT_MICRO_BECKMANN: return mf_refl_f_pdf(b, wo, wi, pdf);
+        case MAT_GLASS_ROUGH: return (wo.y * wi.y < 0) ? mf_trans_f_pdf(b, wo, wi, pdf) : mf_refl_f_pdf(b, wo, wi, pdf);
+        case MAT_PLASTIC_GGX:
+        case MAT_PLASTIC_BECKMANN: return fb_f_pdf(b, wo, wi, pdf);
+    }
+    pdf = 0.f;
+    return f3(0.f, 0.f, 0.f);
+}
+
 // NextCosineUnitHemiSphere (Utils.h:114-123)
 __device__ __forceinline__ float3 cosine_hemisphere(float2 u, float& pdf) {
     float r = sqrtf(u.x);
@@ -377,6 +428,23 @@ __device__ __forceinline__ float bsdf_pdf(const BxDF& b, const Frame& fr, float3
     if ((matches(b.flags, flags) && refl && (b.flags & BXDF_REFLECTION)) || (!refl && (b.flags & BXDF_TRANSMISSION)))
         return bxdf_pdf(b, wo, wi);
     return 0.f;
+}
+
+// BSDF::DistributionFunction and BSDF::Pdf(flags) of one direction pair in one pass.
+__device__ __forceinline__ float3 bsdf_f_pdf(const BxDF& b, const Frame& fr, float3 wo_w, float3 wi_w, int flags, float& pdf) {
+    float3 wo = to_local(fr, wo_w), wi = to_local(fr, wi_w);
+    bool refl = wi.y * wo.y > 0;
+    bool fcond = (refl && (b.flags & BXDF_REFLECTION)) || (!refl && (b.flags & BXDF_TRANSMISSION));
+    bool pcond = (matches(b.flags, flags) && refl && (b.flags & BXDF_REFLECTION)) || (!refl && (b.flags & BXDF_TRANSMISSION));
+    pdf = 0.f;
+    float3 f = f3(0.f, 0.f, 0.f);
+    if (fcond || pcond) {
+        float p;
+        float3 v = bxdf_f_pdf(b, wo, wi, p);
+        if (fcond) f = v;
+        if (pcond) pdf = p;
+    }
+    return f;
 }
 
 // Returns f; wi_w, pdf, stype written when the BxDF matches `flags`.  ok = false when the BSDF

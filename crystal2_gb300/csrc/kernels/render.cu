@@ -88,6 +88,7 @@ struct WaveBuffers {
     float4* mis_o = nullptr;
     float4* mis_d = nullptr;
     float4* mis_c = nullptr;
+    float4* mis_hit = nullptr;
     int* sh_list = nullptr;
     int* mis_list = nullptr;
     int* counters = nullptr;  // [0],[1] path queues, [2] shadow, [3] mis
@@ -178,19 +179,28 @@ __global__ void k_raygen(DevScene S, WaveArgs a, PathRefs out, float4* out_L, in
 }
 
 // ---- extend: closest hit of each queued path ray ------------------------------------------------
+// Per-kernel-kind traversal counters: cnt[3 * kind + {0: rays, 1: nodes, 2: prims}].
+__device__ __forceinline__ void flush_counts(unsigned long long* cnt, int kind, unsigned rays, const TraceCounters& tc) {
+    warp_count(cnt + 3 * kind + 0, rays);
+    warp_count(cnt + 3 * kind + 1, tc.nodes);
+    warp_count(cnt + 3 * kind + 2, tc.prims);
+}
+
 template <bool COUNT>
 __global__ void k_extend(DevScene S, const float4* __restrict__ qo, const float4* __restrict__ qd, float4* hit,
                          const int* qcount, int* zero_a, int* zero_b, int* zero_c, unsigned long long* cnt) {
     if (blockIdx.x == 0 && threadIdx.x == 0) { *zero_a = 0; *zero_b = 0; *zero_c = 0; }
     const int n = *qcount;
     const int stride = gridDim.x * blockDim.x;
+    TraceCounters tc{0, 0};
+    unsigned rays = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         float4 o = qo[i], d = qd[i];
-        TraceCounters tc{0, 0};
         Hit h = trace_closest<COUNT>(S, f3(o), f3(d), &tc);
         hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.obj));
-        if (COUNT) { atomicAdd(cnt + 0, (unsigned long long)tc.nodes); atomicAdd(cnt + 1, (unsigned long long)tc.prims); }
+        rays++;
     }
+    if (COUNT) flush_counts(cnt, C2G_K_EXTEND, rays, tc);
 }
 
 // ---- shade ---------------------------------------------------------------------------------------
@@ -202,6 +212,7 @@ struct ShadeOut {
     int *sh_list, *mis_list;
     int *sh_count, *mis_count;
     int2* acc;
+    float4* mis_hit;   // per path slot: emitted radiance reaching the MIS ray, light index in w
 };
 
 __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs cur, const float4* __restrict__ hits,
@@ -238,18 +249,23 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
         BxDF bx;
         Frame fr;
         float3 wo = -rd;
+        const bool direct = a.integrator == C2G_INTEGRATOR_DIRECT;
         if (alive) {
             make_surface(S, ro, rd, h, s);
-            if (light_path && s.light >= 0) {
+            // DirectLightingIntegrator adds emission at every hit (DirectLightingIntegrator.cpp:40-41)
+            if ((light_path || direct) && s.light >= 0) {
                 const Light& Lg = S.lights[s.light];
                 float3 n_actual = s.front ? s.N : -s.N;
                 L = L + beta * area_Le(Lg, n_actual, -rd);
             }
             if (s.mat < 0) {
-                // no BSDF: continue straight through (PathTracingIntegrator.cpp:64-68)
-                next_o = spawn_origin(s, rd);
-                next_d = rd;
-                cont = true;
+                // no BSDF: continue straight through (PathTracingIntegrator.cpp:64-68); the direct
+                // lighting integrator stops at an emitter instead (DirectLightingIntegrator.cpp:48-55)
+                if (!(direct && s.light >= 0)) {
+                    next_o = spawn_origin(s, rd);
+                    next_d = rd;
+                    cont = true;
+                }
             } else {
                 bx = make_bxdf(S.mats[s.mat], s.front);
                 fr.T = s.dpdu; fr.N = s.N; fr.B = s.dpdv;
@@ -257,19 +273,41 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
             }
         }
         // ---- next-event estimation: UniformSampleAllLights (PathTracingIntegrator.cpp:175-186)
+        // Every material builds one BxDF, so the BSDF sample of EsimateDirect's second half
+        // (:229-238) ignores its 1D sample and uses the 2D sample shared by all lights: it is the
+        // same direction for every light.  It is drawn once here and its ray traced once (k_mis);
+        // the per-light MIS weights and the "hit entity carries this light" test are unchanged.
+        // Specular BxDFs give f = 0 and match no non-specular sample, so they skip the light loop.
         float2 uL = make_float2(0, 0), uB = make_float2(0, 0);
+        const int nsflags = BXDF_ALL & ~BXDF_SPECULAR;
+        bool nee_work = false, mis_ok = false, any_mis = false;
+        float3 f2 = f3(0.f, 0.f, 0.f), wi2 = f3(0.f, 0.f, 0.f);
+        float pdf_b2 = 0.f;
         if (do_nee) {
             uL = make_float2(halton_sample(S, vidx, dim, pixel, sample), halton_sample(S, vidx, dim + 1, pixel, sample));
             uB = make_float2(halton_sample(S, vidx, dim + 2, pixel, sample), halton_sample(S, vidx, dim + 3, pixel, sample));
             dim += 4;
+            int n_area = 0;
+            for (int l = 0; l < S.n_lights; l++) {
+                const Light& Lg = S.lights[l];
+                if (Lg.flux_zero == 0.f && (direct || l != s.light) && Lg.type != LIGHT_POINT) n_area++;
+            }
+            dim += n_area;  // one (unused) 1D sample per eligible non-delta light
+            nee_work = (bx.flags & BXDF_SPECULAR) == 0;
+            if (nee_work && n_area > 0) {
+                int stype = 0;
+                f2 = bsdf_sample(bx, fr, 0.f, uB, wo, wi2, pdf_b2, nsflags, stype, mis_ok);
+                if (mis_ok) f2 = f2 * fmaxf(0.f, dot(s.N, wi2));
+            }
         }
-        const int nsflags = BXDF_ALL & ~BXDF_SPECULAR;
         for (int l = 0; l < K; l++) {
-            bool sh_valid = false, mis_valid = false;
-            float4 sh_o4, sh_d4, sh_c4 = make_float4(0, 0, 0, 0), mis_o4, mis_d4, mis_c4 = make_float4(0, 0, 0, 0);
-            if (do_nee && l < S.n_lights) {
+            bool sh_valid = false;
+            float4 sh_o4, sh_d4, sh_c4 = make_float4(0, 0, 0, 0), mis_c4 = make_float4(0, 0, 0, 0);
+            if (nee_work && l < S.n_lights) {
                 const Light Lg = S.lights[l];
-                bool eligible = !(Lg.flux_zero != 0.f) && l != s.light;
+                // the path tracer skips the hit's own light (PathTracingIntegrator.cpp:182), the direct
+                // lighting integrator does not (DirectLightingIntegrator.cpp:71)
+                bool eligible = !(Lg.flux_zero != 0.f) && (direct || l != s.light);
                 if (eligible) {
                     // light-sampling half (EsimateDirect, :195-227)
                     float3 lpos;
@@ -277,8 +315,8 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                     float3 Li = light_sample_li(S, Lg, s.pos, s.N, uL, lpos, pdf_l);
                     float3 wi = normalize(lpos - s.pos);
                     if (pdf_l != 0.f && !is_zero(Li)) {
-                        float3 f = bsdf_f(bx, fr, wo, wi) * fmaxf(0.f, dot(s.N, wi));
-                        float pdf_b = bsdf_pdf(bx, fr, wo, wi, nsflags);
+                        float pdf_b;
+                        float3 f = bsdf_f_pdf(bx, fr, wo, wi, nsflags, pdf_b) * fmaxf(0.f, dot(s.N, wi));
                         if (!is_zero(f)) {
                             bool back = dot(lpos - s.pos, s.N) < 0;
                             float3 org = s.pos + (back ? -s.N : s.N) * kSpawnEps;
@@ -293,32 +331,13 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                             sh_c4 = make_float4(c.x, c.y, c.z, 0.f);
                         }
                     }
-                    // BSDF-sampling half (:229-270)
-                    if (Lg.type != LIGHT_POINT) {
-                        float u1 = halton_sample(S, vidx, dim, pixel, sample);
-                        dim += 1;
-                        float3 wi2 = f3(0.f, 0.f, 0.f);
-                        float pdf_b2 = 0.f;
-                        int stype = 0;
-                        bool ok;
-                        float3 f = bsdf_sample(bx, fr, u1, uB, wo, wi2, pdf_b2, nsflags, stype, ok);
-                        if (ok) {
-                            float weight = 1.f;
-                            bool good = true;
-                            if (!(stype & BXDF_SPECULAR)) {
-                                f = f * fmaxf(0.f, dot(s.N, wi2));
-                                float pdf_l2 = light_pdf(S, Lg, s.pos, s.N, wi2);
-                                if (pdf_l2 == 0.f) good = false;
-                                else weight = power_heuristic(pdf_b2, pdf_l2);
-                            }
-                            if (good) {
-                                float3 org = spawn_origin(s, wi2);
-                                float3 m = beta * (f * weight / pdf_b2);
-                                mis_valid = true;
-                                mis_o4 = make_float4(org.x, org.y, org.z, __int_as_float(l));
-                                mis_d4 = make_float4(wi2.x, wi2.y, wi2.z, 0.f);
-                                mis_c4 = make_float4(m.x, m.y, m.z, 0.f);
-                            }
+                    // BSDF-sampling half (:229-270): weight for this light of the shared sample
+                    if (mis_ok && Lg.type != LIGHT_POINT) {
+                        float pdf_l2 = light_pdf(S, Lg, s.pos, s.N, wi2);
+                        if (pdf_l2 != 0.f) {
+                            float3 m = beta * (f2 * power_heuristic(pdf_b2, pdf_l2) / pdf_b2);
+                            mis_c4 = make_float4(m.x, m.y, m.z, 0.f);
+                            any_mis = true;
                         }
                     }
                 }
@@ -328,15 +347,23 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                 out.sh_c[e] = sh_c4;
                 out.mis_c[e] = mis_c4;
                 if (sh_valid) { out.sh_o[e] = sh_o4; out.sh_d[e] = sh_d4; }
-                if (mis_valid) { out.mis_o[e] = mis_o4; out.mis_d[e] = mis_d4; }
             }
             int js = warp_append(out.sh_count, sh_valid);
             if (sh_valid) out.sh_list[js] = e;
-            int jm = warp_append(out.mis_count, mis_valid);
-            if (mis_valid) out.mis_list[jm] = e;
         }
-        // ---- continuation: BSDF sample (PathTracingIntegrator.cpp:73-102)
-        if (do_nee) {
+        {
+            // one MIS ray per path (closest hit; k_mis records which light, if any, it reaches)
+            int jm = warp_append(out.mis_count, any_mis);
+            if (any_mis) {
+                float3 org = spawn_origin(s, wi2);
+                out.mis_list[jm] = i;
+                out.mis_o[i] = make_float4(org.x, org.y, org.z, 0.f);
+                out.mis_d[i] = make_float4(wi2.x, wi2.y, wi2.z, 0.f);
+            }
+            if (do_nee) out.mis_hit[i] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+        }
+        // ---- continuation: BSDF sample (PathTracingIntegrator.cpp:73-102); none for direct lighting
+        if (do_nee && !direct) {
             // GCC evaluates SampleDirection(Get1D(), Get2D(), ...) right to left: Get2D first.
             float2 u2 = make_float2(halton_sample(S, vidx, dim, pixel, sample), halton_sample(S, vidx, dim + 1, pixel, sample));
             float u1 = halton_sample(S, vidx, dim + 2, pixel, sample);
@@ -363,7 +390,9 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                 }
             }
         }
-        if (cont && bounce + 1 >= a.max_depth) cont = false;
+        // Depth limit.  Direct lighting only re-enters at the same level through pass-through
+        // surfaces (DirectLightingIntegrator.cpp:54); the 8-bit hop counter bounds that walk.
+        if (cont && (direct ? bounce + 1 >= 255 : bounce + 1 >= a.max_depth)) cont = false;
         // ---- enqueue the continuation; finished paths keep L in place for `accumulate`
         int j = warp_append(out.nxt_count, cont);
         if (valid) {
@@ -386,58 +415,65 @@ __global__ void k_shadow(DevScene S, const int* __restrict__ list, const int* co
                          const float4* __restrict__ sd, float4* sc, unsigned long long* cnt) {
     const int n = *count;
     const int stride = gridDim.x * blockDim.x;
+    TraceCounters tc{0, 0};
+    unsigned rays = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         int e = list[i];
         float4 o = so[e], d = sd[e];
-        TraceCounters tc{0, 0};
         bool occ = trace_any<COUNT>(S, f3(o), f3(d), 0.f, d.w, __float_as_int(o.w), &tc);
         if (occ) sc[e] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (COUNT) { atomicAdd(cnt + 2, (unsigned long long)tc.nodes); atomicAdd(cnt + 3, (unsigned long long)tc.prims); }
+        rays++;
     }
+    if (COUNT) flush_counts(cnt, C2G_K_SHADOW, rays, tc);
 }
 
-// ---- mis: closest hit of NEE BSDF samples; radiance only if the hit emitter is the sampled light --
+// ---- mis: closest hit of the NEE BSDF sample; records the emitter it reaches ---------------------
 template <bool COUNT>
 __global__ void k_mis(DevScene S, const int* __restrict__ list, const int* count, const float4* __restrict__ mo,
-                      const float4* __restrict__ md, float4* mc, unsigned long long* cnt) {
+                      const float4* __restrict__ md, float4* mis_hit, unsigned long long* cnt) {
     const int n = *count;
     const int stride = gridDim.x * blockDim.x;
+    TraceCounters tc{0, 0};
+    unsigned rays = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        int e = list[i];
-        float4 o = mo[e], d = md[e];
-        int l = __float_as_int(o.w);
-        TraceCounters tc{0, 0};
+        int slot = list[i];
+        float4 o = mo[slot], d = md[slot];
         Hit h = trace_closest<COUNT>(S, f3(o), f3(d), &tc);
-        float3 res = f3(0.f, 0.f, 0.f);
+        rays++;
+        float3 Le = f3(0.f, 0.f, 0.f);
+        int light = -1;
         if (h.obj >= 0) {
             const ObjInfo oi = S.objs[h.obj];
-            if (oi.light == l) {
+            if (oi.light >= 0) {
                 Surface s;
                 make_surface(S, f3(o), f3(d), h, s);
                 float3 n_actual = s.front ? s.N : -s.N;
-                float3 Le = area_Le(S.lights[l], n_actual, -f3(d));
-                float4 m = mc[e];
-                res = f3(m) * Le;
+                Le = area_Le(S.lights[oi.light], n_actual, -f3(d));
+                light = oi.light;
             }
         }
         // no hit: Light::Le of an area light is zero (Light.h:52)
-        mc[e] = make_float4(res.x, res.y, res.z, 0.f);
-        if (COUNT) { atomicAdd(cnt + 0, (unsigned long long)tc.nodes); atomicAdd(cnt + 1, (unsigned long long)tc.prims); }
+        mis_hit[slot] = make_float4(Le.x, Le.y, Le.z, __int_as_float(light));
     }
+    if (COUNT) flush_counts(cnt, C2G_K_MIS, rays, tc);
 }
 
 // ---- accumulate ------------------------------------------------------------------------------------
 __global__ void k_accumulate(WaveArgs a, PathRefs cur, PathRefs nxt, const int2* __restrict__ acc, const float4* __restrict__ sc,
-                             const float4* __restrict__ mc, float4* out_L, const int* qcount) {
+                             const float4* __restrict__ mc, const float4* __restrict__ mis_hit, float4* out_L, const int* qcount) {
     const int n = *qcount;
     const int stride = gridDim.x * blockDim.x;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         int2 ac = acc[i];
         float3 direct = f3(0.f, 0.f, 0.f);
         if (ac.y) {
+            float4 mh = mis_hit[i];
+            int hl = __float_as_int(mh.w);
             for (int l = 0; l < a.K; l++) {
-                float4 s = sc[i * a.K + l], m = mc[i * a.K + l];
-                direct = direct + (f3(s) + f3(m));
+                float4 s = sc[i * a.K + l];
+                float3 m = f3(0.f, 0.f, 0.f);
+                if (l == hl) m = f3(mc[i * a.K + l]) * f3(mh);
+                direct = direct + (f3(s) + m);
             }
         }
         if (ac.x >= 0) {
@@ -614,10 +650,10 @@ int GpuScene::upload(const HostScene& s, int tree, const RefTree* ref, const Sah
     sb_->owned.push_back(sb_->err);
     C2G_CUDA(cudaMemset(sb_->err, 0, sizeof(int) * 4));
     S.err = sb_->err;
-    sb_->counts = (unsigned long long*)arena.alloc(sizeof(unsigned long long) * 8, err);
+    sb_->counts = (unsigned long long*)arena.alloc(sizeof(unsigned long long) * 24, err);
     if (!sb_->counts) return C2G_ERR_OOM;
     sb_->owned.push_back(sb_->counts);
-    C2G_CUDA(cudaMemset(sb_->counts, 0, sizeof(unsigned long long) * 8));
+    C2G_CUDA(cudaMemset(sb_->counts, 0, sizeof(unsigned long long) * 24));
     // film
     film_w_ = s.cfg.width;
     film_h_ = s.cfg.height;
@@ -676,8 +712,11 @@ int GpuScene::film_download(float* rgb_sum, float* weight, float* rgb_sumsq, std
 int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_t st, DeviceArena& arena, std::string& err) {
     if (!sb_->film) { err = "no scene loaded"; return C2G_ERR_STATE; }
     if (p.width != film_w_ || p.height != film_h_) { err = "render size differs from the loaded film size"; return C2G_ERR_INVALID; }
-    if (p.max_depth <= 0 || p.sample_count < 0 || p.sample_begin < 0) { err = "invalid render parameters"; return C2G_ERR_INVALID; }
-    if (p.integrator != C2G_INTEGRATOR_PATH) { err = "integrator not available in this build"; return C2G_ERR_UNSUPPORTED; }
+    if (p.max_depth < 0 || p.sample_count < 0 || p.sample_begin < 0) { err = "invalid render parameters"; return C2G_ERR_INVALID; }
+    if (p.integrator != C2G_INTEGRATOR_PATH && p.integrator != C2G_INTEGRATOR_DIRECT) {
+        err = "integrator not available in this build";
+        return C2G_ERR_UNSUPPORTED;
+    }
     if (p.max_depth > 255) { err = "max_depth above 255"; return C2G_ERR_INVALID; }
     DevScene S = sb_->S;
     S.anyhit_clip = p.accel == C2G_ACCEL_BVH ? 1 : 0;
@@ -714,8 +753,9 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         }
         ok = ok && (wb_->hit = (float4*)A(P * 16)) && (wb_->acc = (int2*)A(P * 8)) && (wb_->out_L = (float4*)A(P * 16)) &&
              (wb_->sh_o = (float4*)A(PK * 16)) && (wb_->sh_d = (float4*)A(PK * 16)) && (wb_->sh_c = (float4*)A(PK * 16)) &&
-             (wb_->mis_o = (float4*)A(PK * 16)) && (wb_->mis_d = (float4*)A(PK * 16)) && (wb_->mis_c = (float4*)A(PK * 16)) &&
-             (wb_->sh_list = (int*)A(PK * 4)) && (wb_->mis_list = (int*)A(PK * 4)) && (wb_->counters = (int*)A(64));
+             (wb_->mis_o = (float4*)A(P * 16)) && (wb_->mis_d = (float4*)A(P * 16)) && (wb_->mis_c = (float4*)A(PK * 16)) &&
+             (wb_->mis_hit = (float4*)A(P * 16)) && (wb_->sh_list = (int*)A(PK * 4)) && (wb_->mis_list = (int*)A(P * 4)) &&
+             (wb_->counters = (int*)A(64));
         if (!ok) {
             for (void* q : wb_->owned) arena.free(q);
             wb_->owned.clear();
@@ -726,9 +766,10 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         wb_->K = a.K;
     }
     WaveBuffers& w = *wb_;
-    const bool count = counting_;
+    const bool count = (counting_ & C2G_COUNT_TRAVERSAL) != 0;
+    const bool timing = (counting_ & C2G_COUNT_TIMING) != 0;
     unsigned long long* cnt = sb_->counts;
-    if (count) C2G_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 8, st));
+    if (count) C2G_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 24, st));
 
     static int g_raygen = 0, g_ext = 0, g_ext_c = 0, g_shade = 0, g_sh = 0, g_sh_c = 0, g_mis = 0, g_mis_c = 0, g_acc = 0, g_film = 0;
     if (!g_raygen) {
@@ -743,6 +784,28 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         g_acc = grid_for((const void*)k_accumulate, 256);
         g_film = grid_for((const void*)k_film, 256);
     }
+    // per-launch events (timing mode): a pool reused across calls
+    struct Ev { cudaEvent_t a, b; int kind; };
+    static std::vector<Ev> pool;
+    size_t used = 0;
+    int kcount[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    auto begin = [&](int kind) {
+        kcount[kind]++;
+        if (!timing) return;
+        if (used == pool.size()) {
+            Ev e{};
+            cudaEventCreate(&e.a);
+            cudaEventCreate(&e.b);
+            pool.push_back(e);
+        }
+        pool[used].kind = kind;
+        cudaEventRecord(pool[used].a, st);
+    };
+    auto end = [&]() {
+        if (!timing) return;
+        cudaEventRecord(pool[used].b, st);
+        used++;
+    };
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
@@ -754,30 +817,40 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         a.sample0 = p.sample_begin + s0;
         C2G_CUDA(cudaMemsetAsync(C, 0, 64, st));
         PathRefs buf[2] = {{w.o[0], w.d[0], w.beta[0], w.L[0]}, {w.o[1], w.d[1], w.beta[1], w.L[1]}};
+        begin(C2G_K_RAYGEN);
         k_raygen<<<g_raygen, 256, 0, st>>>(S, a, buf[0], w.out_L, C + 0);
-        launches++;
+        end();
         int cur = 0;
         for (int b = 0; b < p.max_depth; b++) {
             int nxt = cur ^ 1;
+            begin(C2G_K_EXTEND);
             if (count)
                 k_extend<true><<<g_ext_c, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3, cnt);
             else
                 k_extend<false><<<g_ext, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3, cnt);
-            ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc};
+            end();
+            ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc, w.mis_hit};
+            begin(C2G_K_SHADE);
             k_shade<<<g_shade, 128, 0, st>>>(S, a, buf[cur], w.hit, C + cur, so);
-            if (count) {
-                k_shadow<true><<<g_sh_c, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
-                k_mis<true><<<g_mis_c, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_c, cnt);
-            } else {
-                k_shadow<false><<<g_sh, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
-                k_mis<false><<<g_mis, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_c, cnt);
-            }
-            k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.out_L, C + cur);
+            end();
+            begin(C2G_K_SHADOW);
+            if (count) k_shadow<true><<<g_sh_c, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
+            else k_shadow<false><<<g_sh, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
+            end();
+            begin(C2G_K_MIS);
+            if (count) k_mis<true><<<g_mis_c, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
+            else k_mis<false><<<g_mis, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
+            end();
+            begin(C2G_K_ACCUM);
+            k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.mis_hit, w.out_L, C + cur);
+            end();
             launches += 5;
             cur = nxt;
         }
+        begin(C2G_K_FILM);
         k_film<<<g_film, 256, 0, st>>>(a, w.out_L, sb_->film, sb_->film_m2);
-        launches++;
+        end();
+        launches += 2;
         waves++;
     }
     cudaEventRecord(ev1, st);
@@ -792,11 +865,20 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
     stats_.paths = (double)p.width * p.height * p.sample_count;
     stats_.kernel_launches = launches;
     stats_.waves = waves;
+    for (int k = 0; k < 8; k++) stats_.kernel_count[k] = kcount[k];
+    for (size_t i = 0; i < used; i++) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, pool[i].a, pool[i].b);
+        stats_.kernel_ms[pool[i].kind] += t;
+    }
     if (count) {
-        unsigned long long h[8];
+        unsigned long long h[24];
         C2G_CUDA(cudaMemcpy(h, cnt, sizeof(h), cudaMemcpyDeviceToHost));
-        stats_.nodes_visited = (double)(h[0] + h[2]);
-        stats_.prims_tested = (double)(h[1] + h[3]);
+        for (int k = 0; k < 8; k++) {
+            stats_.rays[k] = (double)h[3 * k];
+            stats_.nodes[k] = (double)h[3 * k + 1];
+            stats_.prims[k] = (double)h[3 * k + 2];
+        }
     }
     return check_device_error(err);
 }

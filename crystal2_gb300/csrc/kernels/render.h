@@ -52,14 +52,14 @@ public:
     int halton(int width, int height, int n, const int* px, const int* py, const int* sample, int ndim, float* out,
                DeviceArena& arena, std::string& err);
     int camera_rays(int n, const float* pos2, float* o, float* d, DeviceArena& arena, std::string& err);
-    void set_counting(bool on) { counting_ = on; }
+    void set_counting(int flags) { counting_ = flags; }
     const c2g_stats& stats() const { return stats_; }
     int check_device_error(std::string& err);
 
 private:
     DeviceSceneBuffers* sb_;
     WaveBuffers* wb_;
-    bool counting_ = false;
+    int counting_ = 0;
     c2g_stats stats_{};
     int film_w_ = 0, film_h_ = 0;
 };

@@ -130,8 +130,9 @@ class Context:
         self.check(self._lib.c2g_get_stats(self._h, C.byref(s)))
         return s
 
-    def set_counting(self, on: bool) -> None:
-        self.check(self._lib.c2g_set_counting(self._h, 1 if on else 0))
+    def set_counting(self, flags: int) -> None:
+        """``native.COUNT_TRAVERSAL`` | ``native.COUNT_TIMING`` (0 = off)."""
+        self.check(self._lib.c2g_set_counting(self._h, int(flags)))
 
     # ---- ray queries
     def trace_rays(self, o: np.ndarray, d: np.ndarray, any_hit: bool = False, tmin=None, tmax=None, ignore=None):

@@ -79,14 +79,28 @@ typedef struct {
     uint64_t seed;              /* seed of the hash RNG used for Halton dims >= 100 */
 } c2g_render_params;
 
+/* Kernel kinds of c2g_stats arrays. */
+#define C2G_K_RAYGEN 0
+#define C2G_K_EXTEND 1
+#define C2G_K_SHADE 2
+#define C2G_K_SHADOW 3
+#define C2G_K_MIS 4
+#define C2G_K_ACCUM 5
+#define C2G_K_FILM 6
+#define C2G_K_GUIDE 7
+
+/* Counting / timing switches of c2g_set_counting. */
+#define C2G_COUNT_TRAVERSAL 1  /* rays, nodes visited and prims tested per traversal kernel */
+#define C2G_COUNT_TIMING 2     /* CUDA events around every launch; per-kind device time */
+
 typedef struct {
-    double seconds;             /* wall time of the last c2g_render (device, CUDA events) */
+    double seconds;             /* device time of the last c2g_render (CUDA events on its stream) */
     double paths;               /* camera paths traced by the last c2g_render */
-    double rays_closest;        /* closest-hit queries issued */
-    double rays_shadow;         /* any-hit queries issued */
-    double nodes_visited;       /* filled only when counting is enabled */
-    double prims_tested;        /* filled only when counting is enabled */
-    double kernel_ms[8];        /* per-kernel-kind device time: raygen, extend, shade, shadow, mis, accum, film, guide */
+    double rays[8];             /* rays processed per kernel kind (C2G_COUNT_TRAVERSAL) */
+    double nodes[8];            /* BVH nodes visited per kernel kind (C2G_COUNT_TRAVERSAL) */
+    double prims[8];            /* primitives tested per kernel kind (C2G_COUNT_TRAVERSAL) */
+    double kernel_ms[8];        /* device time per kernel kind (C2G_COUNT_TIMING) */
+    int kernel_count[8];        /* launches per kernel kind */
     int kernel_launches;        /* kernels launched by the last c2g_render */
     int waves;                  /* waves of the last c2g_render */
 } c2g_stats;
@@ -129,8 +143,8 @@ int c2g_film_image(c2g_ctx* ctx, float* rgb);
 /* Per-pixel sum of squares of the samples (variance estimates for parity tests). */
 int c2g_film_download_m2(c2g_ctx* ctx, float* rgb_sumsq);
 int c2g_get_stats(c2g_ctx* ctx, c2g_stats* out);
-/* Count nodes visited / prims tested in the traversal kernels (slower; 0 = off). */
-int c2g_set_counting(c2g_ctx* ctx, int enable);
+/* C2G_COUNT_* flags (0 = off): traversal counters (slower kernels) and per-launch timing. */
+int c2g_set_counting(c2g_ctx* ctx, int flags);
 
 /* ---- ray queries (Scene::Intersect / Scene::IntersectTest, Scene.cpp:50-59) ---------------- */
 /* Closest hit (any_hit = 0): obj = scene index of the hit object or -1, t = distance.

@@ -269,6 +269,7 @@ struct Node { Box b; int a, c; int axis; };  // internal: a=ch0, c=ch1; leaf: a=
 
 struct Scene {
     int W, H, spp, depth;
+    bool direct = false;  // Integrator.Type == "DirectLight"
     bool anyclip = true, closest_box = true;
     V3 eye, look, up, right;
     float CW, CH;
@@ -371,6 +372,7 @@ static void load(Scene& s, const std::string& cfgp, const std::string& scnp) {
     s.anyclip = acc == "BVH";
     s.closest_box = acc != "Brute";
     s.depth = (int)cfg->m("Integrator").m("Depth").I();
+    s.direct = cfg->m("Integrator").m("Type").s == "DirectLight";
     const JNode& objs = scn->m("Scene").m("Objects");
     for (auto& np : objs.a) {
         const JNode& n = *np;
@@ -1151,6 +1153,79 @@ static V3 evaluate(const Scene& s, Ray ray, Sampler& smp) {
     return L;
 }
 
+// DirectLightingIntegrator::eval_rec (DirectLightingIntegrator.cpp:27-156): emission at every hit,
+// pass-through at the same level, one round of UniformSampleAllLights (own light included).
+static V3 evaluate_direct(const Scene& s, Ray ray, Sampler& smp) {
+    V3 L(0, 0, 0);
+    if (s.depth <= 0) return L;
+    for (int hop = 0; hop < 1 << 20; hop++) {
+        Hit h;
+        if (!intersect(s, ray, h)) return L;
+        const Obj& ob = s.objs[h.obj];
+        if (ob.light >= 0) {
+            V3 na = h.front ? h.N : -h.N;
+            if (!(dot(na, -ray.d) < 0)) L = L + s.lights[ob.light].Le;
+        }
+        if (ob.mat < 0) {
+            if (ob.light >= 0) return L;
+            ray = Ray{spawn(h, ray.d), ray.d};
+            continue;
+        }
+        BxDF b = make_bxdf(s.mats[ob.mat], h.front);
+        Frame fr{h.dpdu, h.N, h.dpdv};
+        V3 wo = -ray.d;
+        float lx = smp.get(), ly = smp.get(), bx = smp.get(), by = smp.get();
+        V3 Ld(0, 0, 0);
+        const int ns = BALL & ~BS;
+        for (int li = 0; li < (int)s.lights.size(); li++) {
+            const Light& Lg = s.lights[li];
+            if (Lg.zero) continue;
+            V3 Le(0, 0, 0), ep;
+            float pl;
+            V3 Li = light_sample(s, Lg, h.pos, h.N, lx, ly, ep, pl);
+            V3 wi = normalize(ep - h.pos);
+            if (pl != 0.f && !zero(Li)) {
+                V3 f = bsdf_f(b, fr, wo, wi) * std::max(0.f, dot(h.N, wi));
+                float pb = bsdf_pdf(b, fr, wo, wi, ns);
+                if (!zero(f)) {
+                    bool back = dot(ep - h.pos, h.N) < 0;
+                    V3 org = h.pos + (back ? -h.N : h.N) * 1e-4f;
+                    if (intersect_test(s, Ray{org, ep - org}, 0, 1.f - 1e-5f, Lg.type == 0 ? Lg.obj : -1)) Li = V3();
+                    if (!zero(Li)) Le = Le + (Lg.type == 1 ? f * Li / pl : f * Li * ph(pl, pb) / pl);
+                }
+            }
+            if (Lg.type != 1) {
+                float u1 = smp.get();
+                V3 wi2;
+                float pb2 = 0;
+                int st = 0;
+                V3 f = bsdf_sample(b, fr, u1, bx, by, wo, wi2, pb2, ns, st);
+                bool spec = (st & BS) != 0;
+                float w = 1.f;
+                bool ok = true;
+                if (!spec) {
+                    f = f * std::max(0.f, dot(h.N, wi2));
+                    float pl2 = light_pdf(s, Lg, h.pos, h.N, wi2);
+                    if (pl2 == 0.f) ok = false;
+                    else w = ph(pb2, pl2);
+                }
+                if (ok) {
+                    Hit lh;
+                    V3 Li2(0, 0, 0);
+                    if (intersect(s, Ray{spawn(h, wi2), wi2}, lh) && s.objs[lh.obj].light == li) {
+                        V3 na = lh.front ? lh.N : -lh.N;
+                        if (!(dot(na, -wi2) < 0)) Li2 = Lg.Le;
+                    }
+                    if (!zero(Li2)) Le = Le + f * Li2 * w / pb2;
+                }
+            }
+            Ld = Ld + Le;
+        }
+        return L + Ld;
+    }
+    return L;
+}
+
 static Ray camera_ray(const Scene& s, float px, float py) {
     px = px * 2 - 1; py = py * 2 - 1;
     px *= s.CW; py *= s.CH;
@@ -1236,7 +1311,7 @@ double orc_render_region(void* h, int threads, int x0, int y0, int x1, int y1, i
                     Sampler smp{*s, halton_index(*s, x, y, sample), (uint32_t)(y * s->W + x), (uint32_t)sample, seed};
                     float sx = smp.get(), sy = smp.get();
                     float px = ((float)x + sx) / s->W, py = ((float)y + sy) / s->H;
-                    V3 c = evaluate(*s, camera_ray(*s, px, py), smp);
+                    V3 c = s->direct ? evaluate_direct(*s, camera_ray(*s, px, py), smp) : evaluate(*s, camera_ray(*s, px, py), smp);
                     if (bad(c)) c = V3();
                     for (int j = 0; j < 3; j++) { a[j] += c[j]; q[j] += (double)c[j] * c[j]; }
                 }
@@ -1258,7 +1333,8 @@ void orc_render_samples(void* h, int n, const int* px, const int* py, int spp, u
         for (int k = 0; k < spp; k++) {
             Sampler smp{*s, halton_index(*s, px[p], py[p], k), (uint32_t)(py[p] * s->W + px[p]), (uint32_t)k, seed};
             float sx = smp.get(), sy = smp.get();
-            V3 c = evaluate(*s, camera_ray(*s, ((float)px[p] + sx) / s->W, ((float)py[p] + sy) / s->H), smp);
+            Ray cr = camera_ray(*s, ((float)px[p] + sx) / s->W, ((float)py[p] + sy) / s->H);
+            V3 c = s->direct ? evaluate_direct(*s, cr, smp) : evaluate(*s, cr, smp);
             for (int j = 0; j < 3; j++) out[((size_t)p * spp + k) * 3 + j] = c[j];
         }
 }

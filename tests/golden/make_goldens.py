@@ -134,6 +134,20 @@ def main() -> None:
             np.savez_compressed(os.path.join(out, f"render_{name}.npz"), mean=(s / r.spp).astype(np.float32),
                                 m2=(q / r.spp).astype(np.float32), spp=r.spp, px=px, py=py, samples=samples)
         r.close()
+    # direct lighting integrator (DirectLightingIntegrator.cpp) on the Cornell box
+    import json
+    d = os.path.join(work, "direct")
+    cp, sp = SCENES["cornell"](d)
+    cfg = json.load(open(cp))
+    cfg["Integrator"]["Type"] = "DirectLight"
+    json.dump(cfg, open(cp, "w"))
+    r = B.ref_open(cp, sp)
+    s, q, _ = r.render_region(0, 0, r.W, r.H)
+    px = np.arange(0, r.W, 3)[:16].astype(np.int32)
+    py = ((np.arange(px.shape[0]) * 5) % r.H).astype(np.int32)
+    np.savez_compressed(os.path.join(out, "render_direct_cornell.npz"), mean=(s / r.spp).astype(np.float32),
+                        m2=(q / r.spp).astype(np.float32), spp=r.spp, px=px, py=py, samples=r.render_samples(px, py))
+    r.close()
     # BSDFs
     Bz = {}
     for k, (name, params) in enumerate(BSDF_PARAMS.items()):
