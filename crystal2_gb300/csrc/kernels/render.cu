@@ -91,7 +91,8 @@ struct WaveBuffers {
     float4* mis_hit = nullptr;
     int* sh_list = nullptr;
     int* mis_list = nullptr;
-    int* counters = nullptr;  // [0],[1] path queues, [2] shadow, [3] mis
+    int* bucket_list = nullptr;  // kBuckets lists of P slots
+    int* counters = nullptr;  // [0],[1] path queues, [2] shadow, [3] mis, [8..18) material buckets
     std::vector<void*> owned;
 };
 
@@ -146,6 +147,25 @@ struct PathRefs {
     float4 *o, *d, *beta, *L;
 };
 
+// Hits are shaded per material bucket: 0..7 = MatType of the hit's material, 8 = no material
+// (pass-through), 9 = miss.  k_extend appends each queue slot to its bucket; one specialised
+// k_shade<bucket> per bucket then runs without material divergence.
+constexpr int kBuckets = 10;
+constexpr int kBucketNone = 8;
+constexpr int kBucketMiss = 9;
+constexpr int kCntBucket = 8;  // counters[8 .. 8 + kBuckets): bucket sizes
+
+// Warp-aggregated append into per-key lists (lanes with equal keys share one atomic).
+// Must be called by all 32 lanes; key < 0 appends nothing.
+__device__ __forceinline__ int warp_append_keyed(int* counters, int key) {
+    unsigned peers = __match_any_sync(0xffffffffu, key);
+    int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (key >= 0 && lane_id() == leader) base = atomicAdd(counters + key, __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return key >= 0 ? base + __popc(peers & ((1u << lane_id()) - 1u)) : -1;
+}
+
 // ---- raygen (SamplerIntegrator.cpp:42-55 + PerspCamera::GenerateRay) -----------------------------
 __global__ void k_raygen(DevScene S, WaveArgs a, PathRefs out, float4* out_L, int* qcount) {
     const int total = a.nslots * a.wave_samples;
@@ -188,17 +208,29 @@ __device__ __forceinline__ void flush_counts(unsigned long long* cnt, int kind, 
 
 template <bool COUNT>
 __global__ void k_extend(DevScene S, const float4* __restrict__ qo, const float4* __restrict__ qd, float4* hit,
-                         const int* qcount, int* zero_a, int* zero_b, int* zero_c, unsigned long long* cnt) {
+                         const int* qcount, int* zero_a, int* zero_b, int* zero_c, int* bucket_cnt, int* bucket_list,
+                         int cap, unsigned long long* cnt) {
     if (blockIdx.x == 0 && threadIdx.x == 0) { *zero_a = 0; *zero_b = 0; *zero_c = 0; }
     const int n = *qcount;
     const int stride = gridDim.x * blockDim.x;
     TraceCounters tc{0, 0};
     unsigned rays = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        float4 o = qo[i], d = qd[i];
-        Hit h = trace_closest<COUNT>(S, f3(o), f3(d), &tc);
-        hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.obj));
-        rays++;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int i = base + threadIdx.x;
+        int key = -1;
+        if (i < n) {
+            float4 o = qo[i], d = qd[i];
+            Hit h = trace_closest<COUNT>(S, f3(o), f3(d), &tc);
+            hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.obj));
+            rays++;
+            if (h.obj < 0) key = kBucketMiss;
+            else {
+                int m = S.objs[h.obj].material;
+                key = m < 0 ? kBucketNone : S.mats[m].type;
+            }
+        }
+        int j = warp_append_keyed(bucket_cnt, key);
+        if (key >= 0) bucket_list[key * cap + j] = i;
     }
     if (COUNT) flush_counts(cnt, C2G_K_EXTEND, rays, tc);
 }
@@ -215,14 +247,16 @@ struct ShadeOut {
     float4* mis_hit;   // per path slot: emitted radiance reaching the MIS ray, light index in w
 };
 
+template <int MT>
 __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs cur, const float4* __restrict__ hits,
-                                                const int* qcount, ShadeOut out) {
-    const int n = *qcount;
+                                                const int* bucket_cnt, const int* __restrict__ bucket_list, int cap, ShadeOut out) {
+    const int n = bucket_cnt[MT];
+    const int* list = bucket_list + (size_t)MT * cap;
     const int stride = gridDim.x * blockDim.x;
     const int K = a.K;
     for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        const int i = base + threadIdx.x;
-        const bool valid = i < n;
+        const bool valid = base + (int)threadIdx.x < n;
+        const int i = valid ? __ldg(list + base + threadIdx.x) : 0;
         // ---- load path state
         float4 o4 = make_float4(0, 0, 0, 0), d4 = o4, b4 = o4, L4 = o4, h4 = make_float4(0, 0, 0, __int_as_float(-1));
         if (valid) { o4 = cur.o[i]; d4 = cur.d[i]; b4 = cur.beta[i]; L4 = cur.L[i]; h4 = hits[i]; }
@@ -241,7 +275,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
         float3 beta = f3(b4), L = f3(L4);
         Hit h{h4.x, h4.y, h4.z, __float_as_int(h4.w)};
 
-        bool alive = valid && h.obj >= 0;       // miss: the path ends (no skybox)
+        bool alive = valid && MT != kBucketMiss;  // miss: the path ends (no skybox)
         bool do_nee = false;
         bool cont = false;
         float3 next_o = ro, next_d = rd;
@@ -258,7 +292,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                 float3 n_actual = s.front ? s.N : -s.N;
                 L = L + beta * area_Le(Lg, n_actual, -rd);
             }
-            if (s.mat < 0) {
+            if (MT == kBucketNone) {
                 // no BSDF: continue straight through (PathTracingIntegrator.cpp:64-68); the direct
                 // lighting integrator stops at an emitter instead (DirectLightingIntegrator.cpp:48-55)
                 if (!(direct && s.light >= 0)) {
@@ -268,6 +302,8 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                 }
             } else {
                 bx = make_bxdf(S.mats[s.mat], s.front);
+                bx.mtype = MT;  // compile-time material: the BxDF switches fold away
+                bx.flags = material_flags(MT);
                 fr.T = s.dpdu; fr.N = s.N; fr.B = s.dpdv;
                 do_nee = true;
             }
@@ -591,6 +627,16 @@ int grid_for(const void* kernel, int block, size_t smem = 0) {
 
 }  // namespace
 
+void launch_shade(int bk, int grid, cudaStream_t st, const DevScene& S, const WaveArgs& a, const PathRefs& cur, const float4* hits,
+                  const int* bcnt, const int* blist, int cap, const ShadeOut& so) {
+    switch (bk) {
+#define C2G_SHADE_CASE(B) case B: k_shade<B><<<grid, 128, 0, st>>>(S, a, cur, hits, bcnt, blist, cap, so); break;
+        C2G_SHADE_CASE(0) C2G_SHADE_CASE(1) C2G_SHADE_CASE(2) C2G_SHADE_CASE(3) C2G_SHADE_CASE(4)
+        C2G_SHADE_CASE(5) C2G_SHADE_CASE(6) C2G_SHADE_CASE(7) C2G_SHADE_CASE(8) C2G_SHADE_CASE(9)
+#undef C2G_SHADE_CASE
+    }
+}
+
 int GpuScene::upload(const HostScene& s, int tree, const RefTree* ref, const SahTree* sah, DeviceArena& arena, std::string& err) {
     // release previous scene buffers
     for (void* p : sb_->owned) arena.free(p);
@@ -667,6 +713,8 @@ int GpuScene::upload(const HostScene& s, int tree, const RefTree* ref, const Sah
     C2G_CUDA(cudaMemset(sb_->film, 0, npx * sizeof(float4)));
     C2G_CUDA(cudaMemset(sb_->film_m2, 0, npx * sizeof(float4)));
     sb_->n_lights = S.n_lights;
+    present_buckets_ = 1 << kBucketMiss;
+    for (const ObjInfo& o : s.objs) present_buckets_ |= 1 << (o.material < 0 ? kBucketNone : s.mats[o.material].type);
     // wave buffers depend on the light count: drop them
     for (void* p : wb_->owned) arena.free(p);
     wb_->owned.clear();
@@ -755,7 +803,7 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
              (wb_->sh_o = (float4*)A(PK * 16)) && (wb_->sh_d = (float4*)A(PK * 16)) && (wb_->sh_c = (float4*)A(PK * 16)) &&
              (wb_->mis_o = (float4*)A(P * 16)) && (wb_->mis_d = (float4*)A(P * 16)) && (wb_->mis_c = (float4*)A(PK * 16)) &&
              (wb_->mis_hit = (float4*)A(P * 16)) && (wb_->sh_list = (int*)A(PK * 4)) && (wb_->mis_list = (int*)A(P * 4)) &&
-             (wb_->counters = (int*)A(64));
+             (wb_->bucket_list = (int*)A(P * 4 * kBuckets)) && (wb_->counters = (int*)A(256));
         if (!ok) {
             for (void* q : wb_->owned) arena.free(q);
             wb_->owned.clear();
@@ -776,7 +824,7 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         g_raygen = grid_for((const void*)k_raygen, 256);
         g_ext = grid_for((const void*)k_extend<false>, 128);
         g_ext_c = grid_for((const void*)k_extend<true>, 128);
-        g_shade = grid_for((const void*)k_shade, 128);
+        g_shade = grid_for((const void*)k_shade<MAT_DIFFUSE>, 128);
         g_sh = grid_for((const void*)k_shadow<false>, 128);
         g_sh_c = grid_for((const void*)k_shadow<true>, 128);
         g_mis = grid_for((const void*)k_mis<false>, 128);
@@ -815,7 +863,7 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
     for (int s0 = 0; s0 < p.sample_count; s0 += spw) {
         a.wave_samples = std::min(spw, p.sample_count - s0);
         a.sample0 = p.sample_begin + s0;
-        C2G_CUDA(cudaMemsetAsync(C, 0, 64, st));
+        C2G_CUDA(cudaMemsetAsync(C, 0, 256, st));
         PathRefs buf[2] = {{w.o[0], w.d[0], w.beta[0], w.L[0]}, {w.o[1], w.d[1], w.beta[1], w.L[1]}};
         begin(C2G_K_RAYGEN);
         k_raygen<<<g_raygen, 256, 0, st>>>(S, a, buf[0], w.out_L, C + 0);
@@ -824,15 +872,22 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         for (int b = 0; b < p.max_depth; b++) {
             int nxt = cur ^ 1;
             begin(C2G_K_EXTEND);
+            cudaMemsetAsync(C + kCntBucket, 0, sizeof(int) * kBuckets, st);
             if (count)
-                k_extend<true><<<g_ext_c, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3, cnt);
+                k_extend<true><<<g_ext_c, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
+                                                        C + kCntBucket, w.bucket_list, (int)w.P, cnt);
             else
-                k_extend<false><<<g_ext, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3, cnt);
+                k_extend<false><<<g_ext, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
+                                                         C + kCntBucket, w.bucket_list, (int)w.P, cnt);
             end();
             ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc, w.mis_hit};
-            begin(C2G_K_SHADE);
-            k_shade<<<g_shade, 128, 0, st>>>(S, a, buf[cur], w.hit, C + cur, so);
-            end();
+            for (int bk = 0; bk < kBuckets; bk++) {
+                if (!(present_buckets_ & (1 << bk))) continue;
+                begin(C2G_K_SHADE);
+                launch_shade(bk, g_shade, st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so);
+                end();
+                launches++;
+            }
             begin(C2G_K_SHADOW);
             if (count) k_shadow<true><<<g_sh_c, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
             else k_shadow<false><<<g_sh, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
@@ -844,7 +899,7 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
             begin(C2G_K_ACCUM);
             k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.mis_hit, w.out_L, C + cur);
             end();
-            launches += 5;
+            launches += 4;
             cur = nxt;
         }
         begin(C2G_K_FILM);

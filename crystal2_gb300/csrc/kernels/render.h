@@ -60,6 +60,7 @@ private:
     DeviceSceneBuffers* sb_;
     WaveBuffers* wb_;
     int counting_ = 0;
+    int present_buckets_ = 0;  // material buckets the loaded scene can produce
     c2g_stats stats_{};
     int film_w_ = 0, film_h_ = 0;
 };
