@@ -1,5 +1,7 @@
 #include "bvh.h"
 
+#include "../../../include/c2g.h"
+
 #include <algorithm>
 #include <cmath>
 #include <limits>
@@ -217,6 +219,9 @@ void build_ref_tree(const HostScene& s, RefTree& out) {
 }
 
 void build_sah_tree(const HostScene& s, SahTree& out, int max_leaf) {
+    // traversal packs a leaf as (first prim << 3 | count): counts up to 7, first prim below 2^27
+    if (max_leaf > 7) max_leaf = 7;
+    if (s.num_objects() >= (size_t(1) << 27)) throw SceneError(C2G_ERR_INVALID, "scene exceeds 2^27 primitives");
     std::vector<Box> boxes;
     std::vector<float> centers;
     object_boxes(s, boxes, centers);

@@ -382,10 +382,11 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
             if (do_nee) {
                 out.sh_c[e] = sh_c4;
                 out.mis_c[e] = mis_c4;
-                if (sh_valid) { out.sh_o[e] = sh_o4; out.sh_d[e] = sh_d4; }
             }
+            // shadow rays are stored densely in append order (coalesced reads in k_shadow); the
+            // list keeps the (slot, light) entry the result belongs to
             int js = warp_append(out.sh_count, sh_valid);
-            if (sh_valid) out.sh_list[js] = e;
+            if (sh_valid) { out.sh_list[js] = e; out.sh_o[js] = sh_o4; out.sh_d[js] = sh_d4; }
         }
         {
             // one MIS ray per path (closest hit; k_mis records which light, if any, it reaches)
@@ -393,8 +394,8 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
             if (any_mis) {
                 float3 org = spawn_origin(s, wi2);
                 out.mis_list[jm] = i;
-                out.mis_o[i] = make_float4(org.x, org.y, org.z, 0.f);
-                out.mis_d[i] = make_float4(wi2.x, wi2.y, wi2.z, 0.f);
+                out.mis_o[jm] = make_float4(org.x, org.y, org.z, 0.f);
+                out.mis_d[jm] = make_float4(wi2.x, wi2.y, wi2.z, 0.f);
             }
             if (do_nee) out.mis_hit[i] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
         }
@@ -454,10 +455,9 @@ __global__ void k_shadow(DevScene S, const int* __restrict__ list, const int* co
     TraceCounters tc{0, 0};
     unsigned rays = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        int e = list[i];
-        float4 o = so[e], d = sd[e];
+        float4 o = so[i], d = sd[i];
         bool occ = trace_any<COUNT>(S, f3(o), f3(d), 0.f, d.w, __float_as_int(o.w), &tc);
-        if (occ) sc[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (occ) sc[list[i]] = make_float4(0.f, 0.f, 0.f, 0.f);
         rays++;
     }
     if (COUNT) flush_counts(cnt, C2G_K_SHADOW, rays, tc);
@@ -473,7 +473,7 @@ __global__ void k_mis(DevScene S, const int* __restrict__ list, const int* count
     unsigned rays = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         int slot = list[i];
-        float4 o = mo[slot], d = md[slot];
+        float4 o = mo[i], d = md[i];
         Hit h = trace_closest<COUNT>(S, f3(o), f3(d), &tc);
         rays++;
         float3 Le = f3(0.f, 0.f, 0.f);
@@ -987,5 +987,6 @@ int GpuScene::camera_rays(int n, const float* pos2, float* o, float* d, DeviceAr
     arena.free(buf);
     return rc;
 }
+
 
 }  // namespace c2g

@@ -9,6 +9,8 @@
 // axis-aligned triangle t1 == t2 and the test passes only when both computations agree to the
 // last bit, which makes such triangles partly transparent to shadow rays in the reference.
 #pragma once
+#include <climits>
+
 #include "dev_common.cuh"
 
 namespace c2g {
@@ -293,50 +295,84 @@ __device__ __forceinline__ bool trace_any_ref(const DevScene& S, const RayQ& r, 
     return false;
 }
 
-// Compact SAH tree: both child boxes live in the parent; hit children are visited near-first by
-// entry distance, leaves are intersected as soon as they are reached.
+// Compact SAH tree traversal ("while-while" with leaf postponing).  Both child boxes live in the
+// parent node; a child is an inner-node index or a leaf (first prim, count) packed into a negative
+// reference.  Each lane walks inner nodes until it has found a leaf, then keeps walking while other
+// lanes of the warp still search; the leaves are intersected together once every active lane has
+// one, so the expensive exact triangle tests run with most lanes active.  Closest-hit pushes carry
+// the entry distance so that subtrees beyond the current hit are dropped on pop.
+constexpr int kNoRef = INT_MIN;
+__device__ __forceinline__ int leaf_ref(int first, int count) { return -1 - ((first << 3) | count); }
+__device__ __forceinline__ bool is_leaf(int ref) { return ref < 0 && ref != kNoRef; }
+__device__ __forceinline__ void leaf_range(int ref, int& first, int& count) {
+    int v = -1 - ref;
+    first = v >> 3;
+    count = v & 7;
+}
+
 template <bool COUNT>
 __device__ __forceinline__ Hit trace_closest_sah(const DevScene& S, const RayQ& r, float tmax, TraceCounters* cnt) {
     Hit h{INFINITY, 0.f, 0.f, -1};
     int stack[kStack];
+    float stack_t[kStack];
     int top = 0;
-    int cur = 0;
-    while (true) {
-        const float4* N = reinterpret_cast<const float4*>(S.wide_nodes + cur);
-        float4 L0 = __ldg(N), H0 = __ldg(N + 1), L1 = __ldg(N + 2), H1 = __ldg(N + 3);
-        if (COUNT) cnt->nodes++;
-        float lim = smin(tmax, h.t);
-        float mn0[3] = {L0.x, L0.y, L0.z}, mx0[3] = {H0.x, H0.y, H0.z};
-        float mn1[3] = {L1.x, L1.y, L1.z}, mx1[3] = {H1.x, H1.y, H1.z};
-        float a0 = 0.f, b0 = lim, a1 = 0.f, b1 = lim;
-        bool hit0 = box_test(r, mn0, mx0, a0, b0);
-        bool hit1 = box_test(r, mn1, mx1, a1, b1);
-        int c0 = __float_as_int(L0.w), n0 = __float_as_int(H0.w);
-        int c1 = __float_as_int(L1.w), n1 = __float_as_int(H1.w);
-        // leaves first, in near order
-        bool first1 = hit1 && (!hit0 || a1 < a0);
-        int next = -1;
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            bool side = (k == 0) ? first1 : !first1;  // true = child 1
-            bool hit = side ? hit1 : hit0;
-            if (!hit) continue;
-            int c = side ? c1 : c0, n = side ? n1 : n0;
-            if (n > 0) {
-                for (int i = 0; i < n; i++) {
-                    if (COUNT) cnt->prims++;
-                    closest_prim(S, c + i, r, tmax, h);
-                }
-            } else if (next < 0) {
-                next = c;
-            } else {
+    int ref = 0, leaf = kNoRef;
+    auto pop = [&]() -> int {
+        while (top > 0) {
+            --top;
+            if (stack_t[top] <= h.t) return stack[top];
+        }
+        return kNoRef;
+    };
+    while (ref != kNoRef || leaf != kNoRef) {
+        while (ref >= 0) {
+            const float4* N = reinterpret_cast<const float4*>(S.wide_nodes + ref);
+            float4 L0 = __ldg(N), H0 = __ldg(N + 1), L1 = __ldg(N + 2), H1 = __ldg(N + 3);
+            if (COUNT) cnt->nodes++;
+            float lim = smin(tmax, h.t);
+            float mn0[3] = {L0.x, L0.y, L0.z}, mx0[3] = {H0.x, H0.y, H0.z};
+            float mn1[3] = {L1.x, L1.y, L1.z}, mx1[3] = {H1.x, H1.y, H1.z};
+            float a0 = 0.f, b0 = lim, a1 = 0.f, b1 = lim;
+            bool hit0 = box_test(r, mn0, mx0, a0, b0);
+            bool hit1 = box_test(r, mn1, mx1, a1, b1);
+            int n0 = __float_as_int(H0.w), n1 = __float_as_int(H1.w);
+            int r0 = n0 > 0 ? leaf_ref(__float_as_int(L0.w), n0) : __float_as_int(L0.w);
+            int r1 = n1 > 0 ? leaf_ref(__float_as_int(L1.w), n1) : __float_as_int(L1.w);
+            if (hit0 && hit1) {
+                bool swap = a1 < a0;
+                int nr = swap ? r1 : r0, fr = swap ? r0 : r1;
+                float ft = swap ? a0 : a1;
                 if (top >= kStack) { dev_flag_error(S.err, DEVERR_STACK); return h; }
-                stack[top++] = c;
+                stack[top] = fr;
+                stack_t[top] = ft;
+                top++;
+                ref = nr;
+            } else if (hit0) {
+                ref = r0;
+            } else if (hit1) {
+                ref = r1;
+            } else {
+                ref = pop();
+            }
+            if (is_leaf(ref) && leaf == kNoRef) {
+                leaf = ref;
+                ref = pop();
+            }
+            if (!__any_sync(__activemask(), leaf == kNoRef)) break;
+        }
+        while (leaf != kNoRef) {
+            int first, count;
+            leaf_range(leaf, first, count);
+            for (int i = 0; i < count; i++) {
+                if (COUNT) cnt->prims++;
+                closest_prim(S, first + i, r, tmax, h);
+            }
+            leaf = kNoRef;
+            if (is_leaf(ref)) {
+                leaf = ref;
+                ref = pop();
             }
         }
-        if (next >= 0) { cur = next; continue; }
-        if (!top) break;
-        cur = stack[--top];
     }
     return h;
 }
@@ -345,39 +381,50 @@ template <bool COUNT>
 __device__ __forceinline__ bool trace_any_sah(const DevScene& S, const RayQ& r, float tmin, float tmax, int ignore, TraceCounters* cnt) {
     int stack[kStack];
     int top = 0;
-    int cur = 0;
-    while (true) {
-        const float4* N = reinterpret_cast<const float4*>(S.wide_nodes + cur);
-        float4 L0 = __ldg(N), H0 = __ldg(N + 1), L1 = __ldg(N + 2), H1 = __ldg(N + 3);
-        if (COUNT) cnt->nodes++;
-        float mn0[3] = {L0.x, L0.y, L0.z}, mx0[3] = {H0.x, H0.y, H0.z};
-        float mn1[3] = {L1.x, L1.y, L1.z}, mx1[3] = {H1.x, H1.y, H1.z};
-        float a0 = tmin, b0 = tmax, a1 = tmin, b1 = tmax;
-        bool hit0 = box_test(r, mn0, mx0, a0, b0);
-        bool hit1 = box_test(r, mn1, mx1, a1, b1);
-        int c0 = __float_as_int(L0.w), n0 = __float_as_int(H0.w);
-        int c1 = __float_as_int(L1.w), n1 = __float_as_int(H1.w);
-        int next = -1;
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            bool hit = k ? hit1 : hit0;
-            if (!hit) continue;
-            int c = k ? c1 : c0, n = k ? n1 : n0;
-            if (n > 0) {
-                for (int i = 0; i < n; i++) {
-                    if (COUNT) cnt->prims++;
-                    if (anyhit_prim(S, c + i, r, tmin, tmax, ignore)) return true;
-                }
-            } else if (next < 0) {
-                next = c;
-            } else {
+    int ref = 0, leaf = kNoRef;
+    while (ref != kNoRef || leaf != kNoRef) {
+        while (ref >= 0) {
+            const float4* N = reinterpret_cast<const float4*>(S.wide_nodes + ref);
+            float4 L0 = __ldg(N), H0 = __ldg(N + 1), L1 = __ldg(N + 2), H1 = __ldg(N + 3);
+            if (COUNT) cnt->nodes++;
+            float mn0[3] = {L0.x, L0.y, L0.z}, mx0[3] = {H0.x, H0.y, H0.z};
+            float mn1[3] = {L1.x, L1.y, L1.z}, mx1[3] = {H1.x, H1.y, H1.z};
+            float a0 = tmin, b0 = tmax, a1 = tmin, b1 = tmax;
+            bool hit0 = box_test(r, mn0, mx0, a0, b0);
+            bool hit1 = box_test(r, mn1, mx1, a1, b1);
+            int n0 = __float_as_int(H0.w), n1 = __float_as_int(H1.w);
+            int r0 = n0 > 0 ? leaf_ref(__float_as_int(L0.w), n0) : __float_as_int(L0.w);
+            int r1 = n1 > 0 ? leaf_ref(__float_as_int(L1.w), n1) : __float_as_int(L1.w);
+            if (hit0 && hit1) {
                 if (top >= kStack) { dev_flag_error(S.err, DEVERR_STACK); return false; }
-                stack[top++] = c;
+                stack[top++] = r1;
+                ref = r0;
+            } else if (hit0) {
+                ref = r0;
+            } else if (hit1) {
+                ref = r1;
+            } else {
+                ref = top ? stack[--top] : kNoRef;
+            }
+            if (is_leaf(ref) && leaf == kNoRef) {
+                leaf = ref;
+                ref = top ? stack[--top] : kNoRef;
+            }
+            if (!__any_sync(__activemask(), leaf == kNoRef)) break;
+        }
+        while (leaf != kNoRef) {
+            int first, count;
+            leaf_range(leaf, first, count);
+            for (int i = 0; i < count; i++) {
+                if (COUNT) cnt->prims++;
+                if (anyhit_prim(S, first + i, r, tmin, tmax, ignore)) return true;
+            }
+            leaf = kNoRef;
+            if (is_leaf(ref)) {
+                leaf = ref;
+                ref = top ? stack[--top] : kNoRef;
             }
         }
-        if (next >= 0) { cur = next; continue; }
-        if (!top) break;
-        cur = stack[--top];
     }
     return false;
 }
