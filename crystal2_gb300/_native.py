@@ -86,6 +86,7 @@ SIGNATURES = {
     "c2g_bvh_order": (_I, [_P, _IP, _I]),
     "c2g_bvh_nodes": (_I, [_P, _FP, _IP, _IP, _I]),
     "c2g_render": (_I, [_P, C.POINTER(RenderParams), _P]),
+    "c2g_render_noalloc": (_I, [_P, C.POINTER(RenderParams), _P, _P]),
     "c2g_film_clear": (_I, [_P, _P]),
     "c2g_film_download": (_I, [_P, _FP, _FP]),
     "c2g_film_image": (_I, [_P, _FP]),

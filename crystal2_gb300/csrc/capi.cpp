@@ -226,6 +226,17 @@ int c2g_render(c2g_ctx* ctx, const c2g_render_params* params, void* stream) {
     return C2G_OK;
 }
 
+int c2g_render_noalloc(c2g_ctx* ctx, const c2g_render_params* params, float* film_dev, void* stream) {
+    if (!ctx || !params || !film_dev) return fail(ctx, C2G_ERR_INVALID, "null argument");
+    if (!ctx->loaded) return fail(ctx, C2G_ERR_STATE, "no scene loaded");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    std::string err;
+    rc = ctx->gpu->render_noalloc(*params, (float4*)film_dev, pick_stream(ctx, stream), err);
+    if (rc) return fail(ctx, rc, err);
+    return C2G_OK;
+}
+
 int c2g_film_clear(c2g_ctx* ctx, void* stream) {
     if (!ctx) return C2G_ERR_INVALID;
     if (!ctx->loaded) return fail(ctx, C2G_ERR_STATE, "no scene loaded");

@@ -989,4 +989,137 @@ int GpuScene::camera_rays(int n, const float* pos2, float* o, float* d, DeviceAr
 }
 
 
+// ---- allocation-free rendering ------------------------------------------------------------------
+// Some callers cannot call cudaMalloc while they render: a host application that owns all device
+// memory through its own pool and forbids plug-ins to allocate, or a frame loop that must not
+// pay cudaMalloc's implicit device synchronisation.  render_noalloc() renders with the same
+// kernels as render(), but the wave's working memory (path state, queues, NEE entries, counters)
+// lives in the file-scope array below instead of context allocations, and the film is a buffer
+// the caller provides.  The array is part of the library image: every GPU that loads the library
+// holds it until the process exits.
+//
+// Limits: a frame of at most kNoAllocSlots pixel slots (width and height rounded up to multiples
+// of 8; 16384 slots = 128 x 128 pixels) and at most kNoAllocLights lights; larger requests are
+// rejected with C2G_ERR_INVALID.  One sample per pixel per wave.  The first call on a device looks up
+// the array's device address (cudaGetSymbolAddress, with that device current), so that first call
+// should come before any stream capture.  Every call shares the array and overwrites what the
+// previous call left there; calls that overlap on the GPU (two streams, two threads) race on it.
+constexpr int kNoAllocSlots = 16384;
+constexpr int kNoAllocLights = 8;
+constexpr size_t kNoAllocPathBytes = 2 * 4 * 16   // o, d, beta, L (ping-pong)
+                                   + 16 + 8 + 16  // hit, acc, out_L
+                                   + 16           // per-pixel sums of squares (film_m2; not returned)
+                                   + 3 * 16 + 4   // mis_o, mis_d, mis_hit, mis_list
+                                   + 4 * kBuckets // bucket lists
+                                   + (size_t)kNoAllocLights * (4 * 16 + 4);  // sh_o, sh_d, sh_c, mis_c, sh_list
+constexpr size_t kNoAllocBytes = (size_t)kNoAllocSlots * kNoAllocPathBytes + 256;
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+void* g_noalloc_ptr[kMaxDevices] = {nullptr};
+}  // namespace
+
+int GpuScene::render_noalloc(const c2g_render_params& p, float4* film_dev, cudaStream_t st, std::string& err) {
+    if (!sb_->film) { err = "no scene loaded"; return C2G_ERR_STATE; }
+    if (!film_dev) { err = "film buffer is null"; return C2G_ERR_INVALID; }
+    if (p.width != film_w_ || p.height != film_h_) { err = "render size differs from the loaded film size"; return C2G_ERR_INVALID; }
+    if (p.max_depth < 0 || p.sample_count < 0 || p.sample_begin < 0) { err = "invalid render parameters"; return C2G_ERR_INVALID; }
+    if (p.integrator != C2G_INTEGRATOR_PATH && p.integrator != C2G_INTEGRATOR_DIRECT) { err = "integrator not available in this build"; return C2G_ERR_UNSUPPORTED; }
+    if (p.max_depth > 255) { err = "max_depth above 255"; return C2G_ERR_INVALID; }
+    WaveArgs a{};
+    a.W = p.width;
+    a.H = p.height;
+    a.tiles_x = (p.width + 7) / 8;
+    a.nslots = a.tiles_x * ((p.height + 7) / 8) * 64;
+    a.max_depth = p.max_depth;
+    a.K = std::max(1, sb_->S.n_lights);
+    a.integrator = p.integrator;
+    if (a.nslots > kNoAllocSlots) {
+        err = "allocation-free render: frame of " + std::to_string(a.nslots) + " pixel slots exceeds the maximum of " +
+              std::to_string(kNoAllocSlots) + " (128 x 128 pixels)";
+        return C2G_ERR_INVALID;
+    }
+    if (a.K > kNoAllocLights) {
+        err = "allocation-free render: " + std::to_string(a.K) + " lights exceed the maximum of " + std::to_string(kNoAllocLights);
+        return C2G_ERR_INVALID;
+    }
+    // set-up, once per device with that device current: the device address of the scratch array
+    int dev = 0;
+    C2G_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) { err = "device ordinal out of range"; return C2G_ERR_INVALID; }
+    if (!g_noalloc_ptr[dev]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr) {
+            err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+            return C2G_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = ptr;
+    }
+    // carve the scratch array (slot-sized pieces first, then K-sized ones)
+    const size_t P = (size_t)a.nslots, PK = P * (size_t)a.K;
+    unsigned char* q = (unsigned char*)g_noalloc_ptr[dev];
+    auto take = [&](size_t bytes) { unsigned char* r = q; q += (bytes + 255) & ~size_t(255); return r; };
+    WaveBuffers w;
+    for (int b = 0; b < 2; b++) {
+        w.o[b] = (float4*)take(P * 16); w.d[b] = (float4*)take(P * 16);
+        w.beta[b] = (float4*)take(P * 16); w.L[b] = (float4*)take(P * 16);
+    }
+    w.hit = (float4*)take(P * 16);
+    w.acc = (int2*)take(P * 8);
+    w.out_L = (float4*)take(P * 16);
+    w.mis_o = (float4*)take(P * 16);
+    w.mis_d = (float4*)take(P * 16);
+    w.mis_hit = (float4*)take(P * 16);
+    w.mis_list = (int*)take(P * 4);
+    w.bucket_list = (int*)take(P * 4 * kBuckets);
+    w.sh_o = (float4*)take(PK * 16);
+    w.sh_d = (float4*)take(PK * 16);
+    w.sh_c = (float4*)take(PK * 16);
+    w.mis_c = (float4*)take(PK * 16);
+    w.sh_list = (int*)take(PK * 4);
+    float4* m2 = (float4*)take(P * 16);
+    w.counters = (int*)take(256);
+    if ((size_t)(q - (unsigned char*)g_noalloc_ptr[dev]) > kNoAllocBytes) { err = "allocation-free render: scratch layout overflow"; return C2G_ERR_INVALID; }
+    w.P = P;
+    w.K = a.K;
+    DevScene S = sb_->S;
+    S.anyhit_clip = p.accel == C2G_ACCEL_BVH ? 1 : 0;
+    S.closest_box = p.accel == C2G_ACCEL_BVH ? 1 : 0;
+    S.seed = p.seed;
+    const int g_raygen = grid_for((const void*)k_raygen, 256), g_ext = grid_for((const void*)k_extend<false>, 128);
+    const int g_shade = grid_for((const void*)k_shade<MAT_DIFFUSE>, 128), g_sh = grid_for((const void*)k_shadow<false>, 128);
+    const int g_mis = grid_for((const void*)k_mis<false>, 128), g_acc = grid_for((const void*)k_accumulate, 256);
+    const int g_film = grid_for((const void*)k_film, 256);
+    int* C = w.counters;
+    PathRefs buf[2] = {{w.o[0], w.d[0], w.beta[0], w.L[0]}, {w.o[1], w.d[1], w.beta[1], w.L[1]}};
+    C2G_CUDA(cudaMemsetAsync(m2, 0, P * 16, st));
+    for (int s0 = 0; s0 < p.sample_count; s0++) {
+        a.wave_samples = 1;
+        a.sample0 = p.sample_begin + s0;
+        C2G_CUDA(cudaMemsetAsync(C, 0, 256, st));  // counters start at zero for every wave
+        k_raygen<<<g_raygen, 256, 0, st>>>(S, a, buf[0], w.out_L, C + 0);
+        int cur = 0;
+        for (int b = 0; b < p.max_depth; b++) {
+            int nxt = cur ^ 1;
+            C2G_CUDA(cudaMemsetAsync(C + kCntBucket, 0, sizeof(int) * kBuckets, st));
+            k_extend<false><<<g_ext, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
+                                                     C + kCntBucket, w.bucket_list, (int)w.P, nullptr);
+            ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc, w.mis_hit};
+            for (int bk = 0; bk < kBuckets; bk++)
+                if (present_buckets_ & (1 << bk)) launch_shade(bk, g_shade, st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so);
+            k_shadow<false><<<g_sh, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, nullptr);
+            k_mis<false><<<g_mis, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, nullptr);
+            k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.mis_hit, w.out_L, C + cur);
+            cur = nxt;
+        }
+        // the caller's film gets the radiance sums and weights; the sums of squares stay in scratch
+        k_film<<<g_film, 256, 0, st>>>(a, w.out_L, film_dev, m2);
+    }
+    C2G_CUDA(cudaGetLastError());
+    C2G_CUDA(cudaStreamSynchronize(st));
+    return check_device_error(err);
+}
+
 }  // namespace c2g

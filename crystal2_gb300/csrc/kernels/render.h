@@ -52,6 +52,8 @@ public:
     int halton(int width, int height, int n, const int* px, const int* py, const int* sample, int ndim, float* out,
                DeviceArena& arena, std::string& err);
     int camera_rays(int n, const float* pos2, float* o, float* d, DeviceArena& arena, std::string& err);
+    // Same render as render() into a caller-owned film, with no device allocation (render.cu).
+    int render_noalloc(const c2g_render_params& p, float4* film_dev, cudaStream_t st, std::string& err);
     void set_counting(int flags) { counting_ = flags; }
     const c2g_stats& stats() const { return stats_; }
     int check_device_error(std::string& err);

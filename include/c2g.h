@@ -143,6 +143,18 @@ int c2g_film_image(c2g_ctx* ctx, float* rgb);
 /* Per-pixel sum of squares of the samples (variance estimates for parity tests). */
 int c2g_film_download_m2(c2g_ctx* ctx, float* rgb_sumsq);
 int c2g_get_stats(c2g_ctx* ctx, c2g_stats* out);
+/* Allocation-free variant of c2g_render, for callers that cannot call cudaMalloc while they render
+ * (an application that hands plug-ins no allocation rights and owns device memory through its own
+ * pool, or a frame loop that must avoid cudaMalloc's implicit synchronisation).  No counterpart in
+ * the reference.  It renders the same samples with the same kernels as c2g_render, but its working
+ * memory is a static device array inside the library (about 14 MB, held by every GPU that loads the
+ * library until the process exits) and the result is added to `film_dev`: caller-owned device
+ * memory of width x height float4 (rgb sum, weight), in c2g_film_download's layout, which the
+ * caller clears.  Limits: at most 16384 pixel slots (width and height rounded up to multiples of 8;
+ * e.g. 128 x 128) and at most 8 lights; larger requests fail with C2G_ERR_INVALID.  The first call
+ * on a device sets up the array's address and should come before any stream capture.  Calls share
+ * the array: calls that overlap on the GPU race.  The call synchronises `stream` before returning. */
+int c2g_render_noalloc(c2g_ctx* ctx, const c2g_render_params* params, float* film_dev, void* stream);
 /* C2G_COUNT_* flags (0 = off): traversal counters (slower kernels) and per-launch timing. */
 int c2g_set_counting(c2g_ctx* ctx, int flags);
 
