@@ -97,7 +97,17 @@ SIGNATURES = {
     "c2g_trace_rays_dev": (_I, [_P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
     "c2g_halton": (_I, [_P, _I, _I, _I, _IP, _IP, _IP, _I, _FP]),
     "c2g_camera_rays": (_I, [_P, _I, _FP, _FP, _FP]),
+    "c2g_guide_reset": (_I, [_P, _FP, _FP, C.c_uint64]),
+    "c2g_guide_set_params": (_I, [_P, _FP]),
+    "c2g_guide_get_params": (_I, [_P, _FP]),
+    "c2g_guide_eval": (_I, [_P, _I, _FP, _FP]),
+    "c2g_guide_gradient": (_I, [_P, _I, _FP, _FP, C.POINTER(C.c_double)]),
+    "c2g_guide_stats": (_I, [_P, C.POINTER(C.c_double), _IP, _IP]),
+    "c2g_guide_config": (_I, [_P, C.c_float, C.c_float, _I, _I]),
 }
+
+GUIDE_PARAMS = 16624
+GUIDE_OUTPUTS = 40
 
 _lib = None
 

@@ -20,7 +20,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libc2g.so")
 
 HOST_SOURCES = ["host/json.cpp", "host/scene.cpp", "host/bvh.cpp", "capi.cpp"]
-CUDA_SOURCES = ["kernels/render.cu"]
+CUDA_SOURCES = ["kernels/render.cu", "kernels/guide.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -81,6 +81,16 @@ cudaStream_t pick_stream(c2g_ctx* ctx, void* s) { return s ? (cudaStream_t)s : c
 
 }  // namespace
 
+// ---- learned guiding proposal ----------------------------------------------------------------
+namespace {
+int guide_ready(c2g_ctx* ctx) {
+    if (!ctx) return C2G_ERR_INVALID;
+    if (ctx->host_only) return fail(ctx, C2G_ERR_STATE, "host-only context");
+    if (!ctx->gpu->guide().ready()) return fail(ctx, C2G_ERR_STATE, "no guide network (c2g_guide_reset or a guided render)");
+    return set_device(ctx);
+}
+}  // namespace
+
 extern "C" {
 
 const char* c2g_version(void) { return "crystal2-gb300 0.1 (sm_103a)"; }
@@ -375,6 +385,79 @@ int c2g_camera_rays(c2g_ctx* ctx, int n, const float* pos2, float* o, float* d) 
     std::string err;
     rc = ctx->gpu->camera_rays(n, pos2, o, d, *ctx->arena, err);
     if (rc) return fail(ctx, rc, err);
+    return C2G_OK;
+}
+
+
+static_assert(C2G_GUIDE_PARAMS == kGuideParams, "guide parameter count");
+static_assert(C2G_GUIDE_OUTPUTS == kGuideOut, "guide output count");
+
+int c2g_guide_reset(c2g_ctx* ctx, const float box_lo[3], const float box_hi[3], unsigned long long seed) {
+    if (!ctx || !box_lo || !box_hi) return fail(ctx, C2G_ERR_INVALID, "null argument");
+    if (ctx->host_only) return fail(ctx, C2G_ERR_STATE, "host-only context");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    std::string err;
+    ctx->gpu->guide().release(*ctx->arena);
+    rc = ctx->gpu->guide().init(*ctx->arena, 64, 1, box_lo, box_hi, seed, err);
+    if (!rc && cudaDeviceSynchronize() != cudaSuccess) { rc = C2G_ERR_CUDA; err = cudaGetErrorString(cudaGetLastError()); }
+    return rc ? fail(ctx, rc, err) : C2G_OK;
+}
+
+int c2g_guide_set_params(c2g_ctx* ctx, const float* params) {
+    if (!params) return fail(ctx, C2G_ERR_INVALID, "null argument");
+    int rc = guide_ready(ctx);
+    if (rc) return rc;
+    std::string err;
+    rc = ctx->gpu->guide().set_params(params, err);
+    return rc ? fail(ctx, rc, err) : C2G_OK;
+}
+
+int c2g_guide_get_params(c2g_ctx* ctx, float* params) {
+    if (!params) return fail(ctx, C2G_ERR_INVALID, "null argument");
+    int rc = guide_ready(ctx);
+    if (rc) return rc;
+    std::string err;
+    rc = ctx->gpu->guide().get_params(params, err);
+    return rc ? fail(ctx, rc, err) : C2G_OK;
+}
+
+int c2g_guide_eval(c2g_ctx* ctx, int n, const float* xnw, float* out) {
+    if (n < 0 || (n > 0 && (!xnw || !out))) return fail(ctx, C2G_ERR_INVALID, "null argument");
+    int rc = guide_ready(ctx);
+    if (rc) return rc;
+    std::string err;
+    rc = ctx->gpu->guide().eval(*ctx->arena, xnw, n, out, err);
+    return rc ? fail(ctx, rc, err) : C2G_OK;
+}
+
+int c2g_guide_gradient(c2g_ctx* ctx, int n, const float* samples, float* grad, double* loss) {
+    if (n <= 0 || !samples || !grad) return fail(ctx, C2G_ERR_INVALID, "invalid argument");
+    int rc = guide_ready(ctx);
+    if (rc) return rc;
+    std::string err;
+    rc = ctx->gpu->guide().gradient(*ctx->arena, samples, n, grad, loss, err);
+    return rc ? fail(ctx, rc, err) : C2G_OK;
+}
+
+int c2g_guide_stats(c2g_ctx* ctx, double* loss, int* records, int* steps) {
+    int rc = guide_ready(ctx);
+    if (rc) return rc;
+    GuideStats g = ctx->gpu->guide_stats();
+    if (loss) *loss = g.loss;
+    if (records) *records = g.records;
+    if (steps) *steps = g.steps;
+    return C2G_OK;
+}
+
+int c2g_guide_config(c2g_ctx* ctx, float learning_rate, float bsdf_fraction, int warmup_waves, int train_steps) {
+    if (!ctx) return C2G_ERR_INVALID;
+    if (!(learning_rate > 0.f) || !(bsdf_fraction > 0.f && bsdf_fraction <= 1.f) || warmup_waves < 0 || train_steps < 0)
+        return fail(ctx, C2G_ERR_INVALID, "invalid guide configuration");
+    if (ctx->host_only) return fail(ctx, C2G_ERR_STATE, "host-only context");
+    ctx->gpu->guide().set_learning_rate(learning_rate);
+    ctx->gpu->guide().set_alpha(bsdf_fraction);
+    ctx->gpu->set_guide_schedule(warmup_waves, train_steps);
     return C2G_OK;
 }
 

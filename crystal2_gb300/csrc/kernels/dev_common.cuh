@@ -33,6 +33,11 @@ struct DevScene {
     int* err;                     // device error word (C2G_DEVERR_*)
 };
 
+// Shading buckets: 0..7 = MatType of the hit's material, 8 = no material, 9 = miss.
+constexpr int kBuckets = 10;
+constexpr int kBucketNone = 8;
+constexpr int kBucketMiss = 9;
+
 enum : int {
     DEVERR_STACK = 1,             // traversal stack overflow
     DEVERR_QUEUE = 2,             // queue capacity exceeded

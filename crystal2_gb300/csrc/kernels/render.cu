@@ -16,6 +16,7 @@
 
 #include "../host/bvh.h"
 #include "../host/scene.h"
+#include "guide.cuh"
 #include "render.h"
 #include "shade.cuh"
 
@@ -150,9 +151,6 @@ struct PathRefs {
 // Hits are shaded per material bucket: 0..7 = MatType of the hit's material, 8 = no material
 // (pass-through), 9 = miss.  k_extend appends each queue slot to its bucket; one specialised
 // k_shade<bucket> per bucket then runs without material divergence.
-constexpr int kBuckets = 10;
-constexpr int kBucketNone = 8;
-constexpr int kBucketMiss = 9;
 constexpr int kCntBucket = 8;  // counters[8 .. 8 + kBuckets): bucket sizes
 
 // Warp-aggregated append into per-key lists (lanes with equal keys share one atomic).
@@ -247,9 +245,10 @@ struct ShadeOut {
     float4* mis_hit;   // per path slot: emitted radiance reaching the MIS ray, light index in w
 };
 
-template <int MT>
+template <int MT, bool G>
 __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs cur, const float4* __restrict__ hits,
-                                                const int* bucket_cnt, const int* __restrict__ bucket_list, int cap, ShadeOut out) {
+                                                const int* bucket_cnt, const int* __restrict__ bucket_list, int cap, ShadeOut out,
+                                                GuideView gv) {
     const int n = bucket_cnt[MT];
     const int* list = bucket_list + (size_t)MT * cap;
     const int stride = gridDim.x * blockDim.x;
@@ -410,12 +409,49 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
             int stype = 0;
             bool ok;
             float3 f = bsdf_sample(bx, fr, u1, u2, wo, wi, pdf, BXDF_ALL, stype, ok);
+            if (G && gv.sample && valid && (bx.flags & BXDF_SPECULAR) == 0) {
+                // Guided continuation: one-sample MIS over {BSDF, learned mixture} with the mixture
+                // pdf alpha * p_bsdf + (1 - alpha) * p_guide (exactly evaluated), so the estimator
+                // stays unbiased; the extra random numbers come from dims far above the plain path's.
+                Lobe lobes[kGuideLobes];
+                float o40[kGuideOut];
+                const float* src = gv.out + (size_t)i * kGuideOut;
+                bool finite = true;
+#pragma unroll
+                for (int k = 0; k < kGuideOut; k++) { o40[k] = src[k]; finite = finite && isfinite(o40[k]); }
+                guide_lobes(o40, lobes);
+                // a non-finite network output leaves this vertex to plain BSDF sampling (alpha = 1)
+                const float alpha = finite ? gv.net.alpha : 1.f;
+                float us = hash_uniform(pixel, sample, 0x4000u + 4u * bounce, S.seed);
+                if (us >= alpha) {
+                    float3 wg = guide_sample(lobes, hash_uniform(pixel, sample, 0x4001u + 4u * bounce, S.seed),
+                                             hash_uniform(pixel, sample, 0x4002u + 4u * bounce, S.seed),
+                                             hash_uniform(pixel, sample, 0x4003u + 4u * bounce, S.seed));
+                    wi = clamp1(wg);
+                    float pb;
+                    f = bsdf_f_pdf(bx, fr, wo, wi, BXDF_ALL, pb);
+                    bool refl = dot(wi, s.N) * dot(wo, s.N) > 0;
+                    stype = (bx.flags & ~(BXDF_REFLECTION | BXDF_TRANSMISSION)) | (refl ? BXDF_REFLECTION : BXDF_TRANSMISSION);
+                    pdf = alpha * pb + (1.f - alpha) * guide_pdf(lobes, wg);
+                    ok = !is_zero(f) && pdf > 0.f;
+                } else if (ok && alpha < 1.f) {
+                    pdf = alpha * pdf + (1.f - alpha) * guide_pdf(lobes, normalize(wi));
+                }
+            }
             if (ok && fabsf(pdf) != 0.f) {
                 bool specular = (stype & BXDF_SPECULAR) != 0;
                 float cosine = specular ? 1.0f : fmaxf(0.f, (stype & BXDF_TRANSMISSION) ? dot(-s.N, wi) : dot(s.N, wi));
                 light_path = (specular || (stype & BXDF_TRANSMISSION)) ? 1 : 0;
                 next_o = spawn_origin(s, wi);
                 next_d = wi;
+                if (G && gv.record && !specular && (pid % gv.rec_stride) == 0 && bounce < gv.rec_depth) {
+                    // training record: vertex, throughput and radiance so far (direct light added later)
+                    float4* r = gv.rec + 4 * ((size_t)(pid / gv.rec_stride) * gv.rec_depth + bounce);
+                    r[1] = make_float4(s.N.x, s.N.y, s.N.z, 0.2126f * L.x + 0.7152f * L.y + 0.0722f * L.z);
+                    r[2] = make_float4(wo.x, wo.y, wo.z, 0.2126f * beta.x + 0.7152f * beta.y + 0.0722f * beta.z);
+                    r[3] = make_float4(wi.x, wi.y, wi.z, 0.f);
+                    r[0] = make_float4(s.pos.x, s.pos.y, s.pos.z, 1.f);
+                }
                 beta = beta * (f * cosine / pdf);
                 cont = true;
                 if (bounce > 3) {
@@ -496,7 +532,8 @@ __global__ void k_mis(DevScene S, const int* __restrict__ list, const int* count
 
 // ---- accumulate ------------------------------------------------------------------------------------
 __global__ void k_accumulate(WaveArgs a, PathRefs cur, PathRefs nxt, const int2* __restrict__ acc, const float4* __restrict__ sc,
-                             const float4* __restrict__ mc, const float4* __restrict__ mis_hit, float4* out_L, const int* qcount) {
+                             const float4* __restrict__ mc, const float4* __restrict__ mis_hit, float4* out_L, const int* qcount,
+                             GuideView gv) {
     const int n = *qcount;
     const int stride = gridDim.x * blockDim.x;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
@@ -510,6 +547,14 @@ __global__ void k_accumulate(WaveArgs a, PathRefs cur, PathRefs nxt, const int2*
                 float3 m = f3(0.f, 0.f, 0.f);
                 if (l == hl) m = f3(mc[i * a.K + l]) * f3(mh);
                 direct = direct + (f3(s) + m);
+            }
+        }
+        if (gv.record && ac.y) {
+            int pid = __float_as_int(cur.o[i].w);
+            int bounce = (__float_as_int(cur.d[i].w) >> 16) & 0xff;
+            if ((pid % gv.rec_stride) == 0 && bounce < gv.rec_depth) {
+                float4* r = gv.rec + 4 * ((size_t)(pid / gv.rec_stride) * gv.rec_depth + bounce);
+                if (r[0].w != 0.f) r[1].w += 0.2126f * direct.x + 0.7152f * direct.y + 0.0722f * direct.z;
             }
         }
         if (ac.x >= 0) {
@@ -628,9 +673,17 @@ int grid_for(const void* kernel, int block, size_t smem = 0) {
 }  // namespace
 
 void launch_shade(int bk, int grid, cudaStream_t st, const DevScene& S, const WaveArgs& a, const PathRefs& cur, const float4* hits,
-                  const int* bcnt, const int* blist, int cap, const ShadeOut& so) {
+                  const int* bcnt, const int* blist, int cap, const ShadeOut& so, const GuideView& gv, bool guided) {
+    if (guided) {
+        switch (bk) {
+#define C2G_SHADE_G(B) case B: k_shade<B, true><<<grid, 128, 0, st>>>(S, a, cur, hits, bcnt, blist, cap, so, gv); return;
+            // guided buckets: diffuse, GGX/Beckmann reflection, plastic (exact sampling densities)
+            C2G_SHADE_G(0) C2G_SHADE_G(4) C2G_SHADE_G(5) C2G_SHADE_G(6) C2G_SHADE_G(7)
+#undef C2G_SHADE_G
+        }
+    }
     switch (bk) {
-#define C2G_SHADE_CASE(B) case B: k_shade<B><<<grid, 128, 0, st>>>(S, a, cur, hits, bcnt, blist, cap, so); break;
+#define C2G_SHADE_CASE(B) case B: k_shade<B, false><<<grid, 128, 0, st>>>(S, a, cur, hits, bcnt, blist, cap, so, gv); break;
         C2G_SHADE_CASE(0) C2G_SHADE_CASE(1) C2G_SHADE_CASE(2) C2G_SHADE_CASE(3) C2G_SHADE_CASE(4)
         C2G_SHADE_CASE(5) C2G_SHADE_CASE(6) C2G_SHADE_CASE(7) C2G_SHADE_CASE(8) C2G_SHADE_CASE(9)
 #undef C2G_SHADE_CASE
@@ -713,6 +766,14 @@ int GpuScene::upload(const HostScene& s, int tree, const RefTree* ref, const Sah
     C2G_CUDA(cudaMemset(sb_->film, 0, npx * sizeof(float4)));
     C2G_CUDA(cudaMemset(sb_->film_m2, 0, npx * sizeof(float4)));
     sb_->n_lights = S.n_lights;
+    for (int k = 0; k < 3; k++) { box_lo_[k] = INFINITY; box_hi_[k] = -INFINITY; }
+    for (size_t o = 0; o < s.objs.size(); o++) {
+        float b[6];
+        s.object_box((int)o, b);
+        for (int k = 0; k < 3; k++) { box_lo_[k] = std::min(box_lo_[k], b[k]); box_hi_[k] = std::max(box_hi_[k], b[3 + k]); }
+    }
+    guide_steps_ = 0;
+    guide_.release(arena);  // a new scene trains a new network
     present_buckets_ = 1 << kBucketMiss;
     for (const ObjInfo& o : s.objs) present_buckets_ |= 1 << (o.material < 0 ? kBucketNone : s.mats[o.material].type);
     // wave buffers depend on the light count: drop them
@@ -761,10 +822,11 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
     if (!sb_->film) { err = "no scene loaded"; return C2G_ERR_STATE; }
     if (p.width != film_w_ || p.height != film_h_) { err = "render size differs from the loaded film size"; return C2G_ERR_INVALID; }
     if (p.max_depth < 0 || p.sample_count < 0 || p.sample_begin < 0) { err = "invalid render parameters"; return C2G_ERR_INVALID; }
-    if (p.integrator != C2G_INTEGRATOR_PATH && p.integrator != C2G_INTEGRATOR_DIRECT) {
-        err = "integrator not available in this build";
-        return C2G_ERR_UNSUPPORTED;
+    if (p.integrator != C2G_INTEGRATOR_PATH && p.integrator != C2G_INTEGRATOR_DIRECT && p.integrator != C2G_INTEGRATOR_GUIDED) {
+        err = "unknown integrator";
+        return C2G_ERR_INVALID;
     }
+    const bool guided = p.integrator == C2G_INTEGRATOR_GUIDED;
     if (p.max_depth > 255) { err = "max_depth above 255"; return C2G_ERR_INVALID; }
     DevScene S = sb_->S;
     S.anyhit_clip = p.accel == C2G_ACCEL_BVH ? 1 : 0;
@@ -824,7 +886,7 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         g_raygen = grid_for((const void*)k_raygen, 256);
         g_ext = grid_for((const void*)k_extend<false>, 128);
         g_ext_c = grid_for((const void*)k_extend<true>, 128);
-        g_shade = grid_for((const void*)k_shade<MAT_DIFFUSE>, 128);
+        g_shade = grid_for((const void*)k_shade<MAT_DIFFUSE, false>, 128);
         g_sh = grid_for((const void*)k_shadow<false>, 128);
         g_sh_c = grid_for((const void*)k_shadow<true>, 128);
         g_mis = grid_for((const void*)k_mis<false>, 128);
@@ -854,6 +916,10 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         cudaEventRecord(pool[used].b, st);
         used++;
     };
+    if (guided) {
+        int rc = guide_.init(arena, w.P, p.max_depth, box_lo_, box_hi_, p.seed, err);
+        if (rc) return rc;
+    }
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
@@ -865,6 +931,8 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         a.sample0 = p.sample_begin + s0;
         C2G_CUDA(cudaMemsetAsync(C, 0, 256, st));
         PathRefs buf[2] = {{w.o[0], w.d[0], w.beta[0], w.L[0]}, {w.o[1], w.d[1], w.beta[1], w.L[1]}};
+        // guided waves record training vertices; they sample the mixture once the network has trained
+        const GuideView gv = guided ? guide_.view(true, guide_steps_ >= guide_warmup_) : GuideView{};
         begin(C2G_K_RAYGEN);
         k_raygen<<<g_raygen, 256, 0, st>>>(S, a, buf[0], w.out_L, C + 0);
         end();
@@ -880,11 +948,17 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
                 k_extend<false><<<g_ext, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
                                                          C + kCntBucket, w.bucket_list, (int)w.P, cnt);
             end();
+            if (gv.sample) {
+                begin(C2G_K_GUIDE);
+                guide_.infer(st, &S, buf[cur].o, buf[cur].d, w.hit, C + kCntBucket, w.bucket_list, (int)w.P, present_buckets_);
+                end();
+                launches++;
+            }
             ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc, w.mis_hit};
             for (int bk = 0; bk < kBuckets; bk++) {
                 if (!(present_buckets_ & (1 << bk))) continue;
                 begin(C2G_K_SHADE);
-                launch_shade(bk, g_shade, st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so);
+                launch_shade(bk, g_shade, st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so, gv, guided);
                 end();
                 launches++;
             }
@@ -897,7 +971,7 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
             else k_mis<false><<<g_mis, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
             end();
             begin(C2G_K_ACCUM);
-            k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.mis_hit, w.out_L, C + cur);
+            k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.mis_hit, w.out_L, C + cur, gv);
             end();
             launches += 4;
             cur = nxt;
@@ -907,6 +981,14 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         end();
         launches += 2;
         waves++;
+        if (guided) {
+            // online training on this wave's recorded vertices (batch build, fused fwd/bwd, Adam)
+            begin(C2G_K_GUIDE);
+            guide_.train(st, w.out_L, a.nslots * a.wave_samples, guide_train_steps_);
+            end();
+            launches += 1 + 2 * guide_train_steps_;
+            guide_steps_++;
+        }
     }
     cudaEventRecord(ev1, st);
     C2G_CUDA(cudaGetLastError());
@@ -1089,7 +1171,7 @@ int GpuScene::render_noalloc(const c2g_render_params& p, float4* film_dev, cudaS
     S.closest_box = p.accel == C2G_ACCEL_BVH ? 1 : 0;
     S.seed = p.seed;
     const int g_raygen = grid_for((const void*)k_raygen, 256), g_ext = grid_for((const void*)k_extend<false>, 128);
-    const int g_shade = grid_for((const void*)k_shade<MAT_DIFFUSE>, 128), g_sh = grid_for((const void*)k_shadow<false>, 128);
+    const int g_shade = grid_for((const void*)k_shade<MAT_DIFFUSE, false>, 128), g_sh = grid_for((const void*)k_shadow<false>, 128);
     const int g_mis = grid_for((const void*)k_mis<false>, 128), g_acc = grid_for((const void*)k_accumulate, 256);
     const int g_film = grid_for((const void*)k_film, 256);
     int* C = w.counters;
@@ -1108,10 +1190,11 @@ int GpuScene::render_noalloc(const c2g_render_params& p, float4* film_dev, cudaS
                                                      C + kCntBucket, w.bucket_list, (int)w.P, nullptr);
             ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc, w.mis_hit};
             for (int bk = 0; bk < kBuckets; bk++)
-                if (present_buckets_ & (1 << bk)) launch_shade(bk, g_shade, st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so);
+                if (present_buckets_ & (1 << bk))
+                    launch_shade(bk, g_shade, st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so, GuideView{}, false);
             k_shadow<false><<<g_sh, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, nullptr);
             k_mis<false><<<g_mis, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, nullptr);
-            k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.mis_hit, w.out_L, C + cur);
+            k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.mis_hit, w.out_L, C + cur, GuideView{});
             cur = nxt;
         }
         // the caller's film gets the radiance sums and weights; the sums of squares stay in scratch

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../c2g_types.h"
+#include "guide.h"
 #include "../../../include/c2g.h"
 
 namespace c2g {
@@ -55,6 +56,14 @@ public:
     // Same render as render() into a caller-owned film, with no device allocation (render.cu).
     int render_noalloc(const c2g_render_params& p, float4* film_dev, cudaStream_t st, std::string& err);
     void set_counting(int flags) { counting_ = flags; }
+    GuideStats guide_stats() { return guide_.stats(); }
+    GuideTrainer& guide() { return guide_; }
+    // Guided integrator schedule: waves of plain BSDF sampling before the mixture is used, and
+    // Adam steps per wave.
+    void set_guide_schedule(int warmup_waves, int train_steps) {
+        guide_warmup_ = warmup_waves < 0 ? 0 : warmup_waves;
+        guide_train_steps_ = train_steps < 0 ? 0 : train_steps;
+    }
     const c2g_stats& stats() const { return stats_; }
     int check_device_error(std::string& err);
 
@@ -63,6 +72,11 @@ private:
     WaveBuffers* wb_;
     int counting_ = 0;
     int present_buckets_ = 0;  // material buckets the loaded scene can produce
+    GuideTrainer guide_;       // learned proposal of the guided integrator
+    int guide_steps_ = 0;      // guided waves rendered on the loaded scene
+    int guide_warmup_ = 2;     // guided waves that only record (BSDF sampling) before the mixture is used
+    int guide_train_steps_ = 1;  // Adam steps per guided wave
+    float box_lo_[3] = {0, 0, 0}, box_hi_[3] = {1, 1, 1};  // scene bounds (network input range)
     c2g_stats stats_{};
     int film_w_ = 0, film_h_ = 0;
 };

@@ -164,6 +164,48 @@ class Context:
         self.check(self._lib.c2g_camera_rays(self._h, n, N.fptr(pos2), N.fptr(o), N.fptr(d)))
         return o, d
 
+    # ---- learned guiding proposal (GuidedPathTracer)
+    def guide_reset(self, box_lo, box_hi, seed: int = 0) -> None:
+        lo = np.ascontiguousarray(box_lo, np.float32)
+        hi = np.ascontiguousarray(box_hi, np.float32)
+        self.check(self._lib.c2g_guide_reset(self._h, N.fptr(lo), N.fptr(hi), int(seed)))
+
+    def guide_params(self) -> np.ndarray:
+        p = np.zeros(N.GUIDE_PARAMS, np.float32)
+        self.check(self._lib.c2g_guide_get_params(self._h, N.fptr(p)))
+        return p
+
+    def guide_set_params(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.size == N.GUIDE_PARAMS
+        self.check(self._lib.c2g_guide_set_params(self._h, N.fptr(p)))
+
+    def guide_eval(self, xnw: np.ndarray) -> np.ndarray:
+        """Raw outputs (n, 40) for inputs (n, 9) = position, normal, outgoing direction."""
+        x = np.ascontiguousarray(xnw, np.float32).reshape(-1, 9)
+        out = np.zeros((x.shape[0], N.GUIDE_OUTPUTS), np.float32)
+        self.check(self._lib.c2g_guide_eval(self._h, x.shape[0], N.fptr(x), N.fptr(out)))
+        return out
+
+    def guide_gradient(self, samples: np.ndarray):
+        """(grad, loss) of sum w * -log q(wi) for samples (n, 13) = x, n, wo, wi, w."""
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 13)
+        g = np.zeros(N.GUIDE_PARAMS, np.float32)
+        loss = C.c_double(0.0)
+        self.check(self._lib.c2g_guide_gradient(self._h, s.shape[0], N.fptr(s), N.fptr(g), C.byref(loss)))
+        return g, loss.value
+
+    def guide_stats(self):
+        """(loss, records, steps) of the last guided training step."""
+        loss, rec, steps = C.c_double(0.0), C.c_int(0), C.c_int(0)
+        self.check(self._lib.c2g_guide_stats(self._h, C.byref(loss), C.byref(rec), C.byref(steps)))
+        return loss.value, rec.value, steps.value
+
+    def guide_config(self, learning_rate: float = 2e-3, bsdf_fraction: float = 0.5, warmup_waves: int = 2,
+                     train_steps: int = 1) -> None:
+        self.check(self._lib.c2g_guide_config(self._h, float(learning_rate), float(bsdf_fraction), int(warmup_waves),
+                                              int(train_steps)))
+
 
 class Integrator:
     """String factory of the integrators (Integrator::LoadIntegrator)."""

@@ -158,6 +158,32 @@ int c2g_render_noalloc(c2g_ctx* ctx, const c2g_render_params* params, float* fil
 /* C2G_COUNT_* flags (0 = off): traversal counters (slower kernels) and per-launch timing. */
 int c2g_set_counting(c2g_ctx* ctx, int flags);
 
+/* ---- learned guiding proposal (C2G_INTEGRATOR_GUIDED) -------------------------------------------
+ * No counterpart in the reference, which has no guided integrator; these calls configure and
+ * inspect the network the guided path tracer trains online.  The network maps (position in the
+ * scene box, shading normal, outgoing direction) to an 8-lobe von Mises-Fisher mixture over
+ * directions; its weights are one flat FP32 vector of C2G_GUIDE_PARAMS values, layer by layer
+ * W (inputs x outputs, row-major) then b, for layers 80->64->64->64->48 (the last 8 outputs are
+ * padding, kept zero).  Loading a scene discards the network; a guided render creates one. */
+#define C2G_GUIDE_PARAMS 16624
+#define C2G_GUIDE_OUTPUTS 40
+/* Draw a fresh seeded network for the box [lo, hi] (normalises positions) and clear Adam. */
+int c2g_guide_reset(c2g_ctx* ctx, const float box_lo[3], const float box_hi[3], unsigned long long seed);
+int c2g_guide_set_params(c2g_ctx* ctx, const float* params);
+int c2g_guide_get_params(c2g_ctx* ctx, float* params);
+/* Raw outputs (per lobe: mean direction xyz unnormalised, concentration pre-softplus, weight logit)
+ * for n inputs of 9 floats (x, n, wo) -> out[n * C2G_GUIDE_OUTPUTS]. */
+int c2g_guide_eval(c2g_ctx* ctx, int n, const float* xnw, float* out);
+/* Summed gradient over n samples of 13 floats (x, n, wo, wi, w) of sum_j w_j * -log q(wi_j) as the
+ * training kernel computes it (BF16 operands, FP32 accumulation), written to grad[C2G_GUIDE_PARAMS];
+ * loss = sum w (-log q) / sum w.  No optimiser step. */
+int c2g_guide_gradient(c2g_ctx* ctx, int n, const float* samples, float* grad, double* loss);
+/* Training state of the last guided render: weighted NLL of the last batch, its size, Adam steps. */
+int c2g_guide_stats(c2g_ctx* ctx, double* loss, int* records, int* steps);
+/* learning_rate (Adam), bsdf_fraction (one-sample MIS probability of the BSDF technique, (0, 1]),
+ * warmup_waves (guided waves that only train), train_steps (Adam steps per wave). */
+int c2g_guide_config(c2g_ctx* ctx, float learning_rate, float bsdf_fraction, int warmup_waves, int train_steps);
+
 /* ---- ray queries (Scene::Intersect / Scene::IntersectTest, Scene.cpp:50-59) ---------------- */
 /* Closest hit (any_hit = 0): obj = scene index of the hit object or -1, t = distance.
  * Any hit (any_hit = 1): obj = 1 if occluded else 0 over [tmin, tmax], ignoring object ignore[i]
