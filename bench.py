@@ -240,8 +240,8 @@ def run_ours(args) -> None:
     clocks.start()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
-    kernel_ms = np.zeros(8)
-    kernel_n = np.zeros(8)
+    kernel_ms = np.zeros(N.K_KINDS)
+    kernel_n = np.zeros(N.K_KINDS)
     launches = 0
     ev0.record(stream)
     for i in range(args.steps):
@@ -307,7 +307,7 @@ def run_ours(args) -> None:
             "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
             "alg_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
             "per_ray": {"nodes": nodes / max(1, rays), "prims": prims / max(1, rays)}}
-    share = {names[k]: float(kernel_ms[k] / max(1e-9, kernel_ms.sum())) for k in range(8) if kernel_n[k] > 0}
+    share = {names[k]: float(kernel_ms[k] / max(1e-9, kernel_ms.sum())) for k in range(N.K_KINDS) if kernel_n[k] > 0}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         try:

@@ -54,15 +54,17 @@ class RenderParams(C.Structure):
                 ("wave_paths", C.c_int), ("seed", C.c_uint64)]
 
 
-K_RAYGEN, K_EXTEND, K_SHADE, K_SHADOW, K_MIS, K_ACCUM, K_FILM, K_GUIDE = range(8)
-KERNEL_NAMES = ["raygen", "extend", "shade", "shadow", "mis", "accumulate", "film", "guide"]
+K_RAYGEN, K_EXTEND, K_SHADE, K_SHADOW, K_MIS, K_ACCUM, K_FILM, K_GUIDE, K_TRAIN = range(9)
+K_KINDS = 10
+KERNEL_NAMES = ["raygen", "extend", "shade", "shadow", "mis", "accumulate", "film", "guide", "train", "-"]
 COUNT_TRAVERSAL = 1
 COUNT_TIMING = 2
 
 
 class Stats(C.Structure):
-    _fields_ = [("seconds", C.c_double), ("paths", C.c_double), ("rays", C.c_double * 8), ("nodes", C.c_double * 8),
-                ("prims", C.c_double * 8), ("kernel_ms", C.c_double * 8), ("kernel_count", C.c_int * 8),
+    _fields_ = [("seconds", C.c_double), ("paths", C.c_double), ("rays", C.c_double * K_KINDS),
+                ("nodes", C.c_double * K_KINDS), ("prims", C.c_double * K_KINDS), ("kernel_ms", C.c_double * K_KINDS),
+                ("kernel_count", C.c_int * K_KINDS),
                 ("kernel_launches", C.c_int), ("waves", C.c_int)]
 
 

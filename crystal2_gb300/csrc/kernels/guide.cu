@@ -1,5 +1,5 @@
 // Learned guiding proposal: inference over shading buckets, online training (fused forward +
-// backward on tensor-core tiles, FP32 weight-gradient reduction) and the Adam update.
+// backward + weight gradients on tensor-core tiles) and the Adam update.
 //
 // Training target (neural importance sampling, Mueller et al. 2019): minimise the KL divergence
 // from the product f(wo, wi) cos(wi) Li(wi) to the mixture q(wi | x, n, wo).  Its gradient is
@@ -21,11 +21,22 @@ namespace c2g {
 
 namespace {
 
-constexpr int kLdA0 = 88;    // 80 + 8 (bank-conflict-free rows)
-constexpr int kLdH = 72;     // 64 + 8
-constexpr int kLdO = 56;     // 48 + 8 (BF16 output gradients)
-constexpr int kLdF = 48;     // FP32 outputs (forward)
-constexpr int kLdG = 68;     // FP32 scratch of the training kernel (64 columns + 4)
+// Shared-memory tile strides (elements): rows padded by 8 so that the eight row groups of an MMA
+// fragment load fall in distinct banks.
+constexpr int kLdA0 = 88;    // encoded inputs (80)
+constexpr int kLdH = 72;     // hidden activations / deltas (64)
+constexpr int kLdO = 56;     // output-layer gradient (48)
+constexpr int kLdF = 48;     // FP32 outputs (inference)
+constexpr int kLdOF = 52;    // FP32 outputs (training)
+
+// Padded weight copies in shared memory.  Forward: wt_l (N_l rows of K_l + 8).  Backward: wn_l
+// (K_l rows of N_l + 8), layers 1..3 (the input gradient of layer 0 is never needed).
+__host__ __device__ constexpr int fw_ld(int l) { return guide_k(l) + 8; }
+__host__ __device__ constexpr int fw_off(int l) { return l == 0 ? 0 : fw_off(l - 1) + guide_n(l - 1) * fw_ld(l - 1); }
+constexpr int kFwElems = fw_off(4);
+__host__ __device__ constexpr int bw_ld(int l) { return guide_n(l) + 8; }
+__host__ __device__ constexpr int bw_off(int l) { return l <= 1 ? 0 : bw_off(l - 1) + guide_k(l - 1) * bw_ld(l - 1); }
+constexpr int kBwElems = bw_off(4);
 
 __device__ __forceinline__ float luminance(float3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
 
@@ -36,64 +47,140 @@ __host__ __device__ constexpr bool bucket_guided(int b) {
            b == MAT_PLASTIC_BECKMANN;
 }
 
-// Forward pass of one warp's 32 samples: `in` (per lane, FP32) -> F (32 x kLdF FP32 outputs).
-// `wts` = the four wt_l matrices back to back (shared memory); A, Bb = two per-warp BF16 tiles.
-// F aliases A.
-__device__ __forceinline__ void warp_forward(const GuideNet& net, const __nv_bfloat16* wts, const float* in,
-                                             __nv_bfloat16* A, __nv_bfloat16* Bb, float* F) {
-    const int lane = threadIdx.x & 31;
-    constexpr int o1 = kGuideIn * kGuideHidden, o2 = o1 + kGuideHidden * kGuideHidden, o3 = o2 + kGuideHidden * kGuideHidden;
+__device__ __forceinline__ void stage_forward_weights(const GuideNet& net, __nv_bfloat16* wts) {
 #pragma unroll
-    for (int k = 0; k < kGuideIn; k += 2)
-        *reinterpret_cast<uint32_t*>(A + lane * kLdA0 + k) = pack_bf16(in[k], in[k + 1]);
+    for (int l = 0; l < kGuideLayers; l++) {
+        const int K = guide_k(l), N = guide_n(l), vpr = K / 8;
+        const uint4* src = reinterpret_cast<const uint4*>(net.bf + guide_bf_off(l));
+        for (int i = threadIdx.x; i < N * vpr; i += blockDim.x) {
+            int n = i / vpr, c = i - n * vpr;
+            *reinterpret_cast<uint4*>(wts + fw_off(l) + n * fw_ld(l) + c * 8) = src[i];
+        }
+    }
+}
+
+__device__ __forceinline__ void stage_backward_weights(const GuideNet& net, __nv_bfloat16* wns) {
+#pragma unroll
+    for (int l = 1; l < kGuideLayers; l++) {
+        const int K = guide_k(l), N = guide_n(l), vpr = N / 8;
+        const uint4* src = reinterpret_cast<const uint4*>(net.bf + guide_bf_off(l) + K * N);
+        for (int i = threadIdx.x; i < K * vpr; i += blockDim.x) {
+            int k = i / vpr, c = i - k * vpr;
+            *reinterpret_cast<uint4*>(wns + bw_off(l) + k * bw_ld(l) + c * 8) = src[i];
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+// MT 16-row tiles through one layer: out[16 MT x N] = epilogue(in[16 MT x K] @ W + bias), W given
+// as w = N x K (row stride ldw).  A fragments are loaded once and reused across the N columns;
+// each B fragment serves all MT row tiles.  Epilogue: FP32 store to outf when non-null; else
+// optional ReLU, optional mask (value kept where mask > 0, the ReLU derivative) and a BF16 store.
+template <int MT, int K, int N>
+__device__ __forceinline__ void mma_rows(const __nv_bfloat16* in, int ldi, const __nv_bfloat16* w, int ldw,
+                                         const float* bias, __nv_bfloat16* out, int ldo, bool relu, float* outf, int ldf,
+                                         const __nv_bfloat16* mask, int ldm) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    uint32_t a[MT][K / 16][4];
+#pragma unroll
+    for (int m = 0; m < MT; m++)
+#pragma unroll
+        for (int kk = 0; kk < K / 16; kk++) {
+            const __nv_bfloat16* r0 = in + (m * 16 + g) * ldi + kk * 16 + 2 * t;
+            a[m][kk][0] = ld32(r0);
+            a[m][kk][1] = ld32(r0 + 8 * ldi);
+            a[m][kk][2] = ld32(r0 + 8);
+            a[m][kk][3] = ld32(r0 + 8 * ldi + 8);
+        }
+#pragma unroll
+    for (int n0 = 0; n0 < N; n0 += 8) {
+        float d[MT][4];
+        const float b0 = bias ? bias[n0 + 2 * t] : 0.f, b1 = bias ? bias[n0 + 2 * t + 1] : 0.f;
+#pragma unroll
+        for (int m = 0; m < MT; m++) { d[m][0] = b0; d[m][1] = b1; d[m][2] = b0; d[m][3] = b1; }
+#pragma unroll
+        for (int kk = 0; kk < K / 16; kk++) {
+            uint32_t b[2];
+            const __nv_bfloat16* wr = w + (n0 + g) * ldw + kk * 16 + 2 * t;
+            b[0] = ld32(wr);
+            b[1] = ld32(wr + 8);
+#pragma unroll
+            for (int m = 0; m < MT; m++) mma16816(d[m], a[m][kk], b);
+        }
+#pragma unroll
+        for (int m = 0; m < MT; m++) {
+            const int r0 = m * 16 + g, r1 = r0 + 8, c = n0 + 2 * t;
+            if (outf) {
+                outf[r0 * ldf + c] = d[m][0];
+                outf[r0 * ldf + c + 1] = d[m][1];
+                outf[r1 * ldf + c] = d[m][2];
+                outf[r1 * ldf + c + 1] = d[m][3];
+                continue;
+            }
+            if (relu) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) d[m][q] = fmaxf(d[m][q], 0.f);
+            }
+            if (mask) {
+                __nv_bfloat162 k0 = *reinterpret_cast<const __nv_bfloat162*>(mask + r0 * ldm + c);
+                __nv_bfloat162 k1 = *reinterpret_cast<const __nv_bfloat162*>(mask + r1 * ldm + c);
+                if (!(__low2float(k0) > 0.f)) d[m][0] = 0.f;
+                if (!(__high2float(k0) > 0.f)) d[m][1] = 0.f;
+                if (!(__low2float(k1) > 0.f)) d[m][2] = 0.f;
+                if (!(__high2float(k1) > 0.f)) d[m][3] = 0.f;
+            }
+            *reinterpret_cast<uint32_t*>(out + r0 * ldo + c) = pack_bf16(d[m][0], d[m][1]);
+            *reinterpret_cast<uint32_t*>(out + r1 * ldo + c) = pack_bf16(d[m][2], d[m][3]);
+        }
+    }
+}
+
+// Forward pass of one warp's 32 samples (two row tiles): A holds the encoded inputs (ld kLdA0);
+// the FP32 outputs land in F (ld kLdF), which aliases A.  `wts` = padded forward weights.
+__device__ __forceinline__ void warp_forward32(const GuideNet& net, const __nv_bfloat16* wts, __nv_bfloat16* A,
+                                               __nv_bfloat16* Bb, float* F) {
+    mma_rows<2, 80, 64>(A, kLdA0, wts + fw_off(0), fw_ld(0), net.params + guide_b_off(0), Bb, kLdH, true, nullptr, 0, nullptr, 0);
     __syncwarp();
-    for (int m = 0; m < 2; m++)
-        tile_layer<80, 64>(A + m * 16 * kLdA0, kLdA0, wts, net.params + guide_b_off(0), Bb + m * 16 * kLdH, kLdH, true, nullptr, 0);
+    mma_rows<2, 64, 64>(Bb, kLdH, wts + fw_off(1), fw_ld(1), net.params + guide_b_off(1), A, kLdH, true, nullptr, 0, nullptr, 0);
     __syncwarp();
-    for (int m = 0; m < 2; m++)
-        tile_layer<64, 64>(Bb + m * 16 * kLdH, kLdH, wts + o1, net.params + guide_b_off(1), A + m * 16 * kLdH, kLdH, true, nullptr, 0);
+    mma_rows<2, 64, 64>(A, kLdH, wts + fw_off(2), fw_ld(2), net.params + guide_b_off(2), Bb, kLdH, true, nullptr, 0, nullptr, 0);
     __syncwarp();
-    for (int m = 0; m < 2; m++)
-        tile_layer<64, 64>(A + m * 16 * kLdH, kLdH, wts + o2, net.params + guide_b_off(2), Bb + m * 16 * kLdH, kLdH, true, nullptr, 0);
-    __syncwarp();
-    for (int m = 0; m < 2; m++)
-        tile_layer<64, 48>(Bb + m * 16 * kLdH, kLdH, wts + o3, net.params + guide_b_off(3), nullptr, 0, false, F + m * 16 * kLdF, kLdF);
+    mma_rows<2, 64, 48>(Bb, kLdH, wts + fw_off(3), fw_ld(3), net.params + guide_b_off(3), nullptr, 0, false, F, kLdF, nullptr, 0);
     __syncwarp();
 }
 
-// Copy the forward weights (wt_0..wt_3) into shared memory.
-__device__ __forceinline__ void stage_forward_weights(const GuideNet& net, __nv_bfloat16* wts) {
-    constexpr int o1 = kGuideIn * kGuideHidden, o2 = o1 + kGuideHidden * kGuideHidden, o3 = o2 + kGuideHidden * kGuideHidden;
-    constexpr int total = o3 + kGuideHidden * kGuideOutPad;
-    for (int i = threadIdx.x; i < total; i += blockDim.x) {
-        int l = i >= o3 ? 3 : i >= o2 ? 2 : i >= o1 ? 1 : 0;
-        int base = l == 3 ? o3 : l == 2 ? o2 : l == 1 ? o1 : 0;
-        wts[i] = net.bf[guide_bf_off(l) + (i - base)];
-    }
-    __syncthreads();
+__device__ __forceinline__ void store_inputs(__nv_bfloat16* row, const float* in) {
+#pragma unroll
+    for (int k = 0; k < kGuideIn; k += 2) *reinterpret_cast<uint32_t*>(row + k) = pack_bf16(in[k], in[k + 1]);
 }
 
 // ---- inference ---------------------------------------------------------------------------------
-// 128 threads; dynamic shared memory: forward weights (32 KB) + two per-warp tiles.
+// 128 threads, 32 samples per warp; dynamic shared memory: padded forward weights + per warp an
+// input/output tile (the FP32 outputs overwrite the inputs) and a hidden tile.
 constexpr int kInferWarps = 4;
-constexpr int kTileBytes = 32 * kLdF * 4;  // 6144: holds 32 x 88 BF16 rows or 32 x 48 FP32 rows
+constexpr int kTileA = 32 * kLdF * 4;      // 6144 B: 32 x 88 BF16 inputs or 32 x 48 FP32 outputs
+constexpr int kTileB = 32 * kLdH * 2;      // 4608 B
+constexpr size_t kInferSmem = kFwElems * 2 + kInferWarps * (kTileA + kTileB);
 
 __global__ void __launch_bounds__(128) k_guide_infer(DevScene S, GuideNet net, const float4* __restrict__ ray_o,
                                                      const float4* __restrict__ ray_d, const float4* __restrict__ hits,
                                                      const int* bucket_cnt, const int* __restrict__ bucket_list, int cap,
                                                      int mask, float* out) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __nv_bfloat16* wts = reinterpret_cast<__nv_bfloat16*>(smem);  // wt_0 .. wt_3 back to back
+    __nv_bfloat16* wts = reinterpret_cast<__nv_bfloat16*>(smem);
     stage_forward_weights(net, wts);
+    __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* wbase = smem + 2 * 16384 + warp * 2 * kTileBytes;
+    unsigned char* wbase = smem + kFwElems * 2 + warp * (kTileA + kTileB);
     __nv_bfloat16* A = reinterpret_cast<__nv_bfloat16*>(wbase);
-    __nv_bfloat16* Bb = reinterpret_cast<__nv_bfloat16*>(wbase + kTileBytes);
+    __nv_bfloat16* Bb = reinterpret_cast<__nv_bfloat16*>(wbase + kTileA);
     float* F = reinterpret_cast<float*>(wbase);
     // work list = the guided buckets back to back
     int total = 0;
-    int bstart[10], bcnt[10];
-    for (int b = 0; b < 10; b++) {
+    int bstart[kBuckets], bcnt[kBuckets];
+#pragma unroll
+    for (int b = 0; b < kBuckets; b++) {
         bstart[b] = total;
         bcnt[b] = ((mask >> b) & 1) ? bucket_cnt[b] : 0;
         total += bcnt[b];
@@ -104,7 +191,7 @@ __global__ void __launch_bounds__(128) k_guide_infer(DevScene S, GuideNet net, c
         int slot = -1;
         if (item < total) {
             int b = 0;
-            while (b < 9 && item >= bstart[b] + bcnt[b]) b++;
+            while (b < kBuckets - 1 && item >= bstart[b] + bcnt[b]) b++;
             slot = bucket_list[(size_t)b * cap + (item - bstart[b])];
         }
         float in[kGuideIn];
@@ -118,11 +205,14 @@ __global__ void __launch_bounds__(128) k_guide_infer(DevScene S, GuideNet net, c
 #pragma unroll
             for (int k = 0; k < kGuideIn; k++) in[k] = 0.f;
         }
-        warp_forward(net, wts, in, A, Bb, F);
+        store_inputs(A + lane * kLdA0, in);
+        __syncwarp();
+        warp_forward32(net, wts, A, Bb, F);
         if (slot >= 0) {
-            float* dst = out + (size_t)slot * kGuideOut;
+            float4* dst = reinterpret_cast<float4*>(out + (size_t)slot * kGuideOut);
+            const float4* src = reinterpret_cast<const float4*>(F + lane * kLdF);
 #pragma unroll
-            for (int k = 0; k < kGuideOut; k++) dst[k] = F[lane * kLdF + k];
+            for (int k = 0; k < kGuideOut / 4; k++) dst[k] = src[k];
         }
         __syncwarp();
     }
@@ -134,10 +224,11 @@ __global__ void __launch_bounds__(128) k_guide_eval(GuideNet net, const float* _
     extern __shared__ __align__(16) unsigned char smem[];
     __nv_bfloat16* wts = reinterpret_cast<__nv_bfloat16*>(smem);
     stage_forward_weights(net, wts);
+    __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* wbase = smem + 2 * 16384 + warp * 2 * kTileBytes;
+    unsigned char* wbase = smem + kFwElems * 2 + warp * (kTileA + kTileB);
     __nv_bfloat16* A = reinterpret_cast<__nv_bfloat16*>(wbase);
-    __nv_bfloat16* Bb = reinterpret_cast<__nv_bfloat16*>(wbase + kTileBytes);
+    __nv_bfloat16* Bb = reinterpret_cast<__nv_bfloat16*>(wbase + kTileA);
     float* F = reinterpret_cast<float*>(wbase);
     const int gwarp = blockIdx.x * kInferWarps + warp, nwarps = gridDim.x * kInferWarps;
     for (int base = gwarp * 32; base < n; base += nwarps * 32) {
@@ -150,7 +241,9 @@ __global__ void __launch_bounds__(128) k_guide_eval(GuideNet net, const float* _
 #pragma unroll
             for (int k = 0; k < kGuideIn; k++) in[k] = 0.f;
         }
-        warp_forward(net, wts, in, A, Bb, F);
+        store_inputs(A + lane * kLdA0, in);
+        __syncwarp();
+        warp_forward32(net, wts, A, Bb, F);
         if (j < n) {
 #pragma unroll
             for (int k = 0; k < kGuideOut; k++) out[(size_t)j * kGuideOut + k] = F[lane * kLdF + k];
@@ -190,188 +283,239 @@ __global__ void k_guide_batch(float4* rec, int rec_cap, int rec_depth, int rec_s
         if ((threadIdx.x & 31) == 0 && m) basei = atomicAdd(batch_count, __popc(m));
         basei = __shfl_sync(0xffffffffu, basei, 0);
         int j = basei + __popc(m & ((1u << (threadIdx.x & 31)) - 1u));
-        if (ok && j < batch_cap) {
+        bool keep = ok && j < batch_cap;
+        if (keep) {
             batch[4 * j] = make_float4(r0.x, r0.y, r0.z, w);
             batch[4 * j + 1] = make_float4(r1.x, r1.y, r1.z, 0.f);
             batch[4 * j + 2] = make_float4(r2.x, r2.y, r2.z, 0.f);
             batch[4 * j + 3] = make_float4(r3.x, r3.y, r3.z, 0.f);
-            atomicAdd(stats + 2, w);
         }
+        float ws = keep ? w : 0.f;
+        for (int o = 16; o > 0; o >>= 1) ws += __shfl_xor_sync(0xffffffffu, ws, o);
+        if ((threadIdx.x & 31) == 0 && ws != 0.f) atomicAdd(stats + 2, ws);
     }
 }
 
-// ---- fused training step: forward + backward on tensor-core tiles, weight gradients in FP32 ----
-constexpr int kTrainWarps = 2;
-constexpr int kWarpTrainBytes = 32 * kLdA0 * 2 + 6 * 32 * kLdH * 2 + 32 * kLdG * 4 + 32 * kLdO * 2;
+// ---- fused training step ------------------------------------------------------------------------
+// 256 threads = 8 warps; a block takes 128 samples per iteration, 16 per warp.  Each warp runs the
+// forward and backward passes of its samples on tensor-core tiles (weights staged in shared memory,
+// activations and deltas kept as BF16 tiles).  The weight gradients dW_l = A_l^T D_l are then
+// tensor-core products over the block's 128 samples: the 124 (16 x 8) output tiles of the four
+// layers are split over the warps, each accumulating its tiles in FP32 registers for the whole
+// sweep (A^T and D fragments come from ldmatrix.trans); they reach global memory once per block.
+constexpr int kTrainWarps = 8;
+constexpr int kTrainRows = 16;
+// per-warp tile offsets (elements)
+constexpr int kTA0 = 0;
+constexpr int kTH1 = kTA0 + kTrainRows * kLdA0;
+constexpr int kTH2 = kTH1 + kTrainRows * kLdH;
+constexpr int kTH3 = kTH2 + kTrainRows * kLdH;
+constexpr int kTD1 = kTH3 + kTrainRows * kLdH;
+constexpr int kTD2 = kTD1 + kTrainRows * kLdH;
+constexpr int kTD3 = kTD2 + kTrainRows * kLdH;
+constexpr int kTDO = kTD3 + kTrainRows * kLdH;
+constexpr int kTWarpElems = kTDO + kTrainRows * kLdO;
+static_assert(kTrainRows * kLdOF * 4 <= 2 * kTrainRows * kLdH * 2, "FP32 outputs alias the d1/d2 tiles");
+constexpr size_t kTrainSmem = (size_t)(kFwElems + kBwElems + kTrainWarps * kTWarpElems) * 2;
+// dW tiles: layer 0 5 x 8, layers 1-2 4 x 8, layer 3 4 x 5 (the padded output columns are skipped)
+constexpr int kDwTiles = 40 + 32 + 32 + 20;
+constexpr int kDwPerWarp = (kDwTiles + kTrainWarps - 1) / kTrainWarps;
 
-__device__ __forceinline__ float bf(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t* r, const void* p) {
+    uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x2_trans(uint32_t* r, const void* p) {
+    uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n" : "=r"(r[0]), "=r"(r[1]) : "r"(a));
+}
 
-__global__ void __launch_bounds__(64) k_guide_train(GuideNet net, const float4* __restrict__ batch, const int* batch_count,
-                                                    int batch_cap, float* grad, float* stats) {
+__device__ __forceinline__ void dw_tile(int idx, int& l, int& mt, int& nt) {
+    if (idx < 40) { l = 0; mt = idx >> 3; nt = idx & 7; }
+    else if (idx < 72) { l = 1; mt = (idx - 40) >> 3; nt = (idx - 40) & 7; }
+    else if (idx < 104) { l = 2; mt = (idx - 72) >> 3; nt = (idx - 72) & 7; }
+    else { l = 3; mt = (idx - 104) / 5; nt = (idx - 104) % 5; }
+}
+
+// Gradient of w * -log q(wi) with respect to the 40 raw outputs o (see the oracle for the
+// formulas); returns -log q.  g[40..47] (padding) are left to the caller.
+__device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, float w, float* g) {
+    Lobe L[kGuideLobes];
+    guide_lobes(o, L);
+    float p[kGuideLobes], q = 0.f;
+#pragma unroll
+    for (int k = 0; k < kGuideLobes; k++) { p[k] = L[k].w * vmf_pdf(L[k], wi); q += p[k]; }
+    q = fmaxf(q, 1e-20f);
+    const float inv_q = 1.f / q;
+#pragma unroll
+    for (int k = 0; k < kGuideLobes; k++) {
+        const float r = p[k] * inv_q;
+        const float kap = L[k].kappa;
+        const float c = dot(L[k].mu, wi);
+        // d log vMF / d kappa = 1/kappa - 2 e^-2k / (1 - e^-2k) + (mu.wi - 1)
+        const float e2 = __expf(-2.f * kap);
+        const float dk = 1.f / kap - 2.f * e2 / fmaxf(-expm1f(-2.f * kap), 1e-20f) + (c - 1.f);
+        const float kraw = o[5 * k + 3];
+        float sig = 1.f / (1.f + __expf(-kraw));
+        if (kap >= 2000.f) sig = 0.f;
+        const float3 m = f3(o[5 * k], o[5 * k + 1], o[5 * k + 2]);
+        const float len = fmaxf(sqrtf(dot(m, m)), 1e-12f);
+        const float3 dm = (wi - L[k].mu * c) * (kap / len);
+        g[5 * k + 0] = -w * r * dm.x;
+        g[5 * k + 1] = -w * r * dm.y;
+        g[5 * k + 2] = -w * r * dm.z;
+        g[5 * k + 3] = -w * r * dk * sig;
+        g[5 * k + 4] = -w * (r - L[k].w);
+    }
+#pragma unroll
+    for (int k = 0; k < kGuideOut; k++) {
+        const float v = g[k];
+        g[k] = isfinite(v) ? fminf(fmaxf(v, -1e3f), 1e3f) : 0.f;
+    }
+    return -__logf(q);
+}
+
+__global__ void __launch_bounds__(256, 1) k_guide_train(GuideNet net, const float4* __restrict__ batch, const int* batch_count,
+                                                        int batch_cap, float* grad, float* stats) {
     extern __shared__ __align__(16) unsigned char smem[];
-    float* gacc = reinterpret_cast<float*>(smem);  // kGuideParams block-local gradient sums
-    for (int i = threadIdx.x; i < kGuideParams; i += blockDim.x) gacc[i] = 0.f;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* wb = smem + kGuideParams * 4 + warp * kWarpTrainBytes;
-    __nv_bfloat16* a0 = reinterpret_cast<__nv_bfloat16*>(wb);
-    __nv_bfloat16* h1 = a0 + 32 * kLdA0;
-    __nv_bfloat16* h2 = h1 + 32 * kLdH;
-    __nv_bfloat16* h3 = h2 + 32 * kLdH;
-    __nv_bfloat16* d1 = h3 + 32 * kLdH;   // gradient at the input of layer 1 (masked by h1)
-    __nv_bfloat16* d2 = d1 + 32 * kLdH;
-    __nv_bfloat16* d3 = d2 + 32 * kLdH;
-    float* of = reinterpret_cast<float*>(d3 + 32 * kLdH);
-    __nv_bfloat16* dout = reinterpret_cast<__nv_bfloat16*>(of + 32 * kLdG);
+    __nv_bfloat16* wts = reinterpret_cast<__nv_bfloat16*>(smem);
+    __nv_bfloat16* wns = wts + kFwElems;
+    __nv_bfloat16* tiles = wns + kBwElems;
+    stage_forward_weights(net, wts);
+    stage_backward_weights(net, wns);
     __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __nv_bfloat16* T = tiles + warp * kTWarpElems;
+    float* OF = reinterpret_cast<float*>(T + kTD1);
     const int n = min(*batch_count, batch_cap);
     const float mean_w = stats[2] / fmaxf(1.f, (float)n);
-    const __nv_bfloat16* wt[4];
-    const __nv_bfloat16* wn[4];
-    for (int l = 0; l < 4; l++) {
-        wt[l] = net.bf + guide_bf_off(l);
-        wn[l] = wt[l] + guide_k(l) * guide_n(l);
-    }
+
+    float acc[kDwPerWarp][4];
+#pragma unroll
+    for (int q = 0; q < kDwPerWarp; q++) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+    // bias gradients: thread -> one of the 64 + 64 + 64 + 40 bias columns
+    float bacc = 0.f;
+    int bl = -1, bc = 0;
+    if (threadIdx.x < 192) { bl = threadIdx.x >> 6; bc = threadIdx.x & 63; }
+    else if (threadIdx.x < 192 + kGuideOut) { bl = 3; bc = threadIdx.x - 192; }
     float loss = 0.f, wsum = 0.f;
-    const int per_iter = kTrainWarps * 32;
-    for (int base = blockIdx.x * per_iter; base < n; base += gridDim.x * per_iter) {
-        const int j = base + warp * 32 + lane;
+
+    const int chunk = kTrainWarps * kTrainRows;
+    for (int base = blockIdx.x * chunk; base < n; base += gridDim.x * chunk) {
+        const int s = lane & 15;
+        const int j = base + warp * kTrainRows + s;
         const bool valid = j < n;
-        float in[kGuideIn];
         float3 wi = f3(0.f, 0.f, 1.f);
         float w = 0.f;
-        if (valid) {
-            float4 b0 = batch[4 * j], b1 = batch[4 * j + 1], b2 = batch[4 * j + 2], b3 = batch[4 * j + 3];
-            guide_encode(net, f3(b0), f3(b1), f3(b2), in);
-            wi = f3(b3);
-            w = fminf(b0.w / fmaxf(mean_w, 1e-12f), 100.f);  // normalised, firefly-clamped weight
-        } else {
+        if (lane < 16) {
+            float in[kGuideIn];
+            if (valid) {
+                const float4 b0 = batch[4 * j], b1 = batch[4 * j + 1], b2 = batch[4 * j + 2], b3 = batch[4 * j + 3];
+                guide_encode(net, f3(b0), f3(b1), f3(b2), in);
+                wi = f3(b3);
+                w = fminf(b0.w / fmaxf(mean_w, 1e-12f), 100.f);  // normalised, firefly-clamped weight
+            } else {
 #pragma unroll
-            for (int k = 0; k < kGuideIn; k++) in[k] = 0.f;
+                for (int k = 0; k < kGuideIn; k++) in[k] = 0.f;
+            }
+            store_inputs(T + kTA0 + s * kLdA0, in);
         }
-#pragma unroll
-        for (int k = 0; k < kGuideIn; k += 2) *reinterpret_cast<uint32_t*>(a0 + lane * kLdA0 + k) = pack_bf16(in[k], in[k + 1]);
         __syncwarp();
-        for (int m = 0; m < 2; m++) tile_layer<80, 64>(a0 + m * 16 * kLdA0, kLdA0, wt[0], net.params + guide_b_off(0), h1 + m * 16 * kLdH, kLdH, true, nullptr, 0);
+        mma_rows<1, 80, 64>(T + kTA0, kLdA0, wts + fw_off(0), fw_ld(0), net.params + guide_b_off(0), T + kTH1, kLdH, true, nullptr, 0, nullptr, 0);
         __syncwarp();
-        for (int m = 0; m < 2; m++) tile_layer<64, 64>(h1 + m * 16 * kLdH, kLdH, wt[1], net.params + guide_b_off(1), h2 + m * 16 * kLdH, kLdH, true, nullptr, 0);
+        mma_rows<1, 64, 64>(T + kTH1, kLdH, wts + fw_off(1), fw_ld(1), net.params + guide_b_off(1), T + kTH2, kLdH, true, nullptr, 0, nullptr, 0);
         __syncwarp();
-        for (int m = 0; m < 2; m++) tile_layer<64, 64>(h2 + m * 16 * kLdH, kLdH, wt[2], net.params + guide_b_off(2), h3 + m * 16 * kLdH, kLdH, true, nullptr, 0);
+        mma_rows<1, 64, 64>(T + kTH2, kLdH, wts + fw_off(2), fw_ld(2), net.params + guide_b_off(2), T + kTH3, kLdH, true, nullptr, 0, nullptr, 0);
         __syncwarp();
-        for (int m = 0; m < 2; m++) tile_layer<64, 48>(h3 + m * 16 * kLdH, kLdH, wt[3], net.params + guide_b_off(3), nullptr, 0, false, of + m * 16 * kLdG, kLdG);
+        mma_rows<1, 64, 48>(T + kTH3, kLdH, wts + fw_off(3), fw_ld(3), net.params + guide_b_off(3), nullptr, 0, false, OF, kLdOF, nullptr, 0);
         __syncwarp();
-        // loss gradient at the 40 outputs (per lane, FP32)
+        // loss gradient at the outputs: one lane per sample
         float g[kGuideOutPad];
 #pragma unroll
         for (int k = 0; k < kGuideOutPad; k++) g[k] = 0.f;
-        if (valid && w > 0.f) {
+        if (lane < 16 && valid && w > 0.f) {
             float o[kGuideOut];
 #pragma unroll
-            for (int k = 0; k < kGuideOut; k++) o[k] = of[lane * kLdG + k];
-            Lobe L[kGuideLobes];
-            guide_lobes(o, L);
-            float p[kGuideLobes], q = 0.f;
-#pragma unroll
-            for (int k = 0; k < kGuideLobes; k++) { p[k] = L[k].w * vmf_pdf(L[k], wi); q += p[k]; }
-            q = fmaxf(q, 1e-20f);
-            loss += w * -__logf(q);
+            for (int k = 0; k < kGuideOut; k++) o[k] = OF[s * kLdOF + k];
+            loss += w * nll_output_grad(o, wi, w, g);
             wsum += w;
+        }
+        __syncwarp();  // OF (aliasing d1/d2) fully read before the deltas are written
+        if (lane < 16) {
 #pragma unroll
-            for (int k = 0; k < kGuideLobes; k++) {
-                float r = p[k] / q;
-                float kap = L[k].kappa;
-                float c = dot(L[k].mu, wi);
-                // d log vMF / d kappa = 1/kappa - 2 e^-2k / (1 - e^-2k) + (mu.wi - 1)
-                float e2 = __expf(-2.f * kap);
-                float dk = 1.f / kap - 2.f * e2 / fmaxf(-expm1f(-2.f * kap), 1e-20f) + (c - 1.f);
-                float kraw = o[5 * k + 3];
-                float sig = 1.f / (1.f + __expf(-kraw));
-                if (kap >= 2000.f) sig = 0.f;
-                float3 m = f3(o[5 * k], o[5 * k + 1], o[5 * k + 2]);
-                float len = fmaxf(sqrtf(dot(m, m)), 1e-12f);
-                float3 dm = (wi - L[k].mu * c) * (kap / len);
-                g[5 * k + 0] = -w * r * dm.x;
-                g[5 * k + 1] = -w * r * dm.y;
-                g[5 * k + 2] = -w * r * dm.z;
-                g[5 * k + 3] = -w * r * dk * sig;
-                g[5 * k + 4] = -w * (r - L[k].w);
-            }
-#pragma unroll
-            for (int k = 0; k < kGuideOut; k++) {
-                float v = g[k];
-                g[k] = isfinite(v) ? fminf(fmaxf(v, -1e3f), 1e3f) : 0.f;
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < kGuideOutPad; k += 2) *reinterpret_cast<uint32_t*>(dout + lane * kLdO + k) = pack_bf16(g[k], g[k + 1]);
-        __syncwarp();
-        // backward through the hidden layers: d_in = (d_out @ W^T) masked by relu'(h_in)
-        for (int m = 0; m < 2; m++) tile_layer<48, 64>(dout + m * 16 * kLdO, kLdO, wn[3], nullptr, nullptr, 0, false, of + m * 16 * kLdG, kLdG);
-        __syncwarp();
-        for (int c = 0; c < 64; c += 2) {
-            float v0 = bf(h3 + lane * kLdH + c) > 0.f ? of[lane * kLdG + c] : 0.f;
-            float v1 = bf(h3 + lane * kLdH + c + 1) > 0.f ? of[lane * kLdG + c + 1] : 0.f;
-            *reinterpret_cast<uint32_t*>(d3 + lane * kLdH + c) = pack_bf16(v0, v1);
+            for (int k = 0; k < kGuideOutPad; k += 2) *reinterpret_cast<uint32_t*>(T + kTDO + s * kLdO + k) = pack_bf16(g[k], g[k + 1]);
         }
         __syncwarp();
-        for (int m = 0; m < 2; m++) tile_layer<64, 64>(d3 + m * 16 * kLdH, kLdH, wn[2], nullptr, nullptr, 0, false, of + m * 16 * kLdG, kLdG);
+        // backward: d_l = (d_{l+1} @ W_{l+1}^T) masked by relu'(h)
+        mma_rows<1, 48, 64>(T + kTDO, kLdO, wns + bw_off(3), bw_ld(3), nullptr, T + kTD3, kLdH, false, nullptr, 0, T + kTH3, kLdH);
         __syncwarp();
-        for (int c = 0; c < 64; c += 2) {
-            float v0 = bf(h2 + lane * kLdH + c) > 0.f ? of[lane * kLdG + c] : 0.f;
-            float v1 = bf(h2 + lane * kLdH + c + 1) > 0.f ? of[lane * kLdG + c + 1] : 0.f;
-            *reinterpret_cast<uint32_t*>(d2 + lane * kLdH + c) = pack_bf16(v0, v1);
-        }
+        mma_rows<1, 64, 64>(T + kTD3, kLdH, wns + bw_off(2), bw_ld(2), nullptr, T + kTD2, kLdH, false, nullptr, 0, T + kTH2, kLdH);
         __syncwarp();
-        for (int m = 0; m < 2; m++) tile_layer<64, 64>(d2 + m * 16 * kLdH, kLdH, wn[1], nullptr, nullptr, 0, false, of + m * 16 * kLdG, kLdG);
-        __syncwarp();
-        for (int c = 0; c < 64; c += 2) {
-            float v0 = bf(h1 + lane * kLdH + c) > 0.f ? of[lane * kLdG + c] : 0.f;
-            float v1 = bf(h1 + lane * kLdH + c + 1) > 0.f ? of[lane * kLdG + c + 1] : 0.f;
-            *reinterpret_cast<uint32_t*>(d1 + lane * kLdH + c) = pack_bf16(v0, v1);
-        }
+        mma_rows<1, 64, 64>(T + kTD2, kLdH, wns + bw_off(1), bw_ld(1), nullptr, T + kTD1, kLdH, false, nullptr, 0, T + kTH1, kLdH);
         __syncthreads();
-        // weight and bias gradients of this block's 64 samples: dW_l = a_in^T d_out (FP32 sums)
-        for (int pidx = threadIdx.x; pidx < kGuideParams; pidx += blockDim.x) {
-            int l = 3;
-            while (l > 0 && pidx < guide_w_off(l)) l--;
-            int K = guide_k(l), N = guide_n(l);
-            int rel = pidx - guide_w_off(l);
-            bool is_bias = rel >= K * N;
-            int kk = is_bias ? 0 : rel / N, nn = is_bias ? rel - K * N : rel % N;
-            float acc = 0.f;
-            for (int wv = 0; wv < kTrainWarps; wv++) {
-                unsigned char* wbw = smem + kGuideParams * 4 + wv * kWarpTrainBytes;
-                const __nv_bfloat16* A0 = reinterpret_cast<const __nv_bfloat16*>(wbw);
-                const __nv_bfloat16* H1 = A0 + 32 * kLdA0;
-                const __nv_bfloat16* H2 = H1 + 32 * kLdH;
-                const __nv_bfloat16* H3 = H2 + 32 * kLdH;
-                const __nv_bfloat16* D1 = H3 + 32 * kLdH;
-                const __nv_bfloat16* D2 = D1 + 32 * kLdH;
-                const __nv_bfloat16* D3 = D2 + 32 * kLdH;
-                const float* OF = reinterpret_cast<const float*>(D3 + 32 * kLdH);
-                const __nv_bfloat16* DO = reinterpret_cast<const __nv_bfloat16*>(OF + 32 * kLdG);
-                const __nv_bfloat16* ain = l == 0 ? A0 : (l == 1 ? H1 : (l == 2 ? H2 : H3));
-                const int lda = l == 0 ? kLdA0 : kLdH;
-                const __nv_bfloat16* dlt = l == 0 ? D1 : (l == 1 ? D2 : (l == 2 ? D3 : DO));
-                const int ldd = l == 3 ? kLdO : kLdH;
-                for (int r = 0; r < 32; r++) {
-                    float dv = __bfloat162float(dlt[r * ldd + nn]);
-                    acc += is_bias ? dv : __bfloat162float(ain[r * lda + kk]) * dv;
+        // weight gradients over the block's 128 samples
+        {
+            const int jm = lane >> 3, qr = lane & 7;
+#pragma unroll
+            for (int q = 0; q < kDwPerWarp; q++) {
+                const int idx = warp + kTrainWarps * q;
+                if (idx < kDwTiles) {
+                    int l, mt, nt;
+                    dw_tile(idx, l, mt, nt);
+                    const int ain = l == 0 ? kTA0 : (l == 1 ? kTH1 : (l == 2 ? kTH2 : kTH3));
+                    const int lda = l == 0 ? kLdA0 : kLdH;
+                    const int dlt = l == 0 ? kTD1 : (l == 1 ? kTD2 : (l == 2 ? kTD3 : kTDO));
+                    const int ldd = l == 3 ? kLdO : kLdH;
+                    const int arow = qr + (jm >> 1) * 8, acol = mt * 16 + (jm & 1) * 8;
+                    const int brow = qr + (jm & 1) * 8, bcol = nt * 8;
+#pragma unroll
+                    for (int wv = 0; wv < kTrainWarps; wv++) {
+                        const __nv_bfloat16* Tw = tiles + wv * kTWarpElems;
+                        uint32_t a[4], b[2];
+                        ldsm_x4_trans(a, Tw + ain + arow * lda + acol);
+                        ldsm_x2_trans(b, Tw + dlt + brow * ldd + bcol);
+                        mma16816(acc[q], a, b);
+                    }
                 }
             }
-            gacc[pidx] += acc;
+        }
+        if (bl >= 0) {
+            const int dlt = bl == 0 ? kTD1 : (bl == 1 ? kTD2 : (bl == 2 ? kTD3 : kTDO));
+            const int ldd = bl == 3 ? kLdO : kLdH;
+            for (int wv = 0; wv < kTrainWarps; wv++) {
+                const __nv_bfloat16* D = tiles + wv * kTWarpElems + dlt;
+#pragma unroll
+                for (int r = 0; r < kTrainRows; r++) bacc += __bfloat162float(D[r * ldd + bc]);
+            }
         }
         __syncthreads();
     }
-    for (int i = threadIdx.x; i < kGuideParams; i += blockDim.x) {
-        float v = gacc[i];
-        if (v != 0.f) atomicAdd(grad + i, v);
+    // flush: dW_l[k][n] with k = mt*16 + g (+8), n = nt*8 + 2t (+1)
+    {
+        const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+        for (int q = 0; q < kDwPerWarp; q++) {
+            const int idx = warp + kTrainWarps * q;
+            if (idx < kDwTiles) {
+                int l, mt, nt;
+                dw_tile(idx, l, mt, nt);
+                const int N = guide_n(l);
+                float* G = grad + guide_w_off(l);
+                const int k0 = mt * 16 + g, c = nt * 8 + 2 * t;
+                if (acc[q][0] != 0.f) atomicAdd(G + k0 * N + c, acc[q][0]);
+                if (acc[q][1] != 0.f) atomicAdd(G + k0 * N + c + 1, acc[q][1]);
+                if (acc[q][2] != 0.f) atomicAdd(G + (k0 + 8) * N + c, acc[q][2]);
+                if (acc[q][3] != 0.f) atomicAdd(G + (k0 + 8) * N + c + 1, acc[q][3]);
+            }
+        }
     }
-    // loss bookkeeping
+    if (bl >= 0 && bacc != 0.f) atomicAdd(grad + guide_b_off(bl) + bc, bacc);
     for (int o = 16; o > 0; o >>= 1) {
         loss += __shfl_down_sync(0xffffffffu, loss, o);
         wsum += __shfl_down_sync(0xffffffffu, wsum, o);
     }
-    if (lane == 0) {
+    if (lane == 0 && wsum != 0.f) {
         atomicAdd(stats + 0, loss);
         atomicAdd(stats + 1, wsum);
     }
@@ -421,9 +565,6 @@ __global__ void k_guide_bf16_from_params(const float* params, __nv_bfloat16* bfw
         bfw[guide_bf_off(l) + K * N + kk * N + nn] = h;
     }
 }
-
-constexpr size_t kInferSmem = 2 * 16384 + kInferWarps * 2 * kTileBytes;
-constexpr size_t kTrainSmem = kGuideParams * 4 + kTrainWarps * kWarpTrainBytes;
 
 }  // namespace
 
@@ -537,7 +678,7 @@ void GuideTrainer::train(cudaStream_t st, const float4* out_L, int wave_paths, i
     }
     GuideNet net = view(false, false).net;
     for (int s = 0; s < steps; s++) {
-        k_guide_train<<<grid, 64, kTrainSmem, st>>>(net, batch_, batch_count_, (int)rec_cap_, grad_, loss_acc_);
+        k_guide_train<<<grid, 256, kTrainSmem, st>>>(net, batch_, batch_count_, (int)rec_cap_, grad_, loss_acc_);
         steps_++;
         const float b1 = 0.9f, b2 = 0.99f;
         float c1 = 1.f - std::pow(b1, (float)steps_), c2 = 1.f - std::pow(b2, (float)steps_);
@@ -620,7 +761,7 @@ int GuideTrainer::gradient(DeviceArena& arena, const float* host_samples, int n,
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    k_guide_train<<<sms, 64, kTrainSmem>>>(view(false, false).net, db, batch_count_, n, grad_, loss_acc_);
+    k_guide_train<<<sms, 256, kTrainSmem>>>(view(false, false).net, db, batch_count_, n, grad_, loss_acc_);
     int rc = C2G_OK;
     if (cudaDeviceSynchronize() != cudaSuccess) { err = cudaGetErrorString(cudaGetLastError()); rc = C2G_ERR_CUDA; }
     else {

@@ -9,7 +9,7 @@
 // so the guided estimator can use exactly evaluated pdfs.
 //
 // Matrix products use the warp-level tensor-core instruction mma.sync.m16n8k16 (BF16 inputs, FP32
-// accumulators) on 16-row tiles held in shared memory.  Weight layout per layer l (K_l inputs,
+// accumulators) on 16-row tiles held in shared memory (guide.cu).  Weight layout per layer l (K_l inputs,
 // N_l outputs): `wt` = N_l x K_l row-major BF16 (the B operand of x @ W), `wn` = K_l x N_l row-major
 // BF16 (the B operand of delta @ W^T), bias FP32.
 #pragma once
@@ -26,14 +26,18 @@ __device__ __forceinline__ void guide_encode(const GuideNet& g, float3 x, float3
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         float v = fminf(fmaxf(p[a], 0.f), 1.f);
+        // sin/cos(pi v) with exact argument reduction, then the double-angle recurrence
+        // sin 2u = 2 sin u cos u, cos 2u = (cos u - sin u)(cos u + sin u) for the higher frequencies
+        // (the absolute error grows about 2x per octave: ~1e-4 at 2^11, far below BF16 resolution)
+        float s, c;
+        sincospif(v, &s, &c);
 #pragma unroll
         for (int f = 0; f < kGuideFreqs; f++) {
-            // sin/cos(pi * v * 2^f): the power-of-two scaling is exact and sincospif reduces the
-            // argument exactly, so high frequencies keep full accuracy
-            float s, c;
-            sincospif(v * (float)(1 << f), &s, &c);
             in[a * 2 * kGuideFreqs + 2 * f] = s;
             in[a * 2 * kGuideFreqs + 2 * f + 1] = c;
+            const float s2 = 2.f * s * c, c2 = (c - s) * (c + s);
+            s = s2;
+            c = c2;
         }
     }
     in[72] = n.x; in[73] = n.y; in[74] = n.z;
@@ -52,45 +56,6 @@ __device__ __forceinline__ void mma16816(float* d, const uint32_t* a, const uint
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
-}
-
-// One layer on a 16-row tile: out[16 x N] = act(in[16 x K] @ W + b).  `in` and `out` are BF16
-// row-major tiles in shared memory with leading dimensions ldi / ldo (in elements); `wt` is the
-// N x K BF16 transpose of W (global or shared), `bias` FP32.  relu: apply max(0, .).  When
-// out_f32 is non-null the FP32 pre-activation values are written there instead (ld = ldf).
-template <int K, int N>
-__device__ __forceinline__ void tile_layer(const __nv_bfloat16* in, int ldi, const __nv_bfloat16* wt, const float* bias,
-                                           __nv_bfloat16* out, int ldo, bool relu, float* out_f32, int ldf) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int n0 = 0; n0 < N; n0 += 8) {
-        float d[4];
-        float b0 = bias ? bias[n0 + 2 * t] : 0.f, b1 = bias ? bias[n0 + 2 * t + 1] : 0.f;
-        d[0] = b0; d[1] = b1; d[2] = b0; d[3] = b1;
-#pragma unroll
-        for (int k0 = 0; k0 < K; k0 += 16) {
-            uint32_t a[4], b[2];
-            a[0] = *reinterpret_cast<const uint32_t*>(in + (g) * ldi + k0 + 2 * t);
-            a[1] = *reinterpret_cast<const uint32_t*>(in + (g + 8) * ldi + k0 + 2 * t);
-            a[2] = *reinterpret_cast<const uint32_t*>(in + (g) * ldi + k0 + 2 * t + 8);
-            a[3] = *reinterpret_cast<const uint32_t*>(in + (g + 8) * ldi + k0 + 2 * t + 8);
-            b[0] = *reinterpret_cast<const uint32_t*>(wt + (n0 + g) * K + k0 + 2 * t);
-            b[1] = *reinterpret_cast<const uint32_t*>(wt + (n0 + g) * K + k0 + 2 * t + 8);
-            mma16816(d, a, b);
-        }
-        if (out_f32) {
-            out_f32[(g) * ldf + n0 + 2 * t] = d[0];
-            out_f32[(g) * ldf + n0 + 2 * t + 1] = d[1];
-            out_f32[(g + 8) * ldf + n0 + 2 * t] = d[2];
-            out_f32[(g + 8) * ldf + n0 + 2 * t + 1] = d[3];
-        } else {
-            if (relu) {
-                d[0] = fmaxf(d[0], 0.f); d[1] = fmaxf(d[1], 0.f); d[2] = fmaxf(d[2], 0.f); d[3] = fmaxf(d[3], 0.f);
-            }
-            *reinterpret_cast<uint32_t*>(out + (g) * ldo + n0 + 2 * t) = pack_bf16(d[0], d[1]);
-            *reinterpret_cast<uint32_t*>(out + (g + 8) * ldo + n0 + 2 * t) = pack_bf16(d[2], d[3]);
-        }
-    }
 }
 
 // ---- the directional mixture -----------------------------------------------------------------

@@ -140,8 +140,11 @@ __device__ __forceinline__ void slot_pixel(const WaveArgs& a, int slot, int& x, 
     y = (tile / a.tiles_x) * 8 + (w >> 3);
 }
 
-__device__ __forceinline__ int pack_state(int dim, int bounce, int light_path) {
-    return (dim & 0xffff) | ((bounce & 0xff) << 16) | (light_path << 24);
+// Path state word: Halton dimension (16 bits), bounce (8), light_path (1), mis_emit (1).
+// mis_emit: the ray was drawn by the guided integrator's mixture; an emitter it reaches adds its
+// radiance with the MIS weight against light sampling, the mixture pdf riding in L.w.
+__device__ __forceinline__ int pack_state(int dim, int bounce, int light_path, int mis_emit = 0) {
+    return (dim & 0xffff) | ((bounce & 0xff) << 16) | (light_path << 24) | (mis_emit << 25);
 }
 
 struct PathRefs {
@@ -264,6 +267,8 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
         int dim = packed & 0xffff;
         int bounce = (packed >> 16) & 0xff;
         int light_path = (packed >> 24) & 1;
+        const bool mis_emit = (packed >> 25) & 1;
+        const float prev_pdf = L4.w;
         const int vidx = __float_as_int(b4.w);
         int s_local = valid ? pid / a.nslots : 0;
         int px = 0, py = 0;
@@ -275,8 +280,12 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
         Hit h{h4.x, h4.y, h4.z, __float_as_int(h4.w)};
 
         bool alive = valid && MT != kBucketMiss;  // miss: the path ends (no skybox)
+        // a guided path's ray past the depth limit only collects the emission it reaches
+        const bool emit_only = mis_emit && bounce >= a.max_depth;
         bool do_nee = false;
         bool cont = false;
+        int next_mis = 0;       // guided continuation: MIS-weighted emission at the next hit
+        float next_pdf = 0.f;   // its mixture pdf
         float3 next_o = ro, next_d = rd;
         Surface s;
         BxDF bx;
@@ -290,8 +299,26 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                 const Light& Lg = S.lights[s.light];
                 float3 n_actual = s.front ? s.N : -s.N;
                 L = L + beta * area_Le(Lg, n_actual, -rd);
+            } else if (mis_emit && s.light >= 0) {
+                // mixture-sampled ray reaching an emitter: power heuristic against that light's
+                // sampling pdf (solid angle at the previous vertex); lights NEE skips weigh 1
+                const Light& Lg = S.lights[s.light];
+                float3 n_actual = s.front ? s.N : -s.N;
+                float3 Le = area_Le(Lg, n_actual, -rd);
+                if (!is_zero(Le)) {
+                    float wgt = 1.f;
+                    if (Lg.flux_zero == 0.f) {
+                        float3 dv = s.pos - ro;
+                        float cl = fabsf(dot(normalize(rd), n_actual));
+                        float pdf_light = cl > 0.f ? dot(dv, dv) / (cl * Lg.area) : 0.f;
+                        wgt = pdf_light > 0.f ? power_heuristic(prev_pdf, pdf_light) : 1.f;
+                    }
+                    L = L + beta * (Le * wgt);
+                }
             }
-            if (MT == kBucketNone) {
+            if (emit_only) {
+                // nothing more on this path
+            } else if (MT == kBucketNone) {
                 // no BSDF: continue straight through (PathTracingIntegrator.cpp:64-68); the direct
                 // lighting integrator stops at an emitter instead (DirectLightingIntegrator.cpp:48-55)
                 if (!(direct && s.light >= 0)) {
@@ -315,6 +342,24 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
         // Specular BxDFs give f = 0 and match no non-specular sample, so they skip the light loop.
         float2 uL = make_float2(0, 0), uB = make_float2(0, 0);
         const int nsflags = BXDF_ALL & ~BXDF_SPECULAR;
+        // Guided vertex: the continuation is drawn from alpha * BSDF + (1 - alpha) * learned mixture
+        // and doubles as the BSDF technique of direct lighting (no separate MIS ray); light samples
+        // are weighted against the mixture pdf.  Before the network is trained alpha = 1.
+        const bool gvert = G && do_nee && !direct && (bx.flags & BXDF_SPECULAR) == 0;
+        Lobe lobes[kGuideLobes];
+        float alpha = 1.f, detM = 1.f;
+        if (gvert && gv.sample) {
+            float o40[kGuideOut];
+            const float* src = gv.out + (size_t)i * kGuideOut;
+            bool finite = true;
+#pragma unroll
+            for (int k = 0; k < kGuideOut; k++) { o40[k] = src[k]; finite = finite && isfinite(o40[k]); }
+            guide_lobes(o40, lobes);
+            // a non-finite network output or a degenerate shading frame leaves this vertex to
+            // plain BSDF sampling
+            detM = fabsf(dot(fr.T, cross(fr.N, fr.B)));
+            alpha = (finite && detM > 1e-6f) ? gv.net.alpha : 1.f;
+        }
         bool nee_work = false, mis_ok = false, any_mis = false;
         float3 f2 = f3(0.f, 0.f, 0.f), wi2 = f3(0.f, 0.f, 0.f);
         float pdf_b2 = 0.f;
@@ -329,7 +374,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
             }
             dim += n_area;  // one (unused) 1D sample per eligible non-delta light
             nee_work = (bx.flags & BXDF_SPECULAR) == 0;
-            if (nee_work && n_area > 0) {
+            if (nee_work && n_area > 0 && !gvert) {
                 int stype = 0;
                 f2 = bsdf_sample(bx, fr, 0.f, uB, wo, wi2, pdf_b2, nsflags, stype, mis_ok);
                 if (mis_ok) f2 = f2 * fmaxf(0.f, dot(s.N, wi2));
@@ -352,6 +397,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                     if (pdf_l != 0.f && !is_zero(Li)) {
                         float pdf_b;
                         float3 f = bsdf_f_pdf(bx, fr, wo, wi, nsflags, pdf_b) * fmaxf(0.f, dot(s.N, wi));
+                        if (gvert && alpha < 1.f) pdf_b = alpha * pdf_b + (1.f - alpha) * guide_pdf(lobes, wi);
                         if (!is_zero(f)) {
                             bool back = dot(lpos - s.pos, s.N) < 0;
                             float3 org = s.pos + (back ? -s.N : s.N) * kSpawnEps;
@@ -409,33 +455,35 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
             int stype = 0;
             bool ok;
             float3 f = bsdf_sample(bx, fr, u1, u2, wo, wi, pdf, BXDF_ALL, stype, ok);
-            if (G && gv.sample && valid && (bx.flags & BXDF_SPECULAR) == 0) {
-                // Guided continuation: one-sample MIS over {BSDF, learned mixture} with the mixture
-                // pdf alpha * p_bsdf + (1 - alpha) * p_guide (exactly evaluated), so the estimator
-                // stays unbiased; the extra random numbers come from dims far above the plain path's.
-                Lobe lobes[kGuideLobes];
-                float o40[kGuideOut];
-                const float* src = gv.out + (size_t)i * kGuideOut;
-                bool finite = true;
-#pragma unroll
-                for (int k = 0; k < kGuideOut; k++) { o40[k] = src[k]; finite = finite && isfinite(o40[k]); }
-                guide_lobes(o40, lobes);
-                // a non-finite network output leaves this vertex to plain BSDF sampling (alpha = 1)
-                const float alpha = finite ? gv.net.alpha : 1.f;
+            if (gvert && alpha < 1.f) {
+                // One-sample MIS over {BSDF, learned mixture}: q = alpha p_bsdf + (1 - alpha) p_guide,
+                // both exactly evaluated, so the estimator stays unbiased.  The BSDF technique draws
+                // a local direction l and traces M l (M = [dpdu N dpdv], not orthonormal under
+                // interpolated normals), so q is kept in that local measure: the guide's world pdf
+                // times the Jacobian of l -> M l / |M l|, |det M| / |M l|^3.  The extra random
+                // numbers come from hashed dimensions far above the plain path's.
+                const float3 c0 = cross(fr.N, fr.B), c1 = cross(fr.B, fr.T), c2 = cross(fr.T, fr.N);
+                const float3 wol = to_local(fr, wo);
                 float us = hash_uniform(pixel, sample, 0x4000u + 4u * bounce, S.seed);
                 if (us >= alpha) {
                     float3 wg = guide_sample(lobes, hash_uniform(pixel, sample, 0x4001u + 4u * bounce, S.seed),
                                              hash_uniform(pixel, sample, 0x4002u + 4u * bounce, S.seed),
                                              hash_uniform(pixel, sample, 0x4003u + 4u * bounce, S.seed));
-                    wi = clamp1(wg);
-                    float pb;
-                    f = bsdf_f_pdf(bx, fr, wo, wi, BXDF_ALL, pb);
-                    bool refl = dot(wi, s.N) * dot(wo, s.N) > 0;
-                    stype = (bx.flags & ~(BXDF_REFLECTION | BXDF_TRANSMISSION)) | (refl ? BXDF_REFLECTION : BXDF_TRANSMISSION);
-                    pdf = alpha * pb + (1.f - alpha) * guide_pdf(lobes, wg);
+                    // l = M^-1 wg (rows of the inverse: the cross products over det M; the frame
+                    // [dpdu N N x dpdu] is left-handed, det M < 0), normalised
+                    const float sgn = dot(fr.T, c0) < 0.f ? -1.f : 1.f;
+                    float3 l = normalize(f3(dot(c0, wg), dot(c1, wg), dot(c2, wg)) * sgn);
+                    float pb = 0.f;
+                    f = f3(0.f, 0.f, 0.f);
+                    if (l.y * wol.y > 0.f) f = bxdf_f_pdf(bx, wol, l, pb);  // reflection-only BxDFs
+                    wi = to_world(fr, l);
+                    const float lm = length(wi);
+                    stype = (bx.flags & ~(BXDF_REFLECTION | BXDF_TRANSMISSION)) | BXDF_REFLECTION;
+                    pdf = alpha * pb + (1.f - alpha) * guide_pdf(lobes, wg) * detM / (lm * lm * lm);
                     ok = !is_zero(f) && pdf > 0.f;
-                } else if (ok && alpha < 1.f) {
-                    pdf = alpha * pdf + (1.f - alpha) * guide_pdf(lobes, normalize(wi));
+                } else if (ok) {
+                    const float lm = length(wi);
+                    pdf = alpha * pdf + (1.f - alpha) * guide_pdf(lobes, wi * (1.f / lm)) * detM / (lm * lm * lm);
                 }
             }
             if (ok && fabsf(pdf) != 0.f) {
@@ -444,12 +492,14 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                 light_path = (specular || (stype & BXDF_TRANSMISSION)) ? 1 : 0;
                 next_o = spawn_origin(s, wi);
                 next_d = wi;
+                if (gvert) { next_mis = 1; next_pdf = pdf; }
                 if (G && gv.record && !specular && (pid % gv.rec_stride) == 0 && bounce < gv.rec_depth) {
                     // training record: vertex, throughput and radiance so far (direct light added later)
                     float4* r = gv.rec + 4 * ((size_t)(pid / gv.rec_stride) * gv.rec_depth + bounce);
                     r[1] = make_float4(s.N.x, s.N.y, s.N.z, 0.2126f * L.x + 0.7152f * L.y + 0.0722f * L.z);
                     r[2] = make_float4(wo.x, wo.y, wo.z, 0.2126f * beta.x + 0.7152f * beta.y + 0.0722f * beta.z);
-                    r[3] = make_float4(wi.x, wi.y, wi.z, 0.f);
+                    const float3 wn = normalize(wi);
+                    r[3] = make_float4(wn.x, wn.y, wn.z, 0.f);
                     r[0] = make_float4(s.pos.x, s.pos.y, s.pos.z, 1.f);
                 }
                 beta = beta * (f * cosine / pdf);
@@ -464,16 +514,18 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
             }
         }
         // Depth limit.  Direct lighting only re-enters at the same level through pass-through
-        // surfaces (DirectLightingIntegrator.cpp:54); the 8-bit hop counter bounds that walk.
-        if (cont && (direct ? bounce + 1 >= 255 : bounce + 1 >= a.max_depth)) cont = false;
+        // surfaces (DirectLightingIntegrator.cpp:54); the 8-bit hop counter bounds that walk.  A
+        // guided vertex's ray is traced one level past the limit for the emission it reaches (its
+        // light-sampling partner was counted at this vertex).
+        if (cont && (direct ? bounce + 1 >= 255 : bounce + 1 >= a.max_depth + next_mis)) cont = false;
         // ---- enqueue the continuation; finished paths keep L in place for `accumulate`
         int j = warp_append(out.nxt_count, cont);
         if (valid) {
             if (cont) {
                 out.nxt.o[j] = make_float4(next_o.x, next_o.y, next_o.z, __int_as_float(pid));
-                out.nxt.d[j] = make_float4(next_d.x, next_d.y, next_d.z, __int_as_float(pack_state(dim, bounce + 1, light_path)));
+                out.nxt.d[j] = make_float4(next_d.x, next_d.y, next_d.z, __int_as_float(pack_state(dim, bounce + 1, light_path, next_mis)));
                 out.nxt.beta[j] = make_float4(beta.x, beta.y, beta.z, __int_as_float(vidx));
-                out.nxt.L[j] = make_float4(L.x, L.y, L.z, 0.f);
+                out.nxt.L[j] = make_float4(L.x, L.y, L.z, next_pdf);
             } else {
                 cur.L[i] = make_float4(L.x, L.y, L.z, 0.f);
             }
@@ -560,7 +612,7 @@ __global__ void k_accumulate(WaveArgs a, PathRefs cur, PathRefs nxt, const int2*
         if (ac.x >= 0) {
             if (ac.y) {
                 float4 L = nxt.L[ac.x];
-                nxt.L[ac.x] = make_float4(L.x + direct.x, L.y + direct.y, L.z + direct.z, 0.f);
+                nxt.L[ac.x] = make_float4(L.x + direct.x, L.y + direct.y, L.z + direct.z, L.w);  // w: mixture pdf
             }
         } else {
             float4 L = cur.L[i];
@@ -749,10 +801,10 @@ int GpuScene::upload(const HostScene& s, int tree, const RefTree* ref, const Sah
     sb_->owned.push_back(sb_->err);
     C2G_CUDA(cudaMemset(sb_->err, 0, sizeof(int) * 4));
     S.err = sb_->err;
-    sb_->counts = (unsigned long long*)arena.alloc(sizeof(unsigned long long) * 24, err);
+    sb_->counts = (unsigned long long*)arena.alloc(sizeof(unsigned long long) * 3 * C2G_K_KINDS, err);
     if (!sb_->counts) return C2G_ERR_OOM;
     sb_->owned.push_back(sb_->counts);
-    C2G_CUDA(cudaMemset(sb_->counts, 0, sizeof(unsigned long long) * 24));
+    C2G_CUDA(cudaMemset(sb_->counts, 0, sizeof(unsigned long long) * 3 * C2G_K_KINDS));
     // film
     film_w_ = s.cfg.width;
     film_h_ = s.cfg.height;
@@ -879,7 +931,7 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
     const bool count = (counting_ & C2G_COUNT_TRAVERSAL) != 0;
     const bool timing = (counting_ & C2G_COUNT_TIMING) != 0;
     unsigned long long* cnt = sb_->counts;
-    if (count) C2G_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 24, st));
+    if (count) C2G_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 3 * C2G_K_KINDS, st));
 
     static int g_raygen = 0, g_ext = 0, g_ext_c = 0, g_shade = 0, g_sh = 0, g_sh_c = 0, g_mis = 0, g_mis_c = 0, g_acc = 0, g_film = 0;
     if (!g_raygen) {
@@ -898,7 +950,7 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
     struct Ev { cudaEvent_t a, b; int kind; };
     static std::vector<Ev> pool;
     size_t used = 0;
-    int kcount[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int kcount[C2G_K_KINDS] = {};
     auto begin = [&](int kind) {
         kcount[kind]++;
         if (!timing) return;
@@ -920,6 +972,9 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         int rc = guide_.init(arena, w.P, p.max_depth, box_lo_, box_hi_, p.seed, err);
         if (rc) return rc;
     }
+    // Bounce levels per wave.  A guided vertex's ray is traced one level past the depth for the
+    // emission it reaches; direct lighting walks pass-through surfaces up to 255 hops.
+    const int levels = p.integrator == C2G_INTEGRATOR_DIRECT ? 255 : p.max_depth + (guided ? 1 : 0);
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
@@ -937,8 +992,15 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         k_raygen<<<g_raygen, 256, 0, st>>>(S, a, buf[0], w.out_L, C + 0);
         end();
         int cur = 0;
-        for (int b = 0; b < p.max_depth; b++) {
+        for (int b = 0; b < levels; b++) {
             int nxt = cur ^ 1;
+            if (b >= p.max_depth && p.integrator == C2G_INTEGRATOR_DIRECT) {
+                // pass-through hops past the depth: stop once the queue is empty
+                int qn = 0;
+                C2G_CUDA(cudaMemcpyAsync(&qn, C + cur, sizeof(int), cudaMemcpyDeviceToHost, st));
+                C2G_CUDA(cudaStreamSynchronize(st));
+                if (qn == 0) break;
+            }
             begin(C2G_K_EXTEND);
             cudaMemsetAsync(C + kCntBucket, 0, sizeof(int) * kBuckets, st);
             if (count)
@@ -983,7 +1045,7 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         waves++;
         if (guided) {
             // online training on this wave's recorded vertices (batch build, fused fwd/bwd, Adam)
-            begin(C2G_K_GUIDE);
+            begin(C2G_K_TRAIN);
             guide_.train(st, w.out_L, a.nslots * a.wave_samples, guide_train_steps_);
             end();
             launches += 1 + 2 * guide_train_steps_;
@@ -1002,16 +1064,16 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
     stats_.paths = (double)p.width * p.height * p.sample_count;
     stats_.kernel_launches = launches;
     stats_.waves = waves;
-    for (int k = 0; k < 8; k++) stats_.kernel_count[k] = kcount[k];
+    for (int k = 0; k < C2G_K_KINDS; k++) stats_.kernel_count[k] = kcount[k];
     for (size_t i = 0; i < used; i++) {
         float t = 0.f;
         cudaEventElapsedTime(&t, pool[i].a, pool[i].b);
         stats_.kernel_ms[pool[i].kind] += t;
     }
     if (count) {
-        unsigned long long h[24];
+        unsigned long long h[3 * C2G_K_KINDS];
         C2G_CUDA(cudaMemcpy(h, cnt, sizeof(h), cudaMemcpyDeviceToHost));
-        for (int k = 0; k < 8; k++) {
+        for (int k = 0; k < C2G_K_KINDS; k++) {
             stats_.rays[k] = (double)h[3 * k];
             stats_.nodes[k] = (double)h[3 * k + 1];
             stats_.prims[k] = (double)h[3 * k + 2];

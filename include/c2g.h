@@ -87,7 +87,9 @@ typedef struct {
 #define C2G_K_MIS 4
 #define C2G_K_ACCUM 5
 #define C2G_K_FILM 6
-#define C2G_K_GUIDE 7
+#define C2G_K_GUIDE 7   /* guide network inference */
+#define C2G_K_TRAIN 8   /* guide training: batch build, fused forward/backward, Adam */
+#define C2G_K_KINDS 10  /* size of the per-kind arrays */
 
 /* Counting / timing switches of c2g_set_counting. */
 #define C2G_COUNT_TRAVERSAL 1  /* rays, nodes visited and prims tested per traversal kernel */
@@ -96,11 +98,11 @@ typedef struct {
 typedef struct {
     double seconds;             /* device time of the last c2g_render (CUDA events on its stream) */
     double paths;               /* camera paths traced by the last c2g_render */
-    double rays[8];             /* rays processed per kernel kind (C2G_COUNT_TRAVERSAL) */
-    double nodes[8];            /* BVH nodes visited per kernel kind (C2G_COUNT_TRAVERSAL) */
-    double prims[8];            /* primitives tested per kernel kind (C2G_COUNT_TRAVERSAL) */
-    double kernel_ms[8];        /* device time per kernel kind (C2G_COUNT_TIMING) */
-    int kernel_count[8];        /* launches per kernel kind */
+    double rays[C2G_K_KINDS];             /* rays processed per kernel kind (C2G_COUNT_TRAVERSAL) */
+    double nodes[C2G_K_KINDS];            /* BVH nodes visited per kernel kind (C2G_COUNT_TRAVERSAL) */
+    double prims[C2G_K_KINDS];            /* primitives tested per kernel kind (C2G_COUNT_TRAVERSAL) */
+    double kernel_ms[C2G_K_KINDS];        /* device time per kernel kind (C2G_COUNT_TIMING) */
+    int kernel_count[C2G_K_KINDS];        /* launches per kernel kind */
     int kernel_launches;        /* kernels launched by the last c2g_render */
     int waves;                  /* waves of the last c2g_render */
 } c2g_stats;

@@ -8,7 +8,8 @@ The reference has no learned guiding, so there is no reference function to follo
 restates the network defined by the library's C ABI (include/c2g.h, "learned guiding proposal"):
 
 * input: p = clamp((x - lo) * inv, 0, 1) per axis (FP32), then sin/cos(pi 2^f p) for f = 0..11
-  (axis-major, sin before cos), then the normal, the outgoing direction and two zeros (80 values);
+  (axis-major, sin before cos; octaves above the first by the FP32 double-angle recurrence the
+  kernels use), then the normal, the outgoing direction and two zeros (80 values);
 * layers 80->64->64->64->48 with ReLU after the hidden layers; parameters are one flat vector,
   per layer W (K x N row-major) then b (N);
 * outputs 5 per lobe (8 lobes): mean direction (normalised), concentration softplus(k) + 0.05
@@ -62,10 +63,14 @@ def encode(x, n, wo, lo, hi) -> np.ndarray:
     m = x.shape[0]
     enc = np.zeros((m, N_IN))
     for a in range(3):
+        # sin/cos(pi p) rounded to FP32, then the FP32 double-angle recurrence of the kernels:
+        # sin 2u = 2 sin u cos u, cos 2u = (cos u - sin u)(cos u + sin u)
+        s = np.sin(np.pi * p[:, a]).astype(np.float32)
+        c = np.cos(np.pi * p[:, a]).astype(np.float32)
         for f in range(FREQS):
-            ang = np.pi * (p[:, a] * (1 << f))
-            enc[:, a * 2 * FREQS + 2 * f] = np.sin(ang)
-            enc[:, a * 2 * FREQS + 2 * f + 1] = np.cos(ang)
+            enc[:, a * 2 * FREQS + 2 * f] = s
+            enc[:, a * 2 * FREQS + 2 * f + 1] = c
+            s, c = (np.float32(2) * s * c).astype(np.float32), ((c - s) * (c + s)).astype(np.float32)
     enc[:, 72:75] = np.asarray(n, np.float64)
     enc[:, 75:78] = np.asarray(wo, np.float64)
     return enc
