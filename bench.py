@@ -17,6 +17,13 @@ host) plus the film read back to host memory (c2g_film_download), wall-clock tim
 Multi-GPU: the path does not exchange data; `--gpus N` runs N independent replicas (weak scaling),
 one process per GPU, rendering the same frame; value = all paths / max time.
 
+The second half of the metric, equal-time relMSE of the guided path tracer against the plain
+one, is measured after the timed region on the slit-lit glossy room (`guided_equal_time`;
+`--guided-res 1920x1080 --guided-ref-spp 16384` for the full-size protocol, several minutes).
+
+Batched multi-job rendering (64 seeded jobs through replayed CUDA graphs, autotuned wave size and
+stream count) is measured last (`batch_run`; `--no-batch` skips it).
+
 `--impl reference` times the reference renderer's own CPU code (compiled from its sources by
 oracle/build_ref.py; the oracle port when that library cannot be built) on the host cores, on a
 bounded sample of the same workload: rows of the 1080p frame at 1 spp per step.
@@ -315,6 +322,18 @@ def run_ours(args) -> None:
             cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "Mpaths/s", "cores": 0, "kind": "unavailable", "sample": str(e)[:200]}
+    guided = None
+    if rank == 0 and world == 1 and not args.no_guided:
+        try:
+            guided = guided_equal_time(args)
+        except Exception as e:  # reported beside the headline, never required for it
+            guided = {"unavailable": str(e)[:200]}
+    batch = None
+    if rank == 0 and world == 1 and not args.no_batch:
+        try:
+            batch = batch_run(args)
+        except Exception as e:  # reported beside the headline, never required for it
+            batch = {"unavailable": str(e)[:200]}
     if rank == 0:
         line = {"metric": "Mpaths/s at 1080p (many-material scene, MIS path tracer)", "value": value, "unit": "Mpaths/s",
                 "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
@@ -328,10 +347,125 @@ def run_ours(args) -> None:
                         "d2h_bytes_per_step": int(p.width * p.height * 16)},
                 "gpu_launches": int(launches), "roofline": roof, "kernel_share": share,
                 "traversal_per_step": {k: {"rays": v[0], "nodes": v[1], "prims": v[2]} for k, v in counts.items()},
-                "clocks": clk, "cpu_baseline": cpu}
+                "clocks": clk, "cpu_baseline": cpu, "guided_equal_time": guided, "batch": batch}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def guided_equal_time(args) -> dict:
+    """Equal-time error of the guided path tracer against the plain one on the slit-lit glossy room.
+
+    Both arms render the same frame progressively (chunks of 8 spp, one sample per wave so the
+    guide trains after every sample) for the same budget of render time (the c2g_render calls
+    only; the error is evaluated outside the timer).  relMSE = mean((I - R)^2 / (R^2 + 0.01))
+    against a plain reference of `--guided-ref-spp` samples from a disjoint sample range.
+    Reported: both errors at the budget, the time the guided arm needs to reach the plain arm's
+    error (linear interpolation on its error curve), and their ratio (the target is <= 0.5)."""
+    import numpy as np
+    from crystal2_gb300 import Context, scenes
+    from crystal2_gb300 import _native as N
+
+    W, H = (int(v) for v in args.guided_res.split("x"))
+    d = tempfile.mkdtemp(prefix="c2g_guided_")
+    cp, sp = scenes.slit_room(d, width=W, height=H, spp=64, depth=12, hf_res=512)
+    ctx = Context(0)
+    ctx.load(cp, sp, tree=N.TREE_SAH)
+    tiles = ((W + 7) // 8) * ((H + 7) // 8) * 64
+
+    def params(integ, s0, n, wave_spp=1):
+        q = ctx.render_params()
+        q.integrator, q.sample_begin, q.sample_count, q.wave_paths = integ, s0, n, tiles * wave_spp
+        return q
+
+    t0 = time.perf_counter()
+    ctx.film_clear()
+    ctx.render(params(N.INTEGRATOR_PATH, 1 << 24, args.guided_ref_spp, 8))
+    ref = ctx.image().astype(np.float64)
+    ref_s = time.perf_counter() - t0
+
+    def relmse(img):
+        return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    def progressive(integ):
+        ctx.film_clear()
+        s0, spent, curve = 0, 0.0, []
+        while spent < args.guided_seconds:
+            t = time.perf_counter()
+            ctx.render(params(integ, s0, 8))
+            spent += time.perf_counter() - t
+            s0 += 8
+            curve.append((spent, s0, relmse(ctx.image().astype(np.float64))))
+        return curve
+
+    ctx.film_clear()
+    ctx.render(params(N.INTEGRATOR_PATH, 0, 4))  # first-launch costs out of the way
+    plain = progressive(N.INTEGRATOR_PATH)
+    ctx.load(cp, sp, tree=N.TREE_SAH)  # a fresh, untrained network
+    ctx.guide_config(args.guided_lr, args.guided_bsdf_fraction, 2, 1)
+    guided = progressive(N.INTEGRATOR_GUIDED)
+    target = plain[-1][2]
+    reach = None
+    for (t0_, _, e0), (t1_, _, e1) in zip(guided, guided[1:]):
+        if e1 <= target:
+            reach = t0_ + (t1_ - t0_) * ((e0 - target) / (e0 - e1) if e0 > e1 else 1.0)
+            break
+    if reach is None and guided and guided[0][2] <= target:
+        reach = guided[0][0]
+    loss, records, steps = ctx.guide_stats()
+    return {"scene": f"slit_room {W}x{H} (524k-triangle heightfield, GGX a U(0.1,0.3), slit-lit), max depth 12",
+            "reference_spp": args.guided_ref_spp, "reference_s": round(ref_s, 2), "budget_s": args.guided_seconds,
+            "plain": {"spp": plain[-1][1], "s": round(plain[-1][0], 3), "relMSE": target},
+            "guided": {"spp": guided[-1][1], "s": round(guided[-1][0], 3), "relMSE": guided[-1][2],
+                       "bsdf_fraction": args.guided_bsdf_fraction, "learning_rate": args.guided_lr,
+                       "adam_steps": steps, "last_batch": records, "last_loss": round(loss, 4)},
+            "time_to_plain_relMSE_s": None if reach is None else round(reach, 3),
+            "time_ratio": None if reach is None else round(reach / plain[-1][0], 3),
+            "equal_time_relMSE_ratio": round(guided[-1][2] / target, 3)}
+
+
+def batch_run(args) -> dict:
+    """Batched multi-job rendering: `--batch-jobs` seeded jobs (Cornell and many-material variants,
+    square resolutions log-uniform in [128, 1024], spp from {16, 64, 256, 1024}, guided or plain)
+    rendered together through replayed CUDA graphs on concurrent streams; the wave size and the
+    stream count are picked by the library's autotuner on a 4-spp trial of every job."""
+    import numpy as np
+    from crystal2_gb300 import Batch, Context, scenes
+    from crystal2_gb300 import _native as N
+
+    t0 = time.time()
+    jobs = scenes.batch_jobs(tempfile.mkdtemp(prefix="c2g_batch_"), n_jobs=args.batch_jobs)
+    ctxs = []
+    b = Batch(0)
+    n_guided = 0
+    for cp, sp, spp, guided in jobs:
+        c = Context(0)
+        c.load(cp, sp, tree=N.TREE_SAH)
+        p = c.render_params()
+        p.integrator = N.INTEGRATOR_GUIDED if guided else N.INTEGRATOR_PATH
+        p.sample_begin, p.sample_count = 0, spp
+        c.film_clear()
+        b.add(c, p)
+        ctxs.append(c)
+        n_guided += int(guided)
+    load_s = time.time() - t0
+    t0 = time.time()
+    best = b.autotune(wave_paths=(1 << 18, 1 << 19, 1 << 20, 1 << 21), streams=(1, 2, 4, 8), trial_spp=4)
+    tune_s = time.time() - t0
+    st = b.run()
+    lat = [b.latency_ms(i) for i in range(len(jobs))]
+    out = {"jobs": st.jobs, "guided_jobs": n_guided, "paths": st.paths, "seconds": round(st.seconds, 3),
+           "mpaths_per_s": round(st.mpaths_per_s, 2), "latency_p50_ms": round(st.latency_p50_ms, 2),
+           "latency_p99_ms": round(st.latency_p99_ms, 2), "latency_max_ms": round(st.latency_max_ms, 2),
+           "tuned": {"wave_paths": st.wave_paths, "streams": st.streams, "trial_mpaths_per_s": round(best, 2),
+                     "tune_s": round(tune_s, 2)},
+           "graph_launches": st.graph_launches, "scene_load_s": round(load_s, 1),
+           "resolutions": [int(c.render_params().width) for c in ctxs],
+           "latency_ms": [round(x, 2) for x in lat]}
+    b.close()
+    for c in ctxs:
+        c.close()
+    return out
 
 
 def main() -> int:
@@ -344,6 +478,14 @@ def main() -> int:
     ap.add_argument("--scale", type=float, default=1.0, help="film scale (1.0 = 1920x1080)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-guided", action="store_true", help="skip the guided-vs-plain equal-time measurement")
+    ap.add_argument("--guided-res", default="960x540")
+    ap.add_argument("--guided-ref-spp", type=int, default=4096)
+    ap.add_argument("--guided-seconds", type=float, default=4.0)
+    ap.add_argument("--guided-lr", type=float, default=2e-3)
+    ap.add_argument("--guided-bsdf-fraction", type=float, default=0.7)
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-job measurement")
+    ap.add_argument("--batch-jobs", type=int, default=64)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":

@@ -6,6 +6,6 @@ of ``include/c2g.h``; this package is its Python binding, the reference-shaped d
 """
 from ._native import C2GError, load_library  # noqa: F401
 from . import _native as native  # noqa: F401
-from .renderer import Context, Integrator, RayTracer, write_hdr  # noqa: F401
+from .renderer import Batch, Context, Integrator, RayTracer, write_hdr  # noqa: F401
 
 __all__ = ["C2GError", "Context", "Integrator", "RayTracer", "load_library", "native", "write_hdr"]

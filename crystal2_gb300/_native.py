@@ -68,6 +68,12 @@ class Stats(C.Structure):
                 ("kernel_launches", C.c_int), ("waves", C.c_int)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("jobs", C.c_int), ("paths", C.c_double), ("seconds", C.c_double), ("mpaths_per_s", C.c_double),
+                ("latency_p50_ms", C.c_double), ("latency_p99_ms", C.c_double), ("latency_max_ms", C.c_double),
+                ("wave_paths", C.c_int), ("streams", C.c_int), ("graph_launches", C.c_int)]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _FP = C.POINTER(C.c_float)
@@ -106,6 +112,14 @@ SIGNATURES = {
     "c2g_guide_gradient": (_I, [_P, _I, _FP, _FP, C.POINTER(C.c_double)]),
     "c2g_guide_stats": (_I, [_P, C.POINTER(C.c_double), _IP, _IP]),
     "c2g_guide_config": (_I, [_P, C.c_float, C.c_float, _I, _I]),
+    "c2g_batch_create": (_I, [C.POINTER(_P), _I]),
+    "c2g_batch_destroy": (None, [_P]),
+    "c2g_batch_last_error": (C.c_char_p, [_P]),
+    "c2g_batch_add": (_I, [_P, _P, C.POINTER(RenderParams), _IP]),
+    "c2g_batch_tune": (_I, [_P, _I, _I]),
+    "c2g_batch_autotune": (_I, [_P, _IP, _I, _IP, _I, _I, C.POINTER(C.c_double)]),
+    "c2g_batch_run": (_I, [_P, C.POINTER(BatchStats)]),
+    "c2g_batch_job_latency": (_I, [_P, _I, C.POINTER(C.c_double)]),
 }
 
 GUIDE_PARAMS = 16624

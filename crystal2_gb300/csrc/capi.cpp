@@ -1,6 +1,7 @@
 // C ABI (include/c2g.h) over the host scene, the tree builders and the CUDA renderer.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -458,6 +459,279 @@ int c2g_guide_config(c2g_ctx* ctx, float learning_rate, float bsdf_fraction, int
     ctx->gpu->guide().set_learning_rate(learning_rate);
     ctx->gpu->guide().set_alpha(bsdf_fraction);
     ctx->gpu->set_guide_schedule(warmup_waves, train_steps);
+    return C2G_OK;
+}
+
+}  // extern "C"
+
+// ---- batched multi-job rendering ---------------------------------------------------------------
+namespace {
+struct BatchJob {
+    c2g_ctx* ctx = nullptr;
+    c2g_render_params p{};
+    cudaGraphExec_t g_warm = nullptr;  // guided: waves that only train (mixture not used yet)
+    cudaGraphExec_t g_main = nullptr;
+    int spw = 0, waves = 0, warm_waves = 0;
+    int stream = 0;
+    cudaEvent_t done = nullptr;
+    double latency_ms = 0.0;
+    double paths() const { return (double)p.width * p.height * p.sample_count; }
+};
+}  // namespace
+
+struct c2g_batch {
+    int device = 0;
+    std::vector<BatchJob> jobs;
+    std::vector<cudaStream_t> streams;
+    int wave_paths = 1 << 20;
+    int n_streams = 4;
+    int captured_wave_paths = -1;
+    std::string last_error;
+};
+
+namespace {
+int bfail(c2g_batch* b, int code, const std::string& msg) {
+    if (b) b->last_error = msg;
+    return code;
+}
+
+void drop_graphs(BatchJob& j) {
+    if (j.g_warm) cudaGraphExecDestroy(j.g_warm);
+    if (j.g_main) cudaGraphExecDestroy(j.g_main);
+    j.g_warm = j.g_main = nullptr;
+}
+
+// Capture every job's wave graphs for the batch's wave size.
+int batch_capture(c2g_batch* b) {
+    if (b->captured_wave_paths == b->wave_paths) return C2G_OK;
+    cudaStream_t st = b->streams.empty() ? nullptr : b->streams[0];
+    for (size_t i = 0; i < b->jobs.size(); i++) {
+        BatchJob& j = b->jobs[i];
+        drop_graphs(j);
+        const int nslots = ((j.p.width + 7) / 8) * ((j.p.height + 7) / 8) * 64;
+        // samples per wave: as many as the wave size holds, dividing the job's sample count
+        int spw = std::max(1, std::min(j.p.sample_count, b->wave_paths / nslots));
+        while (j.p.sample_count % spw) spw--;
+        c2g_render_params q = j.p;
+        q.wave_paths = spw * nslots;
+        std::string err;
+        int got = 0;
+        const bool guided = q.integrator == C2G_INTEGRATOR_GUIDED;
+        // g_main: the guided integrator samples its mixture; g_warm: its first waves only train
+        int rc = j.ctx->gpu->capture_wave(q, true, st, *j.ctx->arena, &j.g_main, &got, err);
+        if (!rc && guided) rc = j.ctx->gpu->capture_wave(q, false, st, *j.ctx->arena, &j.g_warm, &got, err);
+        if (rc) return bfail(b, rc, "job " + std::to_string(i) + ": " + err);
+        j.spw = got;
+        j.waves = j.p.sample_count / got;
+        j.warm_waves = guided ? std::min(j.waves, j.ctx->gpu->guide_warmup()) : 0;
+    }
+    b->captured_wave_paths = b->wave_paths;
+    return C2G_OK;
+}
+
+int batch_streams(c2g_batch* b) {
+    while ((int)b->streams.size() < b->n_streams) {
+        cudaStream_t st;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "stream creation failed");
+        b->streams.push_back(st);
+    }
+    return C2G_OK;
+}
+
+// One pass over every job, `spp_limit` samples each (0 = the job's own count).
+int batch_pass(c2g_batch* b, int spp_limit, c2g_batch_stats* out) {
+    if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "cudaSetDevice failed");
+    // work the jobs' contexts queued on their own streams (film clears, renders) comes first
+    if (cudaDeviceSynchronize() != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "device error before the batch");
+    int rc = batch_streams(b);
+    if (rc) return rc;
+    rc = batch_capture(b);
+    if (rc) return rc;
+    const int ns = b->n_streams;
+    // longest job first onto the least-loaded stream; shortest first within a stream
+    std::vector<int> order(b->jobs.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return b->jobs[x].paths() > b->jobs[y].paths(); });
+    std::vector<double> load(ns, 0.0);
+    std::vector<std::vector<int>> per(ns);
+    for (int i : order) {
+        int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[k] += b->jobs[i].paths();
+        per[k].push_back(i);
+    }
+    for (auto& v : per) std::reverse(v.begin(), v.end());
+    for (BatchJob& j : b->jobs) {
+        std::string err;
+        rc = j.ctx->gpu->set_wave_counter(j.p.sample_begin, b->streams[0], *j.ctx->arena, err);
+        if (rc) return bfail(b, rc, err);
+        if (!j.done) cudaEventCreate(&j.done);
+    }
+    cudaEvent_t start, stop;
+    cudaEventCreate(&start);
+    cudaEventCreate(&stop);
+    cudaEventRecord(start, b->streams[0]);
+    for (int k = 1; k < ns; k++) cudaStreamWaitEvent(b->streams[k], start, 0);
+    int launches = 0;
+    double paths = 0.0;
+    // enqueue wave by wave across the streams so that no stream's host-side queue runs far ahead
+    std::vector<size_t> next_job(ns, 0);
+    std::vector<int> next_wave(ns, 0);
+    bool any = true;
+    while (any) {
+        any = false;
+        for (int k = 0; k < ns; k++) {
+            if (next_job[k] >= per[k].size()) continue;
+            any = true;
+            BatchJob& j = b->jobs[per[k][next_job[k]]];
+            const int waves = spp_limit > 0 ? std::max(1, std::min(j.waves, spp_limit / std::max(1, j.spw))) : j.waves;
+            const int w = next_wave[k];
+            cudaGraphExec_t g = (w < j.warm_waves && j.g_warm) ? j.g_warm : j.g_main;
+            if (cudaGraphLaunch(g, b->streams[k]) != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "graph launch failed");
+            launches++;
+            if (w + 1 >= waves) {
+                cudaEventRecord(j.done, b->streams[k]);
+                paths += (double)j.p.width * j.p.height * waves * j.spw;
+                next_job[k]++;
+                next_wave[k] = 0;
+            } else {
+                next_wave[k] = w + 1;
+            }
+        }
+    }
+    for (int k = 0; k < ns; k++) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, b->streams[k]);
+        cudaStreamWaitEvent(b->streams[0], e, 0);
+        cudaEventDestroy(e);
+    }
+    cudaEventRecord(stop, b->streams[0]);
+    cudaError_t e = cudaEventSynchronize(stop);
+    if (e != cudaSuccess) return bfail(b, C2G_ERR_CUDA, std::string("batch: ") + cudaGetErrorString(e));
+    float total = 0.f;
+    cudaEventElapsedTime(&total, start, stop);
+    std::vector<double> lat;
+    for (BatchJob& j : b->jobs) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, start, j.done);
+        j.latency_ms = t;
+        lat.push_back(t);
+    }
+    cudaEventDestroy(start);
+    cudaEventDestroy(stop);
+    for (BatchJob& j : b->jobs) {
+        std::string err;
+        rc = j.ctx->gpu->check_device_error(err);
+        if (rc) return bfail(b, rc, err);
+    }
+    if (out) {
+        std::sort(lat.begin(), lat.end());
+        auto pct = [&](double q) {
+            if (lat.empty()) return 0.0;
+            size_t i = (size_t)std::min<double>((double)lat.size() - 1, std::ceil(q * lat.size()) - 1);
+            return lat[i];
+        };
+        *out = c2g_batch_stats{};
+        out->jobs = (int)b->jobs.size();
+        out->paths = paths;
+        out->seconds = total * 1e-3;
+        out->mpaths_per_s = total > 0 ? paths / (total * 1e-3) / 1e6 : 0.0;
+        out->latency_p50_ms = pct(0.5);
+        out->latency_p99_ms = pct(0.99);
+        out->latency_max_ms = lat.empty() ? 0.0 : lat.back();
+        out->wave_paths = b->wave_paths;
+        out->streams = ns;
+        out->graph_launches = launches;
+    }
+    return C2G_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int c2g_batch_create(c2g_batch** out, int device) {
+    if (!out) return C2G_ERR_INVALID;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return C2G_ERR_DEVICE;
+    c2g_batch* b = new c2g_batch();
+    b->device = device;
+    *out = b;
+    return C2G_OK;
+}
+
+void c2g_batch_destroy(c2g_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    for (BatchJob& j : b->jobs) {
+        drop_graphs(j);
+        if (j.done) cudaEventDestroy(j.done);
+    }
+    for (cudaStream_t st : b->streams) cudaStreamDestroy(st);
+    delete b;
+}
+
+const char* c2g_batch_last_error(c2g_batch* b) { return b ? b->last_error.c_str() : "null batch"; }
+
+int c2g_batch_add(c2g_batch* b, c2g_ctx* job, const c2g_render_params* params, int* index) {
+    if (!b || !job || !params) return bfail(b, C2G_ERR_INVALID, "null argument");
+    if (!job->loaded || job->device != b->device) return bfail(b, C2G_ERR_STATE, "job context has no scene on the batch's device");
+    if (params->sample_count <= 0) return bfail(b, C2G_ERR_INVALID, "a job renders at least one sample");
+    for (const BatchJob& j : b->jobs)
+        if (j.ctx == job) return bfail(b, C2G_ERR_INVALID, "context already in the batch");
+    BatchJob j;
+    j.ctx = job;
+    j.p = *params;
+    b->jobs.push_back(j);
+    b->captured_wave_paths = -1;
+    if (index) *index = (int)b->jobs.size() - 1;
+    return C2G_OK;
+}
+
+int c2g_batch_tune(c2g_batch* b, int wave_paths, int streams) {
+    if (!b) return C2G_ERR_INVALID;
+    if (wave_paths < 64 || streams < 1 || streams > 32) return bfail(b, C2G_ERR_INVALID, "wave_paths >= 64 and 1 <= streams <= 32");
+    if (wave_paths != b->wave_paths) b->captured_wave_paths = -1;
+    b->wave_paths = wave_paths;
+    b->n_streams = streams;
+    return C2G_OK;
+}
+
+int c2g_batch_autotune(c2g_batch* b, const int* wave_paths, int n_wave_paths, const int* streams, int n_streams,
+                       int trial_spp, double* best_mpaths_per_s) {
+    if (!b || !wave_paths || !streams || n_wave_paths <= 0 || n_streams <= 0 || trial_spp <= 0) return bfail(b, C2G_ERR_INVALID, "invalid candidates");
+    double best = -1.0;
+    int bw = b->wave_paths, bs = b->n_streams;
+    for (int i = 0; i < n_wave_paths; i++)
+        for (int k = 0; k < n_streams; k++) {
+            int rc = c2g_batch_tune(b, wave_paths[i], streams[k]);
+            if (rc) return rc;
+            c2g_batch_stats st{};
+            rc = batch_pass(b, trial_spp, &st);
+            if (rc) return rc;
+            if (st.mpaths_per_s > best) { best = st.mpaths_per_s; bw = wave_paths[i]; bs = streams[k]; }
+        }
+    // trials leave samples in the films and train the networks: start the real run clean
+    for (BatchJob& j : b->jobs) {
+        drop_graphs(j);
+        j.ctx->gpu->guide().release(*j.ctx->arena);
+        j.ctx->gpu->film_clear(nullptr);
+    }
+    b->captured_wave_paths = -1;
+    c2g_batch_tune(b, bw, bs);
+    if (best_mpaths_per_s) *best_mpaths_per_s = best;
+    return cudaDeviceSynchronize() == cudaSuccess ? C2G_OK : bfail(b, C2G_ERR_CUDA, "autotune");
+}
+
+int c2g_batch_run(c2g_batch* b, c2g_batch_stats* stats) {
+    if (!b) return C2G_ERR_INVALID;
+    if (b->jobs.empty()) return bfail(b, C2G_ERR_STATE, "empty batch");
+    return batch_pass(b, 0, stats);
+}
+
+int c2g_batch_job_latency(c2g_batch* b, int i, double* ms) {
+    if (!b || !ms || i < 0 || i >= (int)b->jobs.size()) return bfail(b, C2G_ERR_INVALID, "bad job index");
+    *ms = b->jobs[i].latency_ms;
     return C2G_OK;
 }
 

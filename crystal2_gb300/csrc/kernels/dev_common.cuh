@@ -5,43 +5,9 @@
 #include <stdint.h>
 
 #include "../c2g_types.h"
+#include "dev_scene.h"
 
 namespace c2g {
-
-// ---- device scene view -------------------------------------------------------------------
-struct DevScene {
-    const ObjInfo* objs;
-    const TriShade* tri_shade;
-    const float4* tri_pos;        // 3 float4 per scene triangle (v0, v1, v2)
-    const Quadric* quads;
-    const Material* mats;
-    const Light* lights;
-    int n_lights;
-    int n_objs;
-    const Prim* prims;            // traversal order
-    int n_prims;
-    int tree;                     // C2G_TREE_*
-    const RefNode* ref_nodes;     // tree == REF: nodes 1..n, root 1
-    const WideNode* wide_nodes;   // tree == SAH: root 0
-    int anyhit_clip;              // 1: BVH semantics (object-box-clipped shadow interval)
-    int closest_box;              // 1: per-object box prefilter on closest hits
-    Camera cam;
-    HaltonParams hp;
-    const uint16_t* perm;         // 100 concatenated permutation tables
-    const int* perm_off;          // table offsets
-    uint64_t seed;
-    int* err;                     // device error word (C2G_DEVERR_*)
-};
-
-// Shading buckets: 0..7 = MatType of the hit's material, 8 = no material, 9 = miss.
-constexpr int kBuckets = 10;
-constexpr int kBucketNone = 8;
-constexpr int kBucketMiss = 9;
-
-enum : int {
-    DEVERR_STACK = 1,             // traversal stack overflow
-    DEVERR_QUEUE = 2,             // queue capacity exceeded
-};
 
 __device__ __forceinline__ void dev_flag_error(int* err, int code) {
     if (err) atomicOr(err, code);

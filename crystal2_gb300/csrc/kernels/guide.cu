@@ -209,10 +209,10 @@ __global__ void __launch_bounds__(128) k_guide_infer(DevScene S, GuideNet net, c
         __syncwarp();
         warp_forward32(net, wts, A, Bb, F);
         if (slot >= 0) {
-            float4* dst = reinterpret_cast<float4*>(out + (size_t)slot * kGuideOut);
-            const float4* src = reinterpret_cast<const float4*>(F + lane * kLdF);
+            float o[kGuideOut];
 #pragma unroll
-            for (int k = 0; k < kGuideOut / 4; k++) dst[k] = src[k];
+            for (int k = 0; k < kGuideOut; k++) o[k] = F[lane * kLdF + k];
+            pack_lobes(o, out + (size_t)slot * kGuidePacked);
         }
         __syncwarp();
     }
@@ -524,8 +524,12 @@ __global__ void __launch_bounds__(256, 1) k_guide_train(GuideNet net, const floa
 // Adam on the FP32 master weights (gradients normalised by the batch weight sum), then the two
 // BF16 layouts the kernels read.  The padded output columns stay zero.
 __global__ void k_guide_adam(float* params, float* grad, float* m, float* v, __nv_bfloat16* bfw, const float* stats,
-                             float lr, float b1, float b2, float eps, float c1, float c2) {
+                             float lr, float b1, float b2, float eps, const int* step) {
     const float norm = 1.f / fmaxf(stats[1], 1e-12f);
+    // bias corrections of Adam step t = *step + 1 (the counter lives on the device so that captured
+    // graphs replay correctly; k_guide_tick advances it)
+    const float t = (float)(*step + 1);
+    const float c1 = 1.f - powf(b1, t), c2 = 1.f - powf(b2, t);
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < kGuideParams; p += gridDim.x * blockDim.x) {
         int l = 3;
         while (l > 0 && p < guide_w_off(l)) l--;
@@ -552,6 +556,8 @@ __global__ void k_guide_adam(float* params, float* grad, float* m, float* v, __n
     }
 }
 
+__global__ void k_guide_tick(int* step) { *step += 1; }
+
 __global__ void k_guide_bf16_from_params(const float* params, __nv_bfloat16* bfw) {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < kGuideParams; p += gridDim.x * blockDim.x) {
         int l = 3;
@@ -572,7 +578,7 @@ __global__ void k_guide_bf16_from_params(const float* params, __nv_bfloat16* bfw
 GuideTrainer::~GuideTrainer() = default;
 
 void GuideTrainer::release(DeviceArena& arena) {
-    void* ps[] = {params_, grad_, adam_m_, adam_v_, bf_, out_, rec_, batch_, batch_count_, loss_acc_};
+    void* ps[] = {params_, grad_, adam_m_, adam_v_, bf_, out_, rec_, batch_, batch_count_, loss_acc_, step_dev_};
     for (void* p : ps)
         if (p) arena.free(p);
     params_ = grad_ = adam_m_ = adam_v_ = nullptr;
@@ -581,6 +587,7 @@ void GuideTrainer::release(DeviceArena& arena) {
     rec_ = batch_ = nullptr;
     batch_count_ = nullptr;
     loss_acc_ = nullptr;
+    step_dev_ = nullptr;
     cap_ = 0;
     rec_cap_ = 0;
     rec_depth_ = 1;
@@ -598,7 +605,9 @@ int GuideTrainer::init(DeviceArena& arena, size_t paths, int max_depth, const fl
         bf_ = (__nv_bfloat16*)A(kGuideBf16 * 2);
         loss_acc_ = (float*)A(16);
         batch_count_ = (int*)A(16);
-        if (!params_ || !grad_ || !adam_m_ || !adam_v_ || !bf_ || !loss_acc_ || !batch_count_) return C2G_ERR_OOM;
+        step_dev_ = (int*)A(16);
+        if (!params_ || !grad_ || !adam_m_ || !adam_v_ || !bf_ || !loss_acc_ || !batch_count_ || !step_dev_) return C2G_ERR_OOM;
+        cudaMemset(step_dev_, 0, 16);
         // He-uniform initialisation (seeded); the output layer starts small so the first mixture is broad
         std::vector<float> h(kGuideParams, 0.f);
         std::mt19937_64 rng(seed ^ 0x9e3779b97f4a7c15ULL);
@@ -637,7 +646,7 @@ int GuideTrainer::init(DeviceArena& arena, size_t paths, int max_depth, const fl
         // about 2^18 recorded vertices per wave: every rec_stride-th path records its bounces
         rec_stride_ = (int)std::max<size_t>(1, paths * 3 / (1u << 18));
         rec_cap_ = (paths / rec_stride_ + 1) * rec_depth_;
-        out_ = (float*)A(paths * kGuideOut * 4);
+        out_ = (float*)A(paths * kGuidePacked * 4);
         rec_ = (float4*)A(rec_cap_ * 64);
         batch_ = (float4*)A(rec_cap_ * 64);
         if (!out_ || !rec_ || !batch_) return C2G_ERR_OOM;
@@ -646,16 +655,24 @@ int GuideTrainer::init(DeviceArena& arena, size_t paths, int max_depth, const fl
     return C2G_OK;
 }
 
+namespace {
+int g_infer_grid = 0, g_train_grid = 0;
+}  // namespace
+
+void GuideTrainer::prepare_launch() {
+    if (g_infer_grid) return;
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_infer, 128, kInferSmem);
+    g_infer_grid = std::max(1, sms * std::max(1, per));
+    g_train_grid = std::max(1, sms);
+}
+
 void GuideTrainer::infer(cudaStream_t st, const void* Sv, const float4* ray_o, const float4* ray_d, const float4* hits,
                          const int* bucket_cnt, const int* bucket_list, int cap, int bucket_mask) {
-    static int grid = 0;
-    if (!grid) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_infer, 128, kInferSmem);
-        grid = std::max(1, sms * std::max(1, per));
-    }
+    prepare_launch();
+    const int grid = g_infer_grid;
     int mask = 0;
     for (int b = 0; b < kBuckets; b++)
         if (((bucket_mask >> b) & 1) && bucket_guided(b)) mask |= 1 << b;
@@ -669,20 +686,14 @@ void GuideTrainer::train(cudaStream_t st, const float4* out_L, int wave_paths, i
     cudaMemsetAsync(loss_acc_, 0, 16, st);
     k_guide_batch<<<(int)std::min<size_t>(4096, (rec_cap_ + 255) / 256), 256, 0, st>>>(
         rec_, (int)rec_cap_, rec_depth_, rec_stride_, out_L, wave_paths, batch_, batch_count_, loss_acc_, (int)rec_cap_);
-    static int grid = 0;
-    if (!grid) {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        grid = sms;
-    }
+    prepare_launch();
+    const int grid = g_train_grid;
     GuideNet net = view(false, false).net;
     for (int s = 0; s < steps; s++) {
         k_guide_train<<<grid, 256, kTrainSmem, st>>>(net, batch_, batch_count_, (int)rec_cap_, grad_, loss_acc_);
         steps_++;
-        const float b1 = 0.9f, b2 = 0.99f;
-        float c1 = 1.f - std::pow(b1, (float)steps_), c2 = 1.f - std::pow(b2, (float)steps_);
-        k_guide_adam<<<64, 256, 0, st>>>(params_, grad_, adam_m_, adam_v_, bf_, loss_acc_, lr_, b1, b2, 1e-8f, c1, c2);
+        k_guide_adam<<<64, 256, 0, st>>>(params_, grad_, adam_m_, adam_v_, bf_, loss_acc_, lr_, 0.9f, 0.99f, 1e-8f, step_dev_);
+        k_guide_tick<<<1, 1, 0, st>>>(step_dev_);
     }
 }
 
@@ -708,6 +719,7 @@ int GuideTrainer::set_params(const float* host, std::string& err) {
     cudaMemset(grad_, 0, kGuideParams * 4);
     cudaMemset(adam_m_, 0, kGuideParams * 4);
     cudaMemset(adam_v_, 0, kGuideParams * 4);
+    cudaMemset(step_dev_, 0, 16);
     k_guide_bf16_from_params<<<64, 256>>>(params_, bf_);
     steps_ = 0;
     if (cudaDeviceSynchronize() != cudaSuccess) { err = cudaGetErrorString(cudaGetLastError()); return C2G_ERR_CUDA; }
@@ -779,9 +791,11 @@ GuideStats GuideTrainer::stats() {
     int n = 0;
     if (loss_acc_) cudaMemcpy(h, loss_acc_, 16, cudaMemcpyDeviceToHost);
     if (batch_count_) cudaMemcpy(&n, batch_count_, 4, cudaMemcpyDeviceToHost);
+    int t = steps_;
+    if (step_dev_) cudaMemcpy(&t, step_dev_, 4, cudaMemcpyDeviceToHost);
     last_.loss = h[1] > 0 ? h[0] / h[1] : 0.0;
     last_.records = n;
-    last_.steps = steps_;
+    last_.steps = t;
     return last_;
 }
 

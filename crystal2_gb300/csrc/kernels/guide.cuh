@@ -93,40 +93,73 @@ __device__ __forceinline__ float vmf_pdf(const Lobe& l, float3 w) {
     return l.kappa / (2.f * kPiF * (-expm1f(-2.f * l.kappa))) * __expf(l.kappa * (c - 1.f));
 }
 
-__device__ __forceinline__ float guide_pdf(const Lobe* L, float3 w) {
-    float p = 0.f;
+// ---- packed mixture (inference output, read by the shading kernels) ---------------------------
+// Per slot kGuidePacked floats: 8 float4 (mean direction, concentration), the 8 lobe weights, and
+// the 8 products weight x vMF normaliser.  A non-finite network output is flagged by a NaN first
+// weight.
+constexpr int kGuidePacked = 48;
+
+__device__ __forceinline__ void pack_lobes(const float* out, float* dst) {
+    bool finite = true;
 #pragma unroll
-    for (int k = 0; k < kGuideLobes; k++) p += L[k].w * vmf_pdf(L[k], w);
-    return p;
+    for (int k = 0; k < kGuideOut; k++) finite = finite && isfinite(out[k]);
+    Lobe L[kGuideLobes];
+    guide_lobes(out, L);
+    float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+    for (int k = 0; k < kGuideLobes; k++) d4[k] = make_float4(L[k].mu.x, L[k].mu.y, L[k].mu.z, L[k].kappa);
+    float w[kGuideLobes], wc[kGuideLobes];
+#pragma unroll
+    for (int k = 0; k < kGuideLobes; k++) {
+        w[k] = L[k].w;
+        wc[k] = L[k].w * L[k].kappa / (2.f * kPiF * (-expm1f(-2.f * L[k].kappa)));
+    }
+    if (!finite) w[0] = __int_as_float(0x7fc00000);
+    d4[8] = make_float4(w[0], w[1], w[2], w[3]);
+    d4[9] = make_float4(w[4], w[5], w[6], w[7]);
+    d4[10] = make_float4(wc[0], wc[1], wc[2], wc[3]);
+    d4[11] = make_float4(wc[4], wc[5], wc[6], wc[7]);
 }
 
-// Sample: lobe by weight with u0 (rescaled), then the vMF around its mean (w = cos theta).
-__device__ __forceinline__ float3 guide_sample(const Lobe* L, float u0, float u1, float u2) {
+__device__ __forceinline__ bool packed_valid(const float4* p) { return isfinite(__ldg(p + 8).x); }
+
+// Mixture density at the unit direction w.
+__device__ __forceinline__ float packed_pdf(const float4* p, float3 w) {
+    const float* wc = reinterpret_cast<const float*>(p + 10);
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < kGuideLobes; k++) {
+        const float4 m = __ldg(p + k);
+        s += __ldg(wc + k) * __expf(m.w * (m.x * w.x + m.y * w.y + m.z * w.z - 1.f));
+    }
+    return s;
+}
+
+// Sample: lobe by weight with u0, then the vMF around its mean (w = cos theta by inversion).
+__device__ __forceinline__ float3 packed_sample(const float4* p, float u0, float u1, float u2) {
+    const float* wt = reinterpret_cast<const float*>(p + 8);
     int k = kGuideLobes - 1;
     float acc = 0.f;
 #pragma unroll
     for (int i = 0; i < kGuideLobes; i++) {
-        if (u0 < acc + L[i].w) { k = i; break; }
-        acc += L[i].w;
+        acc += __ldg(wt + i);
+        if (u0 < acc) { k = i; break; }
     }
-    // select the chosen lobe without dynamic register indexing
-    Lobe l = L[0];
-#pragma unroll
-    for (int i = 1; i < kGuideLobes; i++)
-        if (i == k) l = L[i];
-    float e = __expf(-2.f * l.kappa);
-    float cw = 1.f + __logf(fmaxf(u1 + (1.f - u1) * e, 1e-30f)) / l.kappa;
+    const float4 l = __ldg(p + k);
+    const float kappa = l.w;
+    const float e = __expf(-2.f * kappa);
+    float cw = 1.f + __logf(fmaxf(u1 + (1.f - u1) * e, 1e-30f)) / kappa;
     cw = fminf(fmaxf(cw, -1.f), 1.f);
-    float sw = sqrtf(fmaxf(0.f, 1.f - cw * cw));
+    const float sw = sqrtf(fmaxf(0.f, 1.f - cw * cw));
     float s, c;
     __sincosf(kTwoPiF * u2, &s, &c);
     // orthonormal basis around mu (Duff et al. 2017, "Building an Orthonormal Basis, Revisited")
-    float3 m = l.mu;
-    float sign = copysignf(1.f, m.z);
-    float a = -1.f / (sign + m.z);
-    float b = m.x * m.y * a;
-    float3 t1 = f3(1.f + sign * m.x * m.x * a, sign * b, -sign * m.x);
-    float3 t2 = f3(b, sign + m.y * m.y * a, -m.y);
+    const float3 m = f3(l.x, l.y, l.z);
+    const float sign = copysignf(1.f, m.z);
+    const float a = -1.f / (sign + m.z);
+    const float b = m.x * m.y * a;
+    const float3 t1 = f3(1.f + sign * m.x * m.x * a, sign * b, -sign * m.x);
+    const float3 t2 = f3(b, sign + m.y * m.y * a, -m.y);
     return normalize(t1 * (sw * c) + t2 * (sw * s) + m * cw);
 }
 

@@ -41,7 +41,7 @@ class DeviceArena;
 // Per-wave view handed to the shading kernels.
 struct GuideView {
     GuideNet net;
-    const float* out;      // per queue slot: kGuideOut raw network outputs
+    const float* out;      // per queue slot: the packed mixture (kGuidePacked floats, guide.cuh)
     float4* rec;           // training records, 4 float4 per (recorded path, bounce)
     int rec_stride;        // every rec_stride-th path id records its vertices
     int rec_depth;         // records per recorded path (= max depth)
@@ -71,6 +71,8 @@ public:
     // Turn this wave's records into weighted samples and take `steps` Adam steps.
     void train(cudaStream_t st, const float4* out_L, int wave_paths, int steps);
     GuideView view(bool record, bool sample) const;
+    // Launch configuration (occupancy queries), done once before any stream capture.
+    static void prepare_launch();
     GuideStats stats();
     void set_learning_rate(float lr) { lr_ = lr; }
     void set_alpha(float a) { alpha_ = a; }
@@ -93,7 +95,8 @@ private:
     float4* rec_ = nullptr;
     float4* batch_ = nullptr;        // compacted training samples (x|w, n, wo, wi)
     int* batch_count_ = nullptr;
-    float* loss_acc_ = nullptr;      // [0] weighted NLL sum, [1] weight sum
+    float* loss_acc_ = nullptr;      // [0] weighted NLL sum, [1] weight sum, [2] raw weight sum
+    int* step_dev_ = nullptr;        // Adam steps taken (device copy: captured graphs advance it)
     size_t cap_ = 0;
     int rec_stride_ = 16, rec_depth_ = 1;
     size_t rec_cap_ = 0;

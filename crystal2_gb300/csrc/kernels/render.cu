@@ -10,6 +10,7 @@
 // (FrameBuffer::AddSample).  Path state is SoA in float4 arrays and is compacted into the
 // next queue with warp ballot/popc appends, so every kernel reads its inputs coalesced.
 #include <algorithm>
+#include <functional>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -123,16 +124,8 @@ __device__ __forceinline__ void warp_count(unsigned long long* dst, unsigned v) 
     if (lane_id() == 0 && s) atomicAdd(dst, s);
 }
 
-struct WaveArgs {
-    int W, H;
-    int tiles_x;
-    int nslots;          // pixel slots (8x8 tiles)
-    int wave_samples;    // samples of this wave
-    int sample0;         // first sample index of the wave
-    int max_depth;
-    int K;               // NEE slots per path
-    int integrator;
-};
+
+__device__ __forceinline__ int wave_sample0(const WaveArgs& a) { return a.sample0_dev ? *a.sample0_dev : a.sample0; }
 
 __device__ __forceinline__ void slot_pixel(const WaveArgs& a, int slot, int& x, int& y) {
     int tile = slot >> 6, w = slot & 63;
@@ -183,7 +176,7 @@ __global__ void k_raygen(DevScene S, WaveArgs a, PathRefs out, float4* out_L, in
         }
         int j = warp_append(qcount, valid);
         if (valid) {
-            int sample = a.sample0 + s_local;
+            int sample = wave_sample0(a) + s_local;
             int vidx = halton_vector_index(S.hp, x, y, sample);
             float sx = halton_dim0(vidx, S.hp);
             float sy = halton_dim1(vidx, S.hp);
@@ -274,7 +267,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
         int px = 0, py = 0;
         if (valid) slot_pixel(a, pid - s_local * a.nslots, px, py);
         const uint32_t pixel = (uint32_t)(py * a.W + px);
-        const uint32_t sample = (uint32_t)(a.sample0 + s_local);
+        const uint32_t sample = (uint32_t)(wave_sample0(a) + s_local);
         float3 ro = f3(o4), rd = f3(d4);
         float3 beta = f3(b4), L = f3(L4);
         Hit h{h4.x, h4.y, h4.z, __float_as_int(h4.w)};
@@ -346,19 +339,13 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
         // and doubles as the BSDF technique of direct lighting (no separate MIS ray); light samples
         // are weighted against the mixture pdf.  Before the network is trained alpha = 1.
         const bool gvert = G && do_nee && !direct && (bx.flags & BXDF_SPECULAR) == 0;
-        Lobe lobes[kGuideLobes];
+        const float4* lobes = reinterpret_cast<const float4*>(gv.out + (size_t)i * kGuidePacked);
         float alpha = 1.f, detM = 1.f;
         if (gvert && gv.sample) {
-            float o40[kGuideOut];
-            const float* src = gv.out + (size_t)i * kGuideOut;
-            bool finite = true;
-#pragma unroll
-            for (int k = 0; k < kGuideOut; k++) { o40[k] = src[k]; finite = finite && isfinite(o40[k]); }
-            guide_lobes(o40, lobes);
             // a non-finite network output or a degenerate shading frame leaves this vertex to
             // plain BSDF sampling
             detM = fabsf(dot(fr.T, cross(fr.N, fr.B)));
-            alpha = (finite && detM > 1e-6f) ? gv.net.alpha : 1.f;
+            alpha = (packed_valid(lobes) && detM > 1e-6f) ? gv.net.alpha : 1.f;
         }
         bool nee_work = false, mis_ok = false, any_mis = false;
         float3 f2 = f3(0.f, 0.f, 0.f), wi2 = f3(0.f, 0.f, 0.f);
@@ -397,7 +384,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                     if (pdf_l != 0.f && !is_zero(Li)) {
                         float pdf_b;
                         float3 f = bsdf_f_pdf(bx, fr, wo, wi, nsflags, pdf_b) * fmaxf(0.f, dot(s.N, wi));
-                        if (gvert && alpha < 1.f) pdf_b = alpha * pdf_b + (1.f - alpha) * guide_pdf(lobes, wi);
+                        if (gvert && alpha < 1.f) pdf_b = alpha * pdf_b + (1.f - alpha) * packed_pdf(lobes, wi);
                         if (!is_zero(f)) {
                             bool back = dot(lpos - s.pos, s.N) < 0;
                             float3 org = s.pos + (back ? -s.N : s.N) * kSpawnEps;
@@ -466,7 +453,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                 const float3 wol = to_local(fr, wo);
                 float us = hash_uniform(pixel, sample, 0x4000u + 4u * bounce, S.seed);
                 if (us >= alpha) {
-                    float3 wg = guide_sample(lobes, hash_uniform(pixel, sample, 0x4001u + 4u * bounce, S.seed),
+                    float3 wg = packed_sample(lobes, hash_uniform(pixel, sample, 0x4001u + 4u * bounce, S.seed),
                                              hash_uniform(pixel, sample, 0x4002u + 4u * bounce, S.seed),
                                              hash_uniform(pixel, sample, 0x4003u + 4u * bounce, S.seed));
                     // l = M^-1 wg (rows of the inverse: the cross products over det M; the frame
@@ -479,11 +466,11 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                     wi = to_world(fr, l);
                     const float lm = length(wi);
                     stype = (bx.flags & ~(BXDF_REFLECTION | BXDF_TRANSMISSION)) | BXDF_REFLECTION;
-                    pdf = alpha * pb + (1.f - alpha) * guide_pdf(lobes, wg) * detM / (lm * lm * lm);
+                    pdf = alpha * pb + (1.f - alpha) * packed_pdf(lobes, wg) * detM / (lm * lm * lm);
                     ok = !is_zero(f) && pdf > 0.f;
                 } else if (ok) {
                     const float lm = length(wi);
-                    pdf = alpha * pdf + (1.f - alpha) * guide_pdf(lobes, wi * (1.f / lm)) * detM / (lm * lm * lm);
+                    pdf = alpha * pdf + (1.f - alpha) * packed_pdf(lobes, wi * (1.f / lm)) * detM / (lm * lm * lm);
                 }
             }
             if (ok && fabsf(pdf) != 0.f) {
@@ -825,6 +812,7 @@ int GpuScene::upload(const HostScene& s, int tree, const RefTree* ref, const Sah
         for (int k = 0; k < 3; k++) { box_lo_[k] = std::min(box_lo_[k], b[k]); box_hi_[k] = std::max(box_hi_[k], b[3 + k]); }
     }
     guide_steps_ = 0;
+    wave_counter_ = nullptr;  // freed with the previous scene's buffers
     guide_.release(arena);  // a new scene trains a new network
     present_buckets_ = 1 << kBucketMiss;
     for (const ObjInfo& o : s.objs) present_buckets_ |= 1 << (o.material < 0 ? kBucketNone : s.mats[o.material].type);
@@ -870,7 +858,27 @@ int GpuScene::film_download(float* rgb_sum, float* weight, float* rgb_sumsq, std
     return C2G_OK;
 }
 
-int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_t st, DeviceArena& arena, std::string& err) {
+namespace {
+int g_raygen = 0, g_ext = 0, g_ext_c = 0, g_shade = 0, g_sh = 0, g_sh_c = 0, g_mis = 0, g_mis_c = 0, g_acc = 0, g_film = 0;
+void ensure_grids() {
+    if (g_raygen) return;
+    g_raygen = grid_for((const void*)k_raygen, 256);
+    g_ext = grid_for((const void*)k_extend<false>, 128);
+    g_ext_c = grid_for((const void*)k_extend<true>, 128);
+    g_shade = grid_for((const void*)k_shade<MAT_DIFFUSE, false>, 128);
+    g_sh = grid_for((const void*)k_shadow<false>, 128);
+    g_sh_c = grid_for((const void*)k_shadow<true>, 128);
+    g_mis = grid_for((const void*)k_mis<false>, 128);
+    g_mis_c = grid_for((const void*)k_mis<true>, 128);
+    g_acc = grid_for((const void*)k_accumulate, 256);
+    g_film = grid_for((const void*)k_film, 256);
+}
+
+__global__ void k_advance(int* sample0, int by) { *sample0 += by; }
+}  // namespace
+
+// Validate p, size the wave buffers and (guided) the network for it; fills the wave plan.
+int GpuScene::prepare(const c2g_render_params& p, DeviceArena& arena, WavePlan& plan, std::string& err) {
     if (!sb_->film) { err = "no scene loaded"; return C2G_ERR_STATE; }
     if (p.width != film_w_ || p.height != film_h_) { err = "render size differs from the loaded film size"; return C2G_ERR_INVALID; }
     if (p.max_depth < 0 || p.sample_count < 0 || p.sample_begin < 0) { err = "invalid render parameters"; return C2G_ERR_INVALID; }
@@ -878,13 +886,15 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         err = "unknown integrator";
         return C2G_ERR_INVALID;
     }
-    const bool guided = p.integrator == C2G_INTEGRATOR_GUIDED;
     if (p.max_depth > 255) { err = "max_depth above 255"; return C2G_ERR_INVALID; }
-    DevScene S = sb_->S;
+    plan.guided = p.integrator == C2G_INTEGRATOR_GUIDED;
+    DevScene& S = plan.S;
+    S = sb_->S;
     S.anyhit_clip = p.accel == C2G_ACCEL_BVH ? 1 : 0;
     S.closest_box = p.accel == C2G_ACCEL_BVH ? 1 : 0;
     S.seed = p.seed;
-    WaveArgs a{};
+    WaveArgs& a = plan.a;
+    a = WaveArgs{};
     a.W = p.width;
     a.H = p.height;
     a.tiles_x = (p.width + 7) / 8;
@@ -897,6 +907,10 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
     size_t want = p.wave_paths > 0 ? (size_t)p.wave_paths : (size_t)(1u << 21);
     int spw = (int)std::max<size_t>(1, want / (size_t)a.nslots);
     spw = std::min(spw, std::max(1, p.sample_count));
+    plan.spw = spw;
+    // Bounce levels per wave.  A guided vertex's ray is traced one level past the depth for the
+    // emission it reaches; direct lighting walks pass-through surfaces up to 255 hops.
+    plan.levels = p.integrator == C2G_INTEGRATOR_DIRECT ? 255 : p.max_depth + (plan.guided ? 1 : 0);
     size_t P = (size_t)spw * a.nslots;
     if (wb_->P < P || wb_->K != a.K) {
         for (void* q : wb_->owned) arena.free(q);
@@ -927,25 +941,152 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         wb_->P = P;
         wb_->K = a.K;
     }
+    if (plan.guided) {
+        int rc = guide_.init(arena, wb_->P, p.max_depth, box_lo_, box_hi_, p.seed, err);
+        if (rc) return rc;
+    }
+    ensure_grids();
+    return C2G_OK;
+}
+
+// Enqueue one wave (a.wave_samples samples of every pixel slot) on st: raygen, the bounce levels,
+// the film and (guided) a training step.  begin/end bracket every launch (timing hooks).
+int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideView& gv, bool count, cudaStream_t st,
+                           const std::function<void(int)>& begin, const std::function<void()>& end, int& launches,
+                           std::string& err) {
+    const DevScene& S = plan.S;
+    const bool guided = plan.guided;
     WaveBuffers& w = *wb_;
+    unsigned long long* cnt = sb_->counts;
+    launches = 0;
+    int* C = w.counters;
+    C2G_CUDA(cudaMemsetAsync(C, 0, 256, st));
+    PathRefs buf[2] = {{w.o[0], w.d[0], w.beta[0], w.L[0]}, {w.o[1], w.d[1], w.beta[1], w.L[1]}};
+    begin(C2G_K_RAYGEN);
+    k_raygen<<<g_raygen, 256, 0, st>>>(S, a, buf[0], w.out_L, C + 0);
+    end();
+    int cur = 0;
+    for (int b = 0; b < plan.levels; b++) {
+        int nxt = cur ^ 1;
+        if (b >= a.max_depth && a.integrator == C2G_INTEGRATOR_DIRECT) {
+            // pass-through hops past the depth: stop once the queue is empty
+            int qn = 0;
+            C2G_CUDA(cudaMemcpyAsync(&qn, C + cur, sizeof(int), cudaMemcpyDeviceToHost, st));
+            C2G_CUDA(cudaStreamSynchronize(st));
+            if (qn == 0) break;
+        }
+        begin(C2G_K_EXTEND);
+        cudaMemsetAsync(C + kCntBucket, 0, sizeof(int) * kBuckets, st);
+        if (count)
+            k_extend<true><<<g_ext_c, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
+                                                    C + kCntBucket, w.bucket_list, (int)w.P, cnt);
+        else
+            k_extend<false><<<g_ext, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
+                                                     C + kCntBucket, w.bucket_list, (int)w.P, cnt);
+        end();
+        if (gv.sample) {
+            begin(C2G_K_GUIDE);
+            guide_.infer(st, &S, buf[cur].o, buf[cur].d, w.hit, C + kCntBucket, w.bucket_list, (int)w.P, present_buckets_);
+            end();
+            launches++;
+        }
+        ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc, w.mis_hit};
+        for (int bk = 0; bk < kBuckets; bk++) {
+            if (!(present_buckets_ & (1 << bk))) continue;
+            begin(C2G_K_SHADE);
+            launch_shade(bk, g_shade, st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so, gv, guided);
+            end();
+            launches++;
+        }
+        begin(C2G_K_SHADOW);
+        if (count) k_shadow<true><<<g_sh_c, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
+        else k_shadow<false><<<g_sh, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
+        end();
+        begin(C2G_K_MIS);
+        if (count) k_mis<true><<<g_mis_c, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
+        else k_mis<false><<<g_mis, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
+        end();
+        begin(C2G_K_ACCUM);
+        k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.mis_hit, w.out_L, C + cur, gv);
+        end();
+        launches += 4;
+        cur = nxt;
+    }
+    begin(C2G_K_FILM);
+    k_film<<<g_film, 256, 0, st>>>(a, w.out_L, sb_->film, sb_->film_m2);
+    end();
+    launches += 2;
+    if (guided) {
+        // online training on this wave's recorded vertices (batch build, fused fwd/bwd, Adam)
+        begin(C2G_K_TRAIN);
+        guide_.train(st, w.out_L, a.nslots * a.wave_samples, guide_train_steps_);
+        end();
+        launches += 1 + 3 * guide_train_steps_;
+    }
+    if (a.sample0_dev) {
+        k_advance<<<1, 1, 0, st>>>(const_cast<int*>(a.sample0_dev), a.wave_samples);
+        launches++;
+    }
+    return C2G_OK;
+}
+
+int GpuScene::set_wave_counter(int sample, cudaStream_t st, DeviceArena& arena, std::string& err) {
+    if (!wave_counter_) {
+        wave_counter_ = (int*)arena.alloc(256, err);
+        if (!wave_counter_) return C2G_ERR_OOM;
+        sb_->owned.push_back(wave_counter_);
+    }
+    C2G_CUDA(cudaMemcpyAsync(wave_counter_, &sample, sizeof(int), cudaMemcpyHostToDevice, st));
+    C2G_CUDA(cudaStreamSynchronize(st));
+    return C2G_OK;
+}
+
+int GpuScene::capture_wave(const c2g_render_params& p, bool guide_sample, cudaStream_t st, DeviceArena& arena,
+                           cudaGraphExec_t* exec, int* wave_samples, std::string& err) {
+    if (p.integrator == C2G_INTEGRATOR_DIRECT) {
+        err = "batched rendering runs the path tracers (the direct lighting walk synchronises)";
+        return C2G_ERR_UNSUPPORTED;
+    }
+    WavePlan plan;
+    int rc = prepare(p, arena, plan, err);
+    if (rc) return rc;
+    rc = set_wave_counter(p.sample_begin, st, arena, err);
+    if (rc) return rc;
+    guide_.prepare_launch();
+    WaveArgs a = plan.a;
+    a.wave_samples = plan.spw;
+    a.sample0 = 0;
+    a.sample0_dev = wave_counter_;
+    const GuideView gv = plan.guided ? guide_.view(true, guide_sample) : GuideView{};
+    auto no_begin = [](int) {};
+    auto no_end = []() {};
+    C2G_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    int launches = 0;
+    rc = enqueue_wave(plan, a, gv, false, st, no_begin, no_end, launches, err);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (rc || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        if (!rc) { err = std::string("stream capture: ") + cudaGetErrorString(e); rc = C2G_ERR_CUDA; }
+        return rc;
+    }
+    e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { err = std::string("graph instantiation: ") + cudaGetErrorString(e); return C2G_ERR_CUDA; }
+    *wave_samples = plan.spw;
+    return C2G_OK;
+}
+
+int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_t st, DeviceArena& arena, std::string& err) {
+    (void)s;
+    WavePlan plan;
+    int rc = prepare(p, arena, plan, err);
+    if (rc) return rc;
+    const bool guided = plan.guided;
     const bool count = (counting_ & C2G_COUNT_TRAVERSAL) != 0;
     const bool timing = (counting_ & C2G_COUNT_TIMING) != 0;
     unsigned long long* cnt = sb_->counts;
     if (count) C2G_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 3 * C2G_K_KINDS, st));
-
-    static int g_raygen = 0, g_ext = 0, g_ext_c = 0, g_shade = 0, g_sh = 0, g_sh_c = 0, g_mis = 0, g_mis_c = 0, g_acc = 0, g_film = 0;
-    if (!g_raygen) {
-        g_raygen = grid_for((const void*)k_raygen, 256);
-        g_ext = grid_for((const void*)k_extend<false>, 128);
-        g_ext_c = grid_for((const void*)k_extend<true>, 128);
-        g_shade = grid_for((const void*)k_shade<MAT_DIFFUSE, false>, 128);
-        g_sh = grid_for((const void*)k_shadow<false>, 128);
-        g_sh_c = grid_for((const void*)k_shadow<true>, 128);
-        g_mis = grid_for((const void*)k_mis<false>, 128);
-        g_mis_c = grid_for((const void*)k_mis<true>, 128);
-        g_acc = grid_for((const void*)k_accumulate, 256);
-        g_film = grid_for((const void*)k_film, 256);
-    }
     // per-launch events (timing mode): a pool reused across calls
     struct Ev { cudaEvent_t a, b; int kind; };
     static std::vector<Ev> pool;
@@ -968,89 +1109,23 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         cudaEventRecord(pool[used].b, st);
         used++;
     };
-    if (guided) {
-        int rc = guide_.init(arena, w.P, p.max_depth, box_lo_, box_hi_, p.seed, err);
-        if (rc) return rc;
-    }
-    // Bounce levels per wave.  A guided vertex's ray is traced one level past the depth for the
-    // emission it reaches; direct lighting walks pass-through surfaces up to 255 hops.
-    const int levels = p.integrator == C2G_INTEGRATOR_DIRECT ? 255 : p.max_depth + (guided ? 1 : 0);
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
     cudaEventRecord(ev0, st);
     int launches = 0, waves = 0;
-    int* C = w.counters;
-    for (int s0 = 0; s0 < p.sample_count; s0 += spw) {
-        a.wave_samples = std::min(spw, p.sample_count - s0);
+    WaveArgs a = plan.a;
+    for (int s0 = 0; s0 < p.sample_count; s0 += plan.spw) {
+        a.wave_samples = std::min(plan.spw, p.sample_count - s0);
         a.sample0 = p.sample_begin + s0;
-        C2G_CUDA(cudaMemsetAsync(C, 0, 256, st));
-        PathRefs buf[2] = {{w.o[0], w.d[0], w.beta[0], w.L[0]}, {w.o[1], w.d[1], w.beta[1], w.L[1]}};
         // guided waves record training vertices; they sample the mixture once the network has trained
         const GuideView gv = guided ? guide_.view(true, guide_steps_ >= guide_warmup_) : GuideView{};
-        begin(C2G_K_RAYGEN);
-        k_raygen<<<g_raygen, 256, 0, st>>>(S, a, buf[0], w.out_L, C + 0);
-        end();
-        int cur = 0;
-        for (int b = 0; b < levels; b++) {
-            int nxt = cur ^ 1;
-            if (b >= p.max_depth && p.integrator == C2G_INTEGRATOR_DIRECT) {
-                // pass-through hops past the depth: stop once the queue is empty
-                int qn = 0;
-                C2G_CUDA(cudaMemcpyAsync(&qn, C + cur, sizeof(int), cudaMemcpyDeviceToHost, st));
-                C2G_CUDA(cudaStreamSynchronize(st));
-                if (qn == 0) break;
-            }
-            begin(C2G_K_EXTEND);
-            cudaMemsetAsync(C + kCntBucket, 0, sizeof(int) * kBuckets, st);
-            if (count)
-                k_extend<true><<<g_ext_c, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
-                                                        C + kCntBucket, w.bucket_list, (int)w.P, cnt);
-            else
-                k_extend<false><<<g_ext, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
-                                                         C + kCntBucket, w.bucket_list, (int)w.P, cnt);
-            end();
-            if (gv.sample) {
-                begin(C2G_K_GUIDE);
-                guide_.infer(st, &S, buf[cur].o, buf[cur].d, w.hit, C + kCntBucket, w.bucket_list, (int)w.P, present_buckets_);
-                end();
-                launches++;
-            }
-            ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc, w.mis_hit};
-            for (int bk = 0; bk < kBuckets; bk++) {
-                if (!(present_buckets_ & (1 << bk))) continue;
-                begin(C2G_K_SHADE);
-                launch_shade(bk, g_shade, st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so, gv, guided);
-                end();
-                launches++;
-            }
-            begin(C2G_K_SHADOW);
-            if (count) k_shadow<true><<<g_sh_c, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
-            else k_shadow<false><<<g_sh, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
-            end();
-            begin(C2G_K_MIS);
-            if (count) k_mis<true><<<g_mis_c, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
-            else k_mis<false><<<g_mis, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
-            end();
-            begin(C2G_K_ACCUM);
-            k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.mis_hit, w.out_L, C + cur, gv);
-            end();
-            launches += 4;
-            cur = nxt;
-        }
-        begin(C2G_K_FILM);
-        k_film<<<g_film, 256, 0, st>>>(a, w.out_L, sb_->film, sb_->film_m2);
-        end();
-        launches += 2;
+        int n = 0;
+        rc = enqueue_wave(plan, a, gv, count, st, begin, end, n, err);
+        if (rc) return rc;
+        launches += n;
         waves++;
-        if (guided) {
-            // online training on this wave's recorded vertices (batch build, fused fwd/bwd, Adam)
-            begin(C2G_K_TRAIN);
-            guide_.train(st, w.out_L, a.nslots * a.wave_samples, guide_train_steps_);
-            end();
-            launches += 1 + 2 * guide_train_steps_;
-            guide_steps_++;
-        }
+        if (guided) guide_steps_++;
     }
     cudaEventRecord(ev1, st);
     C2G_CUDA(cudaGetLastError());

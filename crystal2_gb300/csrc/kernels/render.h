@@ -4,10 +4,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <string>
 #include <vector>
 
 #include "../c2g_types.h"
+#include "dev_scene.h"
 #include "guide.h"
 #include "../../../include/c2g.h"
 
@@ -38,6 +40,28 @@ private:
 struct DeviceSceneBuffers;
 struct WaveBuffers;
 
+// Launch-independent arguments of the wave kernels (render.cu).
+struct WaveArgs {
+    int W, H;
+    int tiles_x;
+    int nslots;          // pixel slots (8x8 tiles)
+    int wave_samples;    // samples of this wave
+    int sample0;         // first sample index of the wave
+    const int* sample0_dev;  // when set: the first sample index is read here (replayed graphs)
+    int max_depth;
+    int K;               // NEE slots per path
+    int integrator;
+};
+
+// One render call's per-wave setup: scene view, wave arguments, samples per wave, bounce levels.
+struct WavePlan {
+    DevScene S;
+    WaveArgs a;
+    int spw = 1;
+    int levels = 0;
+    bool guided = false;
+};
+
 // Everything the kernels need for one loaded scene + its film.
 class GpuScene {
 public:
@@ -67,8 +91,24 @@ public:
     const c2g_stats& stats() const { return stats_; }
     int check_device_error(std::string& err);
 
+    // ---- batched rendering (capi batch calls) ----
+    // Capture one wave of p (samples per wave chosen by prepare) as a CUDA graph whose sample index
+    // lives in device memory and is advanced by the graph itself, so the graph replays wave after
+    // wave.  guide_sample: the guided integrator draws from the mixture in this graph.  Returns
+    // the samples one launch renders in *wave_samples.
+    int capture_wave(const c2g_render_params& p, bool guide_sample, cudaStream_t st, DeviceArena& arena,
+                     cudaGraphExec_t* exec, int* wave_samples, std::string& err);
+    // Device counter the captured graphs read their first sample index from.
+    int set_wave_counter(int sample, cudaStream_t st, DeviceArena& arena, std::string& err);
+    int guide_warmup() const { return guide_warmup_; }
+
 private:
+    int prepare(const c2g_render_params& p, DeviceArena& arena, WavePlan& plan, std::string& err);
+    int enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideView& gv, bool count, cudaStream_t st,
+                     const std::function<void(int)>& begin, const std::function<void()>& end, int& launches,
+                     std::string& err);
     DeviceSceneBuffers* sb_;
+    int* wave_counter_ = nullptr;  // device sample index of captured wave graphs
     WaveBuffers* wb_;
     int counting_ = 0;
     int present_buckets_ = 0;  // material buckets the loaded scene can produce

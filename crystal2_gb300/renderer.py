@@ -207,6 +207,71 @@ class Context:
                                               int(train_steps)))
 
 
+class Batch:
+    """Many jobs (contexts with loaded scenes + render parameters) rendered together on one GPU
+    through replayed CUDA graphs on concurrent streams (c2g_batch_* in include/c2g.h)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = N.load_library()
+        h = C.c_void_p()
+        rc = self._lib.c2g_batch_create(C.byref(h), device)
+        if rc != N.C2G_OK:
+            raise N.C2GError(rc, "c2g_batch_create failed")
+        self._h = h
+        self.jobs: list = []
+
+    def _raise(self, rc: int):
+        raise N.C2GError(rc, (self._lib.c2g_batch_last_error(self._h) or b"").decode())
+
+    def add(self, ctx: "Context", params: N.RenderParams) -> int:
+        """Add a job; returns its index.  The context must outlive the batch."""
+        idx = C.c_int(-1)
+        rc = self._lib.c2g_batch_add(self._h, ctx.handle, C.byref(params), C.byref(idx))
+        if rc:
+            self._raise(rc)
+        self.jobs.append(ctx)
+        return idx.value
+
+    def tune(self, wave_paths: int, streams: int) -> None:
+        rc = self._lib.c2g_batch_tune(self._h, int(wave_paths), int(streams))
+        if rc:
+            self._raise(rc)
+
+    def autotune(self, wave_paths=(1 << 18, 1 << 19, 1 << 20, 1 << 21), streams=(1, 2, 4, 8), trial_spp: int = 4) -> float:
+        wp = np.ascontiguousarray(wave_paths, np.int32)
+        sn = np.ascontiguousarray(streams, np.int32)
+        best = C.c_double(0.0)
+        rc = self._lib.c2g_batch_autotune(self._h, N.iptr(wp), wp.size, N.iptr(sn), sn.size, int(trial_spp), C.byref(best))
+        if rc:
+            self._raise(rc)
+        return best.value
+
+    def run(self) -> N.BatchStats:
+        st = N.BatchStats()
+        rc = self._lib.c2g_batch_run(self._h, C.byref(st))
+        if rc:
+            self._raise(rc)
+        return st
+
+    def latency_ms(self, i: int) -> float:
+        v = C.c_double(0.0)
+        rc = self._lib.c2g_batch_job_latency(self._h, int(i), C.byref(v))
+        if rc:
+            self._raise(rc)
+        return v.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.c2g_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Integrator:
     """String factory of the integrators (Integrator::LoadIntegrator)."""
 

@@ -178,6 +178,53 @@ def cornell(out_dir: str, width=256, height=256, spp=64, depth=8, accel="BVH", t
     return write_scene(d, cfg, camera((0, 1, -3.8), (0, 1, 0), 40), objs, "cornell")
 
 
+def cornell_variant(out_dir: str, seed: int, width=256, height=256, spp=64, depth=8, accel="BVH",
+                    threads=8) -> tuple[str, str]:
+    """The Cornell box with its materials re-drawn from `seed`: wall albedos U(0.2, 0.9) per channel,
+    the two spheres each diffuse, GGX (alpha U(0.05, 0.6)) or mirror."""
+    d = os.path.abspath(out_dir)
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    w = _box_walls(d)
+    lp = os.path.join(d, "light.obj")
+    h, ly = 0.25, 1.999
+    quad_obj(lp, [(-h, ly, -h), (-h, ly, h), (h, ly, h), (h, ly, -h)], (0, -1, 0))
+
+    def ball():
+        k = int(rng.integers(0, 3))
+        if k == 0:
+            return diffuse(rng.uniform(0.2, 0.9, 3))
+        if k == 1:
+            return micro(rng.uniform(0.5, 1.0, 3), rng.uniform(0.05, 0.6))
+        return mirror(rng.uniform(0.7, 1.0, 3))
+
+    objs = [mesh(w[k], diffuse(rng.uniform(0.2, 0.9, 3))) for k in ("floor", "ceiling", "back", "xpos", "xneg")]
+    objs += [mesh(lp, diffuse((0, 0, 0)), area_light=(15, 15, 15)),
+             sphere((-0.45, 0.3, 0.25), 0.3, ball()), sphere((0.45, 0.3, -0.3), 0.3, ball())]
+    cfg = config_json(width, height, spp, depth, accel=accel, threads=threads)
+    return write_scene(d, cfg, camera((0, 1, -3.8), (0, 1, 0), 40), objs, "cornell")
+
+
+def batch_jobs(out_dir: str, n_jobs: int = 64, seed: int = 4, n_grid: int = 8, subdiv: int = 4):
+    """Seeded multi-job workload: each job a variant of the Cornell box or of the many-material
+    scene (materials re-drawn; the many-material variant on an n_grid x n_grid sphere grid),
+    square resolution log-uniform in [128, 1024], spp from {16, 64, 256, 1024}, guided or plain.
+    Returns [(config_path, scene_path, spp, guided)]."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for j in range(n_jobs):
+        side = int(round(2 ** rng.uniform(7, 10)))
+        spp = int(rng.choice([16, 64, 256, 1024]))
+        guided = bool(rng.integers(0, 2))
+        d = os.path.join(out_dir, f"job{j:03d}")
+        if rng.integers(0, 2) == 0:
+            cp, sp = cornell_variant(d, seed=1000 + j, width=side, height=side, spp=spp)
+        else:
+            cp, sp = many_material(d, width=side, height=side, spp=spp, seed=2000 + j, n_grid=n_grid, subdiv=subdiv)
+        jobs.append((cp, sp, spp, guided))
+    return jobs
+
+
 def material_box(out_dir: str, width=64, height=64, spp=16, depth=8, accel="BVH", threads=8) -> tuple[str, str]:
     """Every material family, a disk, a point light, a sphere light and a pass-through object."""
     d = os.path.abspath(out_dir)

@@ -160,6 +160,44 @@ int c2g_render_noalloc(c2g_ctx* ctx, const c2g_render_params* params, float* fil
 /* C2G_COUNT_* flags (0 = off): traversal counters (slower kernels) and per-launch timing. */
 int c2g_set_counting(c2g_ctx* ctx, int flags);
 
+/* ---- batched multi-job rendering ---------------------------------------------------------------
+ * No counterpart in the reference (one scene per RayTracer).  A batch renders many jobs - each a
+ * context with its own loaded scene and its own render parameters (path tracer or guided) - on one
+ * GPU: every job's wave is captured once as a CUDA graph that replays wave after wave, the jobs
+ * are spread over concurrent streams (longest-first onto the least-loaded stream, shortest-first
+ * within a stream), and the films land in each job's context (c2g_film_download).  The wave size
+ * and the stream count come from c2g_batch_tune or c2g_batch_autotune.  Jobs' contexts must live
+ * as long as the batch; a context belongs to at most one batch. */
+typedef struct c2g_batch c2g_batch;
+typedef struct c2g_batch_stats {
+    int jobs;
+    double paths;               /* camera paths rendered by the run */
+    double seconds;             /* device time from the first launch to the last job's end */
+    double mpaths_per_s;
+    double latency_p50_ms;      /* job completion times from the batch start */
+    double latency_p99_ms;
+    double latency_max_ms;
+    int wave_paths;             /* configuration the run used */
+    int streams;
+    int graph_launches;
+} c2g_batch_stats;
+int c2g_batch_create(c2g_batch** out, int device);
+void c2g_batch_destroy(c2g_batch* b);
+const char* c2g_batch_last_error(c2g_batch* b);
+/* Add a job: params->sample_count samples from params->sample_begin; *index = its job index. */
+int c2g_batch_add(c2g_batch* b, c2g_ctx* job, const c2g_render_params* params, int* index);
+/* Fix the configuration: paths per wave (rounded per job so that a wave holds whole samples that
+ * divide the job's sample count) and concurrent streams (1..32). */
+int c2g_batch_tune(c2g_batch* b, int wave_paths, int streams);
+/* Time each (wave_paths, streams) pair of the candidate lists on a short trial of every job
+ * (trial_spp samples each, films and networks reset afterwards), keep the fastest. */
+int c2g_batch_autotune(c2g_batch* b, const int* wave_paths, int n_wave_paths, const int* streams, int n_streams,
+                       int trial_spp, double* best_mpaths_per_s);
+/* Render every job once (films accumulate; clear them with c2g_film_clear between runs). */
+int c2g_batch_run(c2g_batch* b, c2g_batch_stats* stats);
+/* Completion time of job i in the last run (ms from the batch start). */
+int c2g_batch_job_latency(c2g_batch* b, int i, double* ms);
+
 /* ---- learned guiding proposal (C2G_INTEGRATOR_GUIDED) -------------------------------------------
  * No counterpart in the reference, which has no guided integrator; these calls configure and
  * inspect the network the guided path tracer trains online.  The network maps (position in the
