@@ -49,7 +49,7 @@ WORKLOAD = {
     "materials": "GGX U(0.05,0.8), aniso GGX U(0.05,0.6)^2, glass IOR 1.5 a=0.1, mirror, diffuse U(0.2,0.9)",
     "lights": "2 area quads Le=20 (4 triangle lights) + point light flux 50*4pi",
     "resolution": "1920x1080", "spp_full_render": 256, "max_depth": 16, "sampler": "Halton",
-    "tree": "SAH (binned, 2-wide compact nodes)", "accel_semantics": "BVH",
+    "tree": "SAH (binned, 16 bins, leaves <= 4)", "accel_semantics": "BVH",
 }
 
 
@@ -217,6 +217,7 @@ def run_ours(args) -> None:
     cp, sp = make_scene(wdir, spp=spp_full, scale=args.scale)
     ctx = Context(local)
     t0 = time.time()
+    ctx.set_traversal(args.sah_width)
     ctx.load(cp, sp, tree=N.TREE_SAH)
     load_s = time.time() - t0
     p = ctx.render_params()
@@ -342,7 +343,8 @@ def run_ours(args) -> None:
                 "config": dict(WORKLOAD, spp_per_step=sps, paths_per_step=p.width * p.height * sps,
                                parallelism=f"replicas x{world}" if world > 1 else "single GPU",
                                l2="inputs larger than L2 (scene + wave state >> 129 MB); no flush",
-                               scene_load_s=round(load_s, 2), scale=args.scale),
+                               scene_load_s=round(load_s, 2), scale=args.scale,
+                               traversal=f"{args.sah_width}-wide nodes, while-while with leaf postponing"),
                 "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": C.sizeof(p),
                         "d2h_bytes_per_step": int(p.width * p.height * 16)},
                 "gpu_launches": int(launches), "roofline": roof, "kernel_share": share,
@@ -485,6 +487,7 @@ def main() -> int:
     ap.add_argument("--guided-lr", type=float, default=2e-3)
     ap.add_argument("--guided-bsdf-fraction", type=float, default=0.7)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-job measurement")
+    ap.add_argument("--sah-width", type=int, default=4, choices=[2, 4], help="SAH traversal variant")
     ap.add_argument("--batch-jobs", type=int, default=64)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

@@ -101,6 +101,15 @@ struct alignas(16) WideNode {
     float hi1[3]; int n1;
 };
 
+// Four-wide SAH node (128 B): the boxes of up to four children as SoA lanes, then the children:
+// >= 0 an inner Node4 index, < 0 a leaf -1 - (first prim << 3 | count), INT_MIN an empty slot
+// (its box is empty and never hit).  Collapsed from the binary SAH tree: same boxes, same leaves.
+struct alignas(16) Node4 {
+    float lox[4], hix[4], loy[4], hiy[4], loz[4], hiz[4];
+    int child[4];
+    int pad[4];
+};
+
 // Prim record in traversal order (48 B).  Triangles: v0, v1, v2 (w of v0 = obj | type << 30).
 // Spheres/disks: v0 = (unused, obj | type << 30), v1 = box min (w = quadric index), v2 = box max.
 struct alignas(16) Prim {

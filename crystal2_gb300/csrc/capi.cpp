@@ -48,7 +48,10 @@ int build_and_upload(c2g_ctx* ctx, int tree) {
     if (tree != C2G_TREE_REF_EQUAL_COUNT && tree != C2G_TREE_SAH) return fail(ctx, C2G_ERR_INVALID, "unknown tree kind");
     // the reference tree is always built: it defines the primitive order the parity checks use
     build_ref_tree(*ctx->scene, ctx->ref);
-    if (tree == C2G_TREE_SAH) build_sah_tree(*ctx->scene, ctx->sah, 4);
+    if (tree == C2G_TREE_SAH) {
+        build_sah_tree(*ctx->scene, ctx->sah, 4);
+        collapse_bvh4(ctx->sah);
+    }
     ctx->tree = tree;
     ctx->host_loaded = true;
     if (ctx->host_only) return C2G_OK;
@@ -307,6 +310,13 @@ int c2g_get_stats(c2g_ctx* ctx, c2g_stats* out) {
 int c2g_set_counting(c2g_ctx* ctx, int flags) {
     if (!ctx) return C2G_ERR_INVALID;
     ctx->gpu->set_counting(flags);
+    return C2G_OK;
+}
+
+int c2g_set_traversal(c2g_ctx* ctx, int width) {
+    if (!ctx) return C2G_ERR_INVALID;
+    if (width != 2 && width != 4) return fail(ctx, C2G_ERR_INVALID, "traversal width is 2 or 4");
+    ctx->gpu->set_sah_width(width);
     return C2G_OK;
 }
 

@@ -3,6 +3,7 @@
 #include "../../../include/c2g.h"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <limits>
 
@@ -249,6 +250,75 @@ void build_sah_tree(const HostScene& s, SahTree& out, int max_leaf) {
     b.build(0, (int)n, 1);
     out.max_depth = b.max_depth;
     out.leaf_count = b.leaves;
+}
+
+namespace {
+struct Slot {
+    float mn[3], mx[3];
+    int wide;          // >= 0: binary inner node; -1: leaf
+    int first, count;  // leaf range
+};
+
+float slot_area(const Slot& c) {
+    float d[3];
+    for (int k = 0; k < 3; k++) d[k] = std::max(0.f, c.mx[k] - c.mn[k]);
+    return d[0] * d[1] + d[1] * d[2] + d[2] * d[0];
+}
+
+void wide_children(const WideNode& w, Slot out[2]) {
+    for (int k = 0; k < 3; k++) {
+        out[0].mn[k] = w.lo0[k]; out[0].mx[k] = w.hi0[k];
+        out[1].mn[k] = w.lo1[k]; out[1].mx[k] = w.hi1[k];
+    }
+    out[0].wide = w.n0 > 0 ? -1 : w.c0; out[0].first = w.c0; out[0].count = w.n0;
+    out[1].wide = w.n1 > 0 ? -1 : w.c1; out[1].first = w.c1; out[1].count = w.n1;
+    for (int i = 0; i < 2; i++)
+        if (!(out[i].mn[0] <= out[i].mx[0])) { out[i].wide = -1; out[i].count = 0; }  // empty box: no child
+}
+
+int emit4(const std::vector<WideNode>& bin, int wide, std::vector<Node4>& out) {
+    Slot c[4];
+    int n = 0;
+    wide_children(bin[wide], c);
+    n = 2;
+    // an empty child (single-leaf tree) stays a leaf of count 0 and is dropped below
+    while (n < 4) {
+        int best = -1;
+        float best_a = -1.f;
+        for (int i = 0; i < n; i++)
+            if (c[i].wide >= 0 && slot_area(c[i]) > best_a) { best_a = slot_area(c[i]); best = i; }
+        if (best < 0) break;
+        Slot two[2];
+        wide_children(bin[c[best].wide], two);
+        c[best] = two[0];
+        c[n++] = two[1];
+    }
+    const int self = (int)out.size();
+    out.emplace_back();
+    int child[4];
+    for (int i = 0; i < 4; i++) {
+        if (i >= n || (c[i].wide < 0 && c[i].count == 0)) { child[i] = INT_MIN; continue; }
+        child[i] = c[i].wide >= 0 ? emit4(bin, c[i].wide, out) : -1 - ((c[i].first << 3) | c[i].count);
+    }
+    Node4& d = out[self];
+    const float inf = std::numeric_limits<float>::infinity();
+    for (int i = 0; i < 4; i++) {
+        const bool used = child[i] != INT_MIN;
+        d.lox[i] = used ? c[i].mn[0] : inf; d.hix[i] = used ? c[i].mx[0] : -inf;
+        d.loy[i] = used ? c[i].mn[1] : inf; d.hiy[i] = used ? c[i].mx[1] : -inf;
+        d.loz[i] = used ? c[i].mn[2] : inf; d.hiz[i] = used ? c[i].mx[2] : -inf;
+        d.child[i] = child[i];
+        d.pad[i] = 0;
+    }
+    return self;
+}
+}  // namespace
+
+void collapse_bvh4(SahTree& t) {
+    t.nodes4.clear();
+    if (t.nodes.empty()) return;
+    t.nodes4.reserve(t.nodes.size() / 2 + 1);
+    emit4(t.nodes, 0, t.nodes4);
 }
 
 void make_prims(const HostScene& s, const std::vector<int>& order, std::vector<Prim>& prims) {

@@ -26,12 +26,16 @@ struct RefTree {
 struct SahTree {
     std::vector<int> order;       // prim order (scene indices)
     std::vector<WideNode> nodes;  // root = 0
+    std::vector<Node4> nodes4;    // the same tree collapsed to four-wide nodes, root = 0
     int max_depth = 0;
     int leaf_count = 0;
 };
 
 void build_ref_tree(const HostScene& s, RefTree& out);
 void build_sah_tree(const HostScene& s, SahTree& out, int max_leaf = 4);
+// Collapse the binary SAH tree into four-wide nodes: every node absorbs the children of its
+// largest-area inner children until it holds four (Node4; boxes and leaves unchanged).
+void collapse_bvh4(SahTree& t);
 
 // Prim records for an object order (traversal order).
 void make_prims(const HostScene& s, const std::vector<int>& order, std::vector<Prim>& prims);

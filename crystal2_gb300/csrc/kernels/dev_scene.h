@@ -23,6 +23,8 @@ struct DevScene {
     int tree;                     // C2G_TREE_*
     const RefNode* ref_nodes;     // tree == REF: nodes 1..n, root 1
     const WideNode* wide_nodes;   // tree == SAH: root 0
+    const Node4* nodes4;          // tree == SAH: the same tree four-wide, root 0
+    int sah_width;                // SAH traversal variant: 2 (WideNode) or 4 (Node4)
     int anyhit_clip;              // 1: BVH semantics (object-box-clipped shadow interval)
     int closest_box;              // 1: per-object box prefilter on closest hits
     Camera cam;

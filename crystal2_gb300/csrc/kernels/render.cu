@@ -758,6 +758,11 @@ int GpuScene::upload(const HostScene& s, int tree, const RefTree* ref, const Sah
         make_prims(s, sah->order, prims);
         S.wide_nodes = upload_vec(sah->nodes, arena, sb_->owned, err, rc);
         if (rc) return rc;
+        if (!sah->nodes4.empty()) {
+            S.nodes4 = upload_vec(sah->nodes4, arena, sb_->owned, err, rc);
+            if (rc) return rc;
+        }
+        S.sah_width = S.nodes4 ? sah_width_ : 2;
     } else {
         make_prims(s, ref->order, prims);
         S.ref_nodes = upload_vec(ref->nodes, arena, sb_->owned, err, rc);
@@ -1028,6 +1033,11 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
         launches++;
     }
     return C2G_OK;
+}
+
+void GpuScene::set_sah_width(int w) {
+    sah_width_ = w == 2 ? 2 : 4;
+    if (sb_->S.tree == C2G_TREE_SAH) sb_->S.sah_width = sb_->S.nodes4 ? sah_width_ : 2;
 }
 
 int GpuScene::set_wave_counter(int sample, cudaStream_t st, DeviceArena& arena, std::string& err) {

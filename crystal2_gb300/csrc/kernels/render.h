@@ -90,6 +90,9 @@ public:
     }
     const c2g_stats& stats() const { return stats_; }
     int check_device_error(std::string& err);
+    // SAH traversal variant for the next upload and the loaded scene: 2 (binary nodes) or 4.
+    void set_sah_width(int w);
+    int sah_width() const { return sah_width_; }
 
     // ---- batched rendering (capi batch calls) ----
     // Capture one wave of p (samples per wave chosen by prepare) as a CUDA graph whose sample index
@@ -109,6 +112,7 @@ private:
                      std::string& err);
     DeviceSceneBuffers* sb_;
     int* wave_counter_ = nullptr;  // device sample index of captured wave graphs
+    int sah_width_ = 4;            // SAH traversal variant (2 or 4 children per node)
     WaveBuffers* wb_;
     int counting_ = 0;
     int present_buckets_ = 0;  // material buckets the loaded scene can produce

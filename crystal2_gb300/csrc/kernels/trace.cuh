@@ -429,6 +429,143 @@ __device__ __forceinline__ bool trace_any_sah(const DevScene& S, const RayQ& r, 
     return false;
 }
 
+// ---- four-wide SAH traversal --------------------------------------------------------------------
+// The per-axis slab distances are computed with the exact operations of box_test (subtract, then
+// multiply, each rounded) and combined with fmaxf/fminf, which ignore NaN exactly as the
+// reference's std::max/std::min argument order does; so a child is hit here exactly when box_test
+// would accept it, and the leaves reached are those of the binary traversal.
+constexpr int kStack4 = 128;
+
+__device__ __forceinline__ bool slab4(const RayQ& r, float lx, float hx, float ly, float hy, float lz, float hz,
+                                      float t0, float t1, float& tent) {
+    float ax = __fmul_rn(__fsub_rn(lx, r.o.x), r.inv.x), bx = __fmul_rn(__fsub_rn(hx, r.o.x), r.inv.x);
+    float ay = __fmul_rn(__fsub_rn(ly, r.o.y), r.inv.y), by = __fmul_rn(__fsub_rn(hy, r.o.y), r.inv.y);
+    float az = __fmul_rn(__fsub_rn(lz, r.o.z), r.inv.z), bz = __fmul_rn(__fsub_rn(hz, r.o.z), r.inv.z);
+    const float nx = r.neg[0] ? bx : ax, fx = r.neg[0] ? ax : bx;
+    const float ny = r.neg[1] ? by : ay, fy = r.neg[1] ? ay : by;
+    const float nz = r.neg[2] ? bz : az, fz = r.neg[2] ? az : bz;
+    const float tn = fmaxf(fmaxf(nx, ny), fmaxf(nz, t0));
+    const float tf = fminf(fminf(fx, fy), fminf(fz, t1));
+    tent = tn;
+    return tn <= tf;
+}
+
+__device__ __forceinline__ void cswap(float& ta, int& ca, float& tb, int& cb) {
+    if (tb < ta) {
+        float t = ta; ta = tb; tb = t;
+        int c = ca; ca = cb; cb = c;
+    }
+}
+
+template <bool COUNT>
+__device__ __forceinline__ Hit trace_closest_bvh4(const DevScene& S, const RayQ& r, float tmax, TraceCounters* cnt) {
+    Hit h{INFINITY, 0.f, 0.f, -1};
+    int stack[kStack4];
+    float stack_t[kStack4];
+    int top = 0;
+    int ref = 0, leaf = kNoRef;
+    auto pop = [&]() -> int {
+        while (top > 0) {
+            --top;
+            if (stack_t[top] <= h.t) return stack[top];
+        }
+        return kNoRef;
+    };
+    while (ref != kNoRef || leaf != kNoRef) {
+        while (ref >= 0) {
+            const float4* N = reinterpret_cast<const float4*>(S.nodes4 + ref);
+            const float4 lx = __ldg(N), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3), lz = __ldg(N + 4),
+                         hz = __ldg(N + 5);
+            const int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6));
+            if (COUNT) cnt->nodes++;
+            const float lim = smin(tmax, h.t);
+            float t[4];
+            int c[4] = {ch.x, ch.y, ch.z, ch.w};
+            if (!slab4(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, 0.f, lim, t[0])) { t[0] = INFINITY; c[0] = kNoRef; }
+            if (!slab4(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, 0.f, lim, t[1])) { t[1] = INFINITY; c[1] = kNoRef; }
+            if (!slab4(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, 0.f, lim, t[2])) { t[2] = INFINITY; c[2] = kNoRef; }
+            if (!slab4(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, 0.f, lim, t[3])) { t[3] = INFINITY; c[3] = kNoRef; }
+            // nearest first: sort the four (entry, child) pairs, push the far ones far-to-near
+            cswap(t[0], c[0], t[1], c[1]);
+            cswap(t[2], c[2], t[3], c[3]);
+            cswap(t[0], c[0], t[2], c[2]);
+            cswap(t[1], c[1], t[3], c[3]);
+            cswap(t[1], c[1], t[2], c[2]);
+            if (top + 3 > kStack4) { dev_flag_error(S.err, DEVERR_STACK); return h; }
+#pragma unroll
+            for (int k = 3; k >= 1; k--)
+                if (c[k] != kNoRef) { stack[top] = c[k]; stack_t[top] = t[k]; top++; }
+            ref = c[0] != kNoRef ? c[0] : pop();
+            if (is_leaf(ref) && leaf == kNoRef) {
+                leaf = ref;
+                ref = pop();
+            }
+            if (!__any_sync(__activemask(), leaf == kNoRef)) break;
+        }
+        while (leaf != kNoRef) {
+            int first, count;
+            leaf_range(leaf, first, count);
+            for (int i = 0; i < count; i++) {
+                if (COUNT) cnt->prims++;
+                closest_prim(S, first + i, r, tmax, h);
+            }
+            leaf = kNoRef;
+            if (is_leaf(ref)) {
+                leaf = ref;
+                ref = pop();
+            }
+        }
+    }
+    return h;
+}
+
+template <bool COUNT>
+__device__ __forceinline__ bool trace_any_bvh4(const DevScene& S, const RayQ& r, float tmin, float tmax, int ignore, TraceCounters* cnt) {
+    int stack[kStack4];
+    int top = 0;
+    int ref = 0, leaf = kNoRef;
+    while (ref != kNoRef || leaf != kNoRef) {
+        while (ref >= 0) {
+            const float4* N = reinterpret_cast<const float4*>(S.nodes4 + ref);
+            const float4 lx = __ldg(N), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3), lz = __ldg(N + 4),
+                         hz = __ldg(N + 5);
+            const int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6));
+            if (COUNT) cnt->nodes++;
+            float te;
+            const bool h0 = slab4(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, tmin, tmax, te);
+            const bool h1 = slab4(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, tmin, tmax, te);
+            const bool h2 = slab4(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, tmin, tmax, te);
+            const bool h3 = slab4(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, tmin, tmax, te);
+            if (top + 3 > kStack4) { dev_flag_error(S.err, DEVERR_STACK); return false; }
+            int next = kNoRef;
+            if (h3) next = ch.w;
+            if (h2) { if (next != kNoRef) stack[top++] = next; next = ch.z; }
+            if (h1) { if (next != kNoRef) stack[top++] = next; next = ch.y; }
+            if (h0) { if (next != kNoRef) stack[top++] = next; next = ch.x; }
+            ref = next != kNoRef ? next : (top ? stack[--top] : kNoRef);
+            if (is_leaf(ref) && leaf == kNoRef) {
+                leaf = ref;
+                ref = top ? stack[--top] : kNoRef;
+            }
+            if (!__any_sync(__activemask(), leaf == kNoRef)) break;
+        }
+        while (leaf != kNoRef) {
+            int first, count;
+            leaf_range(leaf, first, count);
+            for (int i = 0; i < count; i++) {
+                if (COUNT) cnt->prims++;
+                if (anyhit_prim(S, first + i, r, tmin, tmax, ignore)) return true;
+            }
+            leaf = kNoRef;
+            if (is_leaf(ref)) {
+                leaf = ref;
+                ref = top ? stack[--top] : kNoRef;
+            }
+        }
+    }
+    return false;
+}
+
 // Brute semantics (Brute.cpp:19-55): every object, no box tests.
 __device__ __forceinline__ Hit trace_closest_brute(const DevScene& S, const RayQ& r) {
     Hit h{INFINITY, 0.f, 0.f, -1};
@@ -444,14 +581,14 @@ __device__ __forceinline__ bool trace_any_brute(const DevScene& S, const RayQ& r
 template <bool COUNT>
 __device__ __forceinline__ Hit trace_closest(const DevScene& S, float3 o, float3 d, TraceCounters* cnt) {
     RayQ r = make_rayq(o, d);
-    if (S.tree == 1) return trace_closest_sah<COUNT>(S, r, INFINITY, cnt);
+    if (S.tree == 1) return S.sah_width == 4 ? trace_closest_bvh4<COUNT>(S, r, INFINITY, cnt) : trace_closest_sah<COUNT>(S, r, INFINITY, cnt);
     return trace_closest_ref<COUNT>(S, r, INFINITY, cnt);
 }
 
 template <bool COUNT>
 __device__ __forceinline__ bool trace_any(const DevScene& S, float3 o, float3 d, float tmin, float tmax, int ignore, TraceCounters* cnt) {
     RayQ r = make_rayq(o, d);
-    if (S.tree == 1) return trace_any_sah<COUNT>(S, r, tmin, tmax, ignore, cnt);
+    if (S.tree == 1) return S.sah_width == 4 ? trace_any_bvh4<COUNT>(S, r, tmin, tmax, ignore, cnt) : trace_any_sah<COUNT>(S, r, tmin, tmax, ignore, cnt);
     return trace_any_ref<COUNT>(S, r, tmin, tmax, ignore, cnt);
 }
 

@@ -134,6 +134,10 @@ class Context:
         """``native.COUNT_TRAVERSAL`` | ``native.COUNT_TIMING`` (0 = off)."""
         self.check(self._lib.c2g_set_counting(self._h, int(flags)))
 
+    def set_traversal(self, width: int) -> None:
+        """SAH traversal variant: 2 (binary nodes) or 4 (four-wide nodes, default)."""
+        self.check(self._lib.c2g_set_traversal(self._h, int(width)))
+
     # ---- ray queries
     def trace_rays(self, o: np.ndarray, d: np.ndarray, any_hit: bool = False, tmin=None, tmax=None, ignore=None):
         o = np.ascontiguousarray(o, np.float32)

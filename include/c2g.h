@@ -159,6 +159,9 @@ int c2g_get_stats(c2g_ctx* ctx, c2g_stats* out);
 int c2g_render_noalloc(c2g_ctx* ctx, const c2g_render_params* params, float* film_dev, void* stream);
 /* C2G_COUNT_* flags (0 = off): traversal counters (slower kernels) and per-launch timing. */
 int c2g_set_counting(c2g_ctx* ctx, int flags);
+/* SAH-tree traversal variant: 2 (binary nodes) or 4 (four-wide nodes, the default).  Both visit the
+ * same leaves; no counterpart in the reference (its BVH is binary). */
+int c2g_set_traversal(c2g_ctx* ctx, int width);
 
 /* ---- batched multi-job rendering ---------------------------------------------------------------
  * No counterpart in the reference (one scene per RayTracer).  A batch renders many jobs - each a
