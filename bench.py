@@ -360,9 +360,10 @@ def run_ours(args) -> None:
 def guided_equal_time(args) -> dict:
     """Equal-time error of the guided path tracer against the plain one on the slit-lit glossy room.
 
-    Both arms render the same frame progressively (chunks of 8 spp, one sample per wave so the
-    guide trains after every sample) for the same budget of render time (the c2g_render calls
-    only; the error is evaluated outside the timer).  relMSE = mean((I - R)^2 / (R^2 + 0.01))
+    Both arms render the same frame progressively in chunks of 8 spp, each in its fastest wave
+    schedule (plain: one wave of 8 samples; guided: waves of 2 samples, `--guided-train-steps`
+    Adam steps after each), for the same budget of render time (the c2g_render calls only; the
+    error is evaluated outside the timer).  relMSE = mean((I - R)^2 / (R^2 + 0.01))
     against a plain reference of `--guided-ref-spp` samples from a disjoint sample range.
     Reported: both errors at the budget, the time the guided arm needs to reach the plain arm's
     error (linear interpolation on its error curve), and their ratio (the target is <= 0.5)."""
@@ -391,12 +392,12 @@ def guided_equal_time(args) -> dict:
     def relmse(img):
         return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
 
-    def progressive(integ):
+    def progressive(integ, wave_spp):
         ctx.film_clear()
         s0, spent, curve = 0, 0.0, []
         while spent < args.guided_seconds:
             t = time.perf_counter()
-            ctx.render(params(integ, s0, 8))
+            ctx.render(params(integ, s0, 8, wave_spp))
             spent += time.perf_counter() - t
             s0 += 8
             curve.append((spent, s0, relmse(ctx.image().astype(np.float64))))
@@ -404,10 +405,12 @@ def guided_equal_time(args) -> dict:
 
     ctx.film_clear()
     ctx.render(params(N.INTEGRATOR_PATH, 0, 4))  # first-launch costs out of the way
-    plain = progressive(N.INTEGRATOR_PATH)
+    # each arm in its fastest wave schedule: plain 8 samples per wave; guided 2 (a training
+    # step set after every wave)
+    plain = progressive(N.INTEGRATOR_PATH, 8)
     ctx.load(cp, sp, tree=N.TREE_SAH)  # a fresh, untrained network
-    ctx.guide_config(args.guided_lr, args.guided_bsdf_fraction, 2, 1)
-    guided = progressive(N.INTEGRATOR_GUIDED)
+    ctx.guide_config(args.guided_lr, args.guided_bsdf_fraction, 2, args.guided_train_steps)
+    guided = progressive(N.INTEGRATOR_GUIDED, 2)
     target = plain[-1][2]
     reach = None
     for (t0_, _, e0), (t1_, _, e1) in zip(guided, guided[1:]):
@@ -419,9 +422,10 @@ def guided_equal_time(args) -> dict:
     loss, records, steps = ctx.guide_stats()
     return {"scene": f"slit_room {W}x{H} (524k-triangle heightfield, GGX a U(0.1,0.3), slit-lit), max depth 12",
             "reference_spp": args.guided_ref_spp, "reference_s": round(ref_s, 2), "budget_s": args.guided_seconds,
-            "plain": {"spp": plain[-1][1], "s": round(plain[-1][0], 3), "relMSE": target},
+            "plain": {"spp": plain[-1][1], "s": round(plain[-1][0], 3), "relMSE": target, "samples_per_wave": 8},
             "guided": {"spp": guided[-1][1], "s": round(guided[-1][0], 3), "relMSE": guided[-1][2],
                        "bsdf_fraction": args.guided_bsdf_fraction, "learning_rate": args.guided_lr,
+                       "train_steps_per_wave": args.guided_train_steps, "samples_per_wave": 2,
                        "adam_steps": steps, "last_batch": records, "last_loss": round(loss, 4)},
             "time_to_plain_relMSE_s": None if reach is None else round(reach, 3),
             "time_ratio": None if reach is None else round(reach / plain[-1][0], 3),
@@ -488,6 +492,7 @@ def main() -> int:
     ap.add_argument("--guided-seconds", type=float, default=4.0)
     ap.add_argument("--guided-lr", type=float, default=2e-3)
     ap.add_argument("--guided-bsdf-fraction", type=float, default=0.7)
+    ap.add_argument("--guided-train-steps", type=int, default=4)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-job measurement")
     ap.add_argument("--sah-width", type=int, default=4, choices=[2, 4], help="SAH traversal variant")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0: the library default, 2^21)")
