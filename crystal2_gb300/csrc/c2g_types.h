@@ -39,6 +39,8 @@ enum MatType : int {
     MAT_MICRO_BECKMANN = 5,
     MAT_PLASTIC_GGX = 6,  // Lambertain(kd) + MicrofacetReflection(ks) (Plastic.cpp)
     MAT_PLASTIC_BECKMANN = 7,
+    MAT_ORENNAYAR = 8,    // OrenNayarReflection (Reflections.cpp); A, B precomputed in ax, ay, sigma in ior
+    MAT_BLINNPHONG = 9,   // BlinnPhongReflection (BlinnPhongReflection.cpp); exponent K in ior
 };
 
 struct alignas(16) Material {

@@ -168,8 +168,23 @@ struct Loader {
             if (ndf == "GGX") m.type = MAT_PLASTIC_GGX;
             else if (ndf == "Beckmann") m.type = MAT_PLASTIC_BECKMANN;
             else throw SceneError(C2G_ERR_INVALID, "Cannot find NDF Type: " + ndf);
-        } else if (type == "Phong" || type == "OrenNayar") {
-            throw SceneError(C2G_ERR_UNSUPPORTED, "material type " + type + " is not supported");
+        } else if (type == "Phong") {
+            // PhongMaterial -> BlinnPhongReflection(color, K) (Material.cpp:86-99, PhongMaterial.cpp:11-19)
+            if (n.has("Kd")) throw SceneError(C2G_ERR_UNSUPPORTED, "texture-mapped Phong (Kd) is not supported");
+            m.type = MAT_BLINNPHONG;
+            color("Color");
+            m.ior = (float)n.at("K").as_int();
+        } else if (type == "OrenNayar") {
+            // OrenNayarMaterial -> OrenNayarReflection(color, sigma) (Material.cpp:100-121); the
+            // constructor's A and B (Reflections.cpp:20-26) in float, as the reference computes them
+            if (n.has("Kd")) throw SceneError(C2G_ERR_UNSUPPORTED, "Not implemented");
+            m.type = MAT_ORENNAYAR;
+            color("Color");
+            const float sigma = (float)n.at("Sigma").as_float();
+            const float s2 = sigma * sigma;
+            m.ior = sigma;
+            m.ax = 1.f - s2 / (2 * (s2 + 0.33f));
+            m.ay = (0.45f * s2) / (s2 + 0.09f);
         } else {
             throw SceneError(C2G_ERR_INVALID, "Invalid material name");
         }

@@ -39,6 +39,8 @@ __device__ __forceinline__ int material_flags(int mtype) {
         case MAT_MICRO_BECKMANN: return BXDF_REFLECTION | BXDF_GLOSSY;
         case MAT_PLASTIC_GGX:
         case MAT_PLASTIC_BECKMANN: return BXDF_REFLECTION | BXDF_GLOSSY;
+        case MAT_ORENNAYAR: return BXDF_DIFFUSE | BXDF_REFLECTION;
+        case MAT_BLINNPHONG: return BXDF_GLOSSY | BXDF_REFLECTION;
     }
     return 0;
 }
@@ -54,8 +56,10 @@ __device__ __forceinline__ BxDF make_bxdf(const Material& m, bool front_face) {
     // Glass / Micro swap the IORs on back faces (Glass.cpp:19-20, MicrofacetMaterial.cpp:20-21);
     // Mirror uses 1, 1 (MirrorMaterial.cpp:11-13).
     b.etaA = 1.f;
-    b.etaB = (m.type == MAT_MIRROR || m.type == MAT_DIFFUSE) ? 1.f : m.ior;
-    if (!front_face && m.type != MAT_MIRROR && m.type != MAT_DIFFUSE) { float t = b.etaA; b.etaA = b.etaB; b.etaB = t; }
+    const bool dielectric = m.type != MAT_MIRROR && m.type != MAT_DIFFUSE && m.type != MAT_ORENNAYAR && m.type != MAT_BLINNPHONG;
+    b.etaB = dielectric ? m.ior : 1.f;
+    if (!front_face && dielectric) { float t = b.etaA; b.etaA = b.etaB; b.etaB = t; }
+    if (m.type == MAT_BLINNPHONG) b.ax = m.ior;  // the exponent K
     return b;
 }
 
@@ -243,6 +247,44 @@ __device__ __forceinline__ float3 fb_f(const BxDF& b, float3 wo, float3 wi) {
     return diffuse + s * schlick;
 }
 
+// ---- Oren-Nayar (BSDFs/Reflections.cpp:7-66); A, B in ax, ay -----------------------------
+__device__ __forceinline__ float3 on_f(const BxDF& b, float3 wo, float3 wi) {
+    const float sinO = sqrtf(fmaxf(0.f, 1.f - wo.y * wo.y)), sinI = sqrtf(fmaxf(0.f, 1.f - wi.y * wi.y));
+    float sinA, tanB;
+    if (wo.y < wi.y) { sinA = sinI; tanB = sinO / wo.y; }
+    else { sinA = sinO; tanB = sinI / wi.y; }
+    float dcos = 0.f;
+    if (sinI > 1e-5f && sinO > 1e-5f) {
+        const float2 dI = cos_sin_phi(wi, sinI), dO = cos_sin_phi(wo, sinO);
+        dcos = fmaxf(0.f, dI.x * dO.x + dI.y * dO.y);
+    }
+    return b.R / kPiF * (b.ax + b.ay * (dcos * sinA * tanB));
+}
+
+// ---- Blinn-Phong (BSDFs/BlinnPhongReflection.cpp:14-58); exponent K in ax -------------------
+// The reference raises float to int powers with std::pow, i.e. in double: so does this.
+__device__ __forceinline__ float bp_pdf(const BxDF& b, float3 wo, float3 wi) {
+    const float3 wh = normalize(wo + wi);
+    const float k = b.ax;
+    return (float)((double)((k + 2.f) / kTwoPiF) * pow((double)fmaxf(0.f, wh.y), (double)(k + 1.f)));
+}
+__device__ __forceinline__ float3 bp_f(const BxDF& b, float3 wo, float3 wi) {
+    const float3 wh = normalize(wo + wi);
+    const float k = b.ax;
+    const float s = (float)pow((double)fmaxf(0.f, wh.y), (double)k) * (k + 2.f) / kTwoPiF;
+    return b.R * s / (4.f * fmaxf(0.f, wi.y) * fmaxf(0.f, wo.y));
+}
+// A rejected half vector is redrawn.  The reference redraws from a static std::mt19937 shared by
+// all render threads (BlinnPhongReflection.cpp:33-56), which no other run can reproduce; here the
+// next pair is a hash of the rejected pair and the attempt number, and the loop stops after
+// kPhongAttempts draws (the sample then fails) instead of looping without bound.
+constexpr int kPhongAttempts = 64;
+__device__ __forceinline__ float2 phong_redraw(float2 u, int attempt) {
+    const uint32_t h = hash32(__float_as_uint(u.x) ^ hash32(__float_as_uint(u.y) + 0x9E3779B9u * (uint32_t)(attempt + 1)));
+    const uint32_t g = hash32(h ^ 0x85EBCA6Bu);
+    return make_float2((float)(h >> 8) * 0x1p-24f, (float)(g >> 8) * 0x1p-24f);
+}
+
 // ---- per-BxDF dispatch (local frame) ------------------------------------------------------
 __device__ __forceinline__ float3 bxdf_f(const BxDF& b, float3 wo, float3 wi) {
     switch (b.mtype) {
@@ -252,6 +294,8 @@ __device__ __forceinline__ float3 bxdf_f(const BxDF& b, float3 wo, float3 wi) {
         case MAT_GLASS_ROUGH: return (wo.y * wi.y < 0) ? mf_trans_f(b, wo, wi) : mf_refl_f(b, wo, wi);
         case MAT_PLASTIC_GGX:
         case MAT_PLASTIC_BECKMANN: return fb_f(b, wo, wi);
+        case MAT_ORENNAYAR: return on_f(b, wo, wi);
+        case MAT_BLINNPHONG: return bp_f(b, wo, wi);
     }
     return f3(0.f, 0.f, 0.f);  // specular BxDFs
 }
@@ -263,6 +307,8 @@ __device__ __forceinline__ float bxdf_pdf(const BxDF& b, float3 wo, float3 wi) {
         case MAT_GLASS_ROUGH: return (wo.y * wi.y < 0) ? mf_trans_pdf(b, wo, wi) : mf_refl_pdf(b, wo, wi);
         case MAT_PLASTIC_GGX:
         case MAT_PLASTIC_BECKMANN: return fb_pdf(b, wo, wi);
+        case MAT_ORENNAYAR: return fmaxf(0.f, wi.y) / kPiF;
+        case MAT_BLINNPHONG: return bp_pdf(b, wo, wi);
     }
     return 0.f;
 }
@@ -313,6 +359,8 @@ __device__ __forceinline__ float3 bxdf_f_pdf(const BxDF& b, float3 wo, float3 wi
         case MAT_GLASS_ROUGH: return (wo.y * wi.y < 0) ? mf_trans_f_pdf(b, wo, wi, pdf) : mf_refl_f_pdf(b, wo, wi, pdf);
         case MAT_PLASTIC_GGX:
         case MAT_PLASTIC_BECKMANN: return fb_f_pdf(b, wo, wi, pdf);
+        case MAT_ORENNAYAR: pdf = fmaxf(0.f, wi.y) / kPiF; return on_f(b, wo, wi);
+        case MAT_BLINNPHONG: pdf = bp_pdf(b, wo, wi); return bp_f(b, wo, wi);
     }
     pdf = 0.f;
     return f3(0.f, 0.f, 0.f);
@@ -406,6 +454,25 @@ __device__ __forceinline__ float3 bxdf_sample(const BxDF& b, float2 u, float3 wo
             }
             pdf = fb_pdf(b, wo, wi);
             return fb_f(b, wo, wi);
+        }
+        case MAT_ORENNAYAR: {
+            wi = cosine_hemisphere(u, pdf);
+            return on_f(b, wo, wi);
+        }
+        case MAT_BLINNPHONG: {
+            float2 s = u;
+            for (int attempt = 0; attempt < kPhongAttempts; attempt++) {
+                const float cosT = (float)pow((double)s.x, 1.0 / (double)(b.ax + 2.f));
+                const float phi = kTwoPiF * s.y;
+                const float3 N = unit_from_cos(cosT, phi);
+                if (dot(N, wo) < 0.f) { s = phong_redraw(s, attempt); continue; }
+                const float3 w = reflect(-wo, N);
+                if (w.y < 0.f) { s = phong_redraw(s, attempt); continue; }
+                wi = w;
+                pdf = bp_pdf(b, wo, wi);
+                return bp_f(b, wo, wi);
+            }
+            return zero;
         }
     }
     return zero;

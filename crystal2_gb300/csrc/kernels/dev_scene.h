@@ -35,10 +35,10 @@ struct DevScene {
     int* err;                     // device error word (C2G_DEVERR_*)
 };
 
-// Shading buckets: 0..7 = MatType of the hit's material, 8 = no material, 9 = miss.
-constexpr int kBuckets = 10;
-constexpr int kBucketNone = 8;
-constexpr int kBucketMiss = 9;
+// Shading buckets: 0..9 = MatType of the hit's material, 10 = no material, 11 = miss.
+constexpr int kBuckets = 12;
+constexpr int kBucketNone = 10;
+constexpr int kBucketMiss = 11;
 
 enum : int {
     DEVERR_STACK = 1,             // traversal stack overflow

@@ -44,7 +44,7 @@ __device__ __forceinline__ float luminance(float3 c) { return 0.2126f * c.x + 0.
 // the exact density of the directions it draws (the mixture pdf needs it at guide-drawn directions).
 __host__ __device__ constexpr bool bucket_guided(int b) {
     return b == MAT_DIFFUSE || b == MAT_MICRO_GGX || b == MAT_MICRO_BECKMANN || b == MAT_PLASTIC_GGX ||
-           b == MAT_PLASTIC_BECKMANN;
+           b == MAT_PLASTIC_BECKMANN || b == MAT_ORENNAYAR;
 }
 
 __device__ __forceinline__ void stage_forward_weights(const GuideNet& net, __nv_bfloat16* wts) {

@@ -94,7 +94,7 @@ struct WaveBuffers {
     int* sh_list = nullptr;
     int* mis_list = nullptr;
     int* bucket_list = nullptr;  // kBuckets lists of P slots
-    int* counters = nullptr;  // [0],[1] path queues, [2] shadow, [3] mis, [8..18) material buckets
+    int* counters = nullptr;  // [0],[1] path queues, [2] shadow, [3] mis, [8..20) material buckets
     std::vector<void*> owned;
 };
 
@@ -716,8 +716,8 @@ void launch_shade(int bk, int grid, cudaStream_t st, const DevScene& S, const Wa
     if (guided) {
         switch (bk) {
 #define C2G_SHADE_G(B) case B: k_shade<B, true><<<grid, 128, 0, st>>>(S, a, cur, hits, bcnt, blist, cap, so, gv); return;
-            // guided buckets: diffuse, GGX/Beckmann reflection, plastic (exact sampling densities)
-            C2G_SHADE_G(0) C2G_SHADE_G(4) C2G_SHADE_G(5) C2G_SHADE_G(6) C2G_SHADE_G(7)
+            // guided buckets: diffuse, GGX/Beckmann reflection, plastic, Oren-Nayar (exact sampling densities)
+            C2G_SHADE_G(0) C2G_SHADE_G(4) C2G_SHADE_G(5) C2G_SHADE_G(6) C2G_SHADE_G(7) C2G_SHADE_G(8)
 #undef C2G_SHADE_G
         }
     }
@@ -725,6 +725,7 @@ void launch_shade(int bk, int grid, cudaStream_t st, const DevScene& S, const Wa
 #define C2G_SHADE_CASE(B) case B: k_shade<B, false><<<grid, 128, 0, st>>>(S, a, cur, hits, bcnt, blist, cap, so, gv); break;
         C2G_SHADE_CASE(0) C2G_SHADE_CASE(1) C2G_SHADE_CASE(2) C2G_SHADE_CASE(3) C2G_SHADE_CASE(4)
         C2G_SHADE_CASE(5) C2G_SHADE_CASE(6) C2G_SHADE_CASE(7) C2G_SHADE_CASE(8) C2G_SHADE_CASE(9)
+        C2G_SHADE_CASE(10) C2G_SHADE_CASE(11)
 #undef C2G_SHADE_CASE
     }
 }

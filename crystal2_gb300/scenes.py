@@ -114,6 +114,14 @@ def glass(c=(1, 1, 1), rough=(0.1, 0.1), ior=1.5) -> dict:
     return {"Type": "Glass", "Color": _v(c), "Roughness": _v(rough), "IOR": _f(ior)}
 
 
+def oren_nayar(c, sigma) -> dict:
+    return {"Type": "OrenNayar", "Color": _v(c), "Sigma": _f(sigma)}
+
+
+def phong(c, k: int) -> dict:
+    return {"Type": "Phong", "Color": _v(c), "K": int(k)}
+
+
 def plastic(kd, ks, rough, ndf="GGX") -> dict:
     return {"Type": "Plastic", "Kd": _v(kd), "Ks": _v(ks), "Roughness": _v(rough), "NDF": ndf}
 
@@ -223,6 +231,28 @@ def batch_jobs(out_dir: str, n_jobs: int = 64, seed: int = 4, n_grid: int = 8, s
             cp, sp = many_material(d, width=side, height=side, spp=spp, seed=2000 + j, n_grid=n_grid, subdiv=subdiv)
         jobs.append((cp, sp, spp, guided))
     return jobs
+
+
+def brdf_box(out_dir: str, width=48, height=48, spp=16, depth=6, accel="BVH", threads=8) -> tuple[str, str]:
+    """Box with Oren-Nayar walls (sigma 0.3 / 0.7) and Blinn-Phong spheres (K 8 and 60)."""
+    d = os.path.abspath(out_dir)
+    os.makedirs(d, exist_ok=True)
+    w = _box_walls(d)
+    lp = os.path.join(d, "light.obj")
+    h, ly = 0.3, 1.999
+    quad_obj(lp, [(-h, ly, -h), (-h, ly, h), (h, ly, h), (h, ly, -h)], (0, -1, 0))
+    objs = [
+        mesh(w["floor"], oren_nayar((0.7, 0.7, 0.7), 0.3)),
+        mesh(w["ceiling"], oren_nayar((0.75, 0.75, 0.75), 0.7)),
+        mesh(w["back"], oren_nayar((0.6, 0.6, 0.7), 0.5)),
+        mesh(w["xpos"], oren_nayar((0.65, 0.1, 0.1), 0.7)),
+        mesh(w["xneg"], diffuse((0.1, 0.5, 0.15))),
+        mesh(lp, diffuse((0, 0, 0)), area_light=(14, 14, 14)),
+        sphere((-0.45, 0.35, 0.2), 0.35, phong((0.8, 0.8, 0.8), 8)),
+        sphere((0.45, 0.3, -0.25), 0.3, phong((0.9, 0.7, 0.4), 60)),
+    ]
+    cfg = config_json(width, height, spp, depth, accel=accel, threads=threads)
+    return write_scene(d, cfg, camera((0, 1, -3.8), (0, 1, 0), 40), objs, "brdf_box")
 
 
 def material_box(out_dir: str, width=64, height=64, spp=16, depth=8, accel="BVH", threads=8) -> tuple[str, str]:

@@ -296,6 +296,10 @@ def material_json(kind: str, params) -> str:
         m = {"Type": "Glass", "Color": c, "Roughness": [ax, ay], "IOR": ior}
     elif kind.startswith("Micro"):
         m = {"Type": "Micro", "Color": c, "Roughness": [ax, ay], "IOR": ior, "NDF": "GGX" if kind.endswith("GGX") else "Beckmann"}
+    elif kind == "OrenNayar":
+        m = {"Type": "OrenNayar", "Color": c, "Sigma": ior}
+    elif kind == "Phong":
+        m = {"Type": "Phong", "Color": c, "K": int(ior)}
     else:
         m = {"Type": "Plastic", "Kd": c, "Ks": ks, "Roughness": [ax, ay], "NDF": "GGX" if kind.endswith("GGX") else "Beckmann"}
     return json.dumps(m)

@@ -258,7 +258,7 @@ static V3 vec3(const JNode& n) { return V3((float)n.a.at(0)->F(), (float)n.a.at(
 
 // ---------------------------------------------------------------- scene
 enum { TRI = 0, SPH = 1, DSK = 2 };
-enum { M_DIFF, M_MIRROR, M_GLASS_R, M_GLASS_S, M_MICRO_GGX, M_MICRO_BECK, M_PLAST_GGX, M_PLAST_BECK };
+enum { M_DIFF, M_MIRROR, M_GLASS_R, M_GLASS_S, M_MICRO_GGX, M_MICRO_BECK, M_PLAST_GGX, M_PLAST_BECK, M_OREN, M_PHONG };
 struct Mat { int type; V3 R, S; float ax = 0, ay = 0, ior = 1; };
 struct Tri { V3 p[3], n[3]; V3 dpdu; };
 struct Quad { V3 pos; float r; M3 l2w, w2l; };
@@ -344,6 +344,14 @@ static int add_mat(Scene& s, const JNode& n) {
         m.R = vec3(n.m("Kd")); m.S = vec3(n.m("Ks"));
         m.ax = (float)n.m("Roughness").a[0]->F(); m.ay = (float)n.m("Roughness").a[1]->F();
         m.type = n.m("NDF").s == "GGX" ? M_PLAST_GGX : M_PLAST_BECK;
+    } else if (t == "OrenNayar") {  // Material.cpp:100-121 -> OrenNayarReflection(color, sigma)
+        m.type = M_OREN;
+        m.R = vec3(n.m("Color"));
+        m.ior = (float)n.m("Sigma").F();
+    } else if (t == "Phong") {      // Material.cpp:86-99 -> BlinnPhongReflection(color, K)
+        m.type = M_PHONG;
+        m.R = vec3(n.m("Color"));
+        m.ior = (float)n.m("K").I();
     } else throw std::runtime_error("material " + t + " not restated");
     s.mats.push_back(m);
     return (int)s.mats.size() - 1;
@@ -793,6 +801,7 @@ struct BxDF { int mt, flags; V3 R, S; float ax, ay, etaA, etaB; };
 static int mflags(int mt) {
     switch (mt) {
         case M_DIFF: return BD | BR;
+        case M_OREN: return BD | BR;
         case M_MIRROR: return BS | BR;
         case M_GLASS_R: return BT | BR | BG;
         case M_GLASS_S: return BT | BR | BS;
@@ -801,7 +810,17 @@ static int mflags(int mt) {
 }
 static BxDF make_bxdf(const Mat& m, bool front) {
     BxDF b{m.type, mflags(m.type), m.R, m.S, m.ax, m.ay, 1.f, 1.f};
-    if (m.type != M_MIRROR && m.type != M_DIFF) { b.etaB = m.ior; if (!front) std::swap(b.etaA, b.etaB); }
+    if (m.type == M_OREN) {
+        // OrenNayarReflection constructor (Reflections.cpp:20-26): A, B from sigma
+        float s2 = m.ior * m.ior;
+        b.ax = 1.f - s2 / (2 * (s2 + 0.33f));
+        b.ay = (0.45f * s2) / (s2 + 0.09f);
+    } else if (m.type == M_PHONG) {
+        b.ax = m.ior;  // exponent K
+    } else if (m.type != M_MIRROR && m.type != M_DIFF) {
+        b.etaB = m.ior;
+        if (!front) std::swap(b.etaA, b.etaB);
+    }
     return b;
 }
 static float sqf(float x) { return x * x; }
@@ -885,6 +904,44 @@ static V3 sample_wh(const BxDF& b, float ux, float uy) {
     return ucos(1.f / std::sqrt(1.f + t2), phi);
 }
 static V3 reflectv(V3 I, V3 N) { return I - N * dot(N, I) * 2.f; }
+// OrenNayarReflection::DistributionFunction (Reflections.cpp:36-58)
+static V3 onf(const BxDF& b, V3 o, V3 i) {
+    float sO = std::sqrt(std::max(0.f, 1.f - o.y * o.y)), sI = std::sqrt(std::max(0.f, 1.f - i.y * i.y));
+    float sa, tb;
+    if (o.y < i.y) { sa = sI; tb = sO / o.y; }
+    else { sa = sO; tb = sI / i.y; }
+    float dc = 0.f;
+    if (sI > 1e-5f && sO > 1e-5f) {
+        float ci, si_, co, so;
+        csphi(i, sI, ci, si_);
+        csphi(o, sO, co, so);
+        dc = std::max(0.f, ci * co + si_ * so);
+    }
+    return b.R / PI * (b.ax + b.ay * (dc * sa * tb));
+}
+// BlinnPhongReflection::Pdf / DistributionFunction (BlinnPhongReflection.cpp:14-27); std::pow of a
+// float and an int is evaluated in double
+static float bppdf(const BxDF& b, V3 o, V3 i) {
+    V3 wh = normalize(o + i);
+    return (float)((double)((b.ax + 2.f) / TWO_PI) * std::pow((double)std::max(0.f, wh.y), (double)(b.ax + 1.f)));
+}
+static V3 bpf(const BxDF& b, V3 o, V3 i) {
+    V3 wh = normalize(o + i);
+    float s = (float)std::pow((double)std::max(0.f, wh.y), (double)b.ax) * (b.ax + 2.f) / TWO_PI;
+    return b.R * s / (4.f * std::max(0.f, i.y) * std::max(0.f, o.y));
+}
+// Redraw after a rejected half vector: a hash of the rejected pair and the attempt (the reference
+// redraws from a shared static std::mt19937, BlinnPhongReflection.cpp:33-56); at most 64 draws.
+static uint32_t bph(uint32_t x) { x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16; return x; }
+static void phong_redraw(float& ux, float& uy, int attempt) {
+    uint32_t bx, by;
+    std::memcpy(&bx, &ux, 4);
+    std::memcpy(&by, &uy, 4);
+    uint32_t h = bph(bx ^ bph(by + 0x9E3779B9u * (uint32_t)(attempt + 1)));
+    uint32_t g = bph(h ^ 0x85EBCA6Bu);
+    ux = (float)(h >> 8) * 0x1p-24f;
+    uy = (float)(g >> 8) * 0x1p-24f;
+}
 static bool refractv(V3 wo, V3 wh, float eta, V3& wt) {
     float co = std::min(std::max(dot(wo, wh), -1.f), 1.f), s2o = std::max(0.f, 1.f - co * co), s2i = eta * eta * s2o;
     if (s2i > 1.f) return false;
@@ -930,6 +987,8 @@ static V3 bxf(const BxDF& b, V3 o, V3 i) {
         case M_MICRO_GGX: case M_MICRO_BECK: return rf(b, o, i);
         case M_GLASS_R: return o.y * i.y < 0 ? tf(b, o, i) : rf(b, o, i);
         case M_PLAST_GGX: case M_PLAST_BECK: return fbf(b, o, i);
+        case M_OREN: return onf(b, o, i);
+        case M_PHONG: return bpf(b, o, i);
     }
     return V3();
 }
@@ -939,6 +998,8 @@ static float bxpdf(const BxDF& b, V3 o, V3 i) {
         case M_MICRO_GGX: case M_MICRO_BECK: return rpdf(b, o, i);
         case M_GLASS_R: return o.y * i.y < 0 ? tpdf(b, o, i) : rpdf(b, o, i);
         case M_PLAST_GGX: case M_PLAST_BECK: return fbpdf(b, o, i);
+        case M_OREN: return std::max(0.f, i.y) / PI;
+        case M_PHONG: return bppdf(b, o, i);
     }
     return 0.f;
 }
@@ -982,6 +1043,20 @@ static V3 bxsample(const BxDF& b, float ux, float uy, V3 o, V3& i, float& pdf, i
             }
             pdf = fbpdf(b, o, i);
             return fbf(b, o, i);
+        }
+        case M_OREN: i = cosine_hemi(ux, uy, pdf); return onf(b, o, i);
+        case M_PHONG: {
+            for (int attempt = 0; attempt < 64; attempt++) {
+                float ct = (float)std::pow((double)ux, 1.0 / (double)(b.ax + 2.f));
+                V3 N = ucos(ct, TWO_PI * uy);
+                if (dot(N, o) < 0) { phong_redraw(ux, uy, attempt); continue; }
+                V3 w = reflectv(-o, N);
+                if (w.y < 0) { phong_redraw(ux, uy, attempt); continue; }
+                i = w;
+                pdf = bppdf(b, o, i);
+                return bpf(b, o, i);
+            }
+            return V3();
         }
     }
     return V3();
@@ -1351,6 +1426,8 @@ int orc_bsdf(const char* kind, const float* params, int front, const float* fram
     else if (k == "MicroBeckmann") m.type = M_MICRO_BECK;
     else if (k == "PlasticGGX") m.type = M_PLAST_GGX;
     else if (k == "PlasticBeckmann") m.type = M_PLAST_BECK;
+    else if (k == "OrenNayar") m.type = M_OREN;
+    else if (k == "Phong") m.type = M_PHONG;
     else return -1;
     m.R = V3(params[0], params[1], params[2]); m.S = V3(params[3], params[4], params[5]);
     m.ax = params[6]; m.ay = params[7]; m.ior = params[8];

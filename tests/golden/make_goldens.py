@@ -15,6 +15,7 @@ Fixtures:
   isect_<scene>.npz  Scene::Intersect (object, t) and Scene::IntersectTest results for seeded rays
   bsdf.npz       BSDF f/pdf and sampled (f, wi, pdf, type) for every material kind
   render_<scene>.npz per-sample radiance of a pixel subset and the per-pixel mean image
+                 (cornell, material_box, spheres, direct_cornell, brdf_box: Oren-Nayar + Blinn-Phong)
 """
 from __future__ import annotations
 
@@ -85,6 +86,8 @@ BSDF_PARAMS = {
     "MicroGGXAniso": [0.9, 0.7, 0.5, 0, 0, 0, 0.08, 0.45, 1.5],
     "MicroBeckmann": [0.8, 0.8, 0.8, 0, 0, 0, 0.25, 0.25, 1.5],
     "PlasticGGX": [0.5, 0.4, 0.3, 0.2, 0.2, 0.2, 0.3, 0.3, 1],
+    "OrenNayar": [0.7, 0.6, 0.5, 0, 0, 0, 0, 0, 0.35],   # sigma in the last slot
+    "Phong": [0.8, 0.7, 0.6, 0, 0, 0, 0, 0, 20],         # exponent K in the last slot
 }
 
 
@@ -146,6 +149,16 @@ def main() -> None:
     px = np.arange(0, r.W, 3)[:16].astype(np.int32)
     py = ((np.arange(px.shape[0]) * 5) % r.H).astype(np.int32)
     np.savez_compressed(os.path.join(out, "render_direct_cornell.npz"), mean=(s / r.spp).astype(np.float32),
+                        m2=(q / r.spp).astype(np.float32), spp=r.spp, px=px, py=py, samples=r.render_samples(px, py))
+    r.close()
+    # Oren-Nayar and Blinn-Phong materials in a box (Reflections.cpp, BlinnPhongReflection.cpp)
+    d = os.path.join(work, "brdf_box")
+    cp, sp = scenes.brdf_box(d)
+    r = B.ref_open(cp, sp)
+    s, q, _ = r.render_region(0, 0, r.W, r.H)
+    px = np.arange(0, r.W, 3)[:16].astype(np.int32)
+    py = ((np.arange(px.shape[0]) * 5) % r.H).astype(np.int32)
+    np.savez_compressed(os.path.join(out, "render_brdf_box.npz"), mean=(s / r.spp).astype(np.float32),
                         m2=(q / r.spp).astype(np.float32), spp=r.spp, px=px, py=py, samples=r.render_samples(px, py))
     r.close()
     # BSDFs

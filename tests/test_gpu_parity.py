@@ -350,3 +350,28 @@ def test_direct_lighting_integrator(tmp_path):
     z = np.load(os.path.join(GOLDEN, "render_direct_cornell.npz"))
     gm = G.mean(0)
     np.testing.assert_allclose(gm.mean(), z["mean"].mean(), rtol=2e-3)
+
+
+def test_oren_nayar_blinn_phong_vs_reference_and_oracle(tmp_path):
+    """Oren-Nayar walls and Blinn-Phong spheres: image means within 3 standard errors of the
+    reference's golden render, and per-sample radiance against the oracle (bit-identical except
+    for CUDA vs libm rounding redirecting a path)."""
+    cp, sp = scenes.brdf_box(str(tmp_path / "b"))
+    ctx = _ctx(cp, sp)
+    p = ctx.render_params()
+    ctx.render(p)
+    s, w = ctx.film()
+    m2 = ctx.film_m2()
+    z = np.load(os.path.join(GOLDEN, "render_brdf_box.npz"))
+    gm = s / w[..., None]
+    gv = np.maximum(m2 / w[..., None] - gm ** 2, 0) / p.spp
+    rv = np.maximum(z["m2"] - z["mean"] ** 2, 0) / int(z["spp"])
+    zt = (gm - z["mean"]) / np.sqrt(gv + rv + 1e-12)
+    assert (np.abs(zt) > 3).mean() <= 0.01
+    assert abs(gm.mean() - z["mean"].mean()) <= 3 * np.sqrt((gv + rv).sum()) / gm.size + 1e-6
+    o = B.oracle_open(cp, sp)
+    ref = o.render_samples(z["px"], z["py"])
+    ctx_ref = _ctx(cp, sp, N.TREE_REF_EQUAL_COUNT)  # the reference tree: no near-tie reordering
+    gs = _per_sample(ctx_ref, p.spp)[:, z["py"], z["px"]].transpose(1, 0, 2)
+    close = np.abs(gs - ref).max(-1) <= 1e-6 * (1 + np.abs(ref).max(-1))
+    assert close.mean() >= 0.85

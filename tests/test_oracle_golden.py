@@ -53,6 +53,20 @@ def test_intersections_match_reference(name, tmp_path):
     assert np.array_equal(occ, z["occ"])
 
 
+def _phong_first_draw_accepted(frame, wo, u3, k, margin=1e-3):
+    """Rows whose first Blinn-Phong half vector is clearly accepted (BlinnPhongReflection.cpp:36-50)."""
+    N, T, Bv = (frame[i:i + 3].astype(np.float64) for i in (0, 3, 6))
+    w = wo.astype(np.float64)
+    wl = np.stack([w @ T, w @ N, w @ Bv], 1)
+    ct = u3[:, 1].astype(np.float64) ** (1.0 / (k + 2))
+    phi = 2 * np.pi * u3[:, 2].astype(np.float64)
+    r = np.sqrt(np.maximum(0.0, 1 - ct * ct))
+    h = np.stack([r * np.cos(phi), ct, -r * np.sin(phi)], 1)
+    d = np.einsum("ij,ij->i", h, wl)
+    refl_y = -wl[:, 1] + 2 * d * h[:, 1]
+    return (d > margin) & (refl_y > margin)
+
+
 def test_bsdf_matches_reference():
     z = np.load(os.path.join(GOLDEN, "bsdf.npz"))
     for k, (name, params) in enumerate(BSDF_PARAMS.items()):
@@ -62,10 +76,16 @@ def test_bsdf_matches_reference():
                 fe, pe, fs, ws, ps, ts = B.bsdf_eval("orc", bsdf_kind(name), params, front, frame, wo, wi, u3, flags)
                 key = f"{name}_{front}_{flags}"
                 # identical float arithmetic except libm transcendentals: tight relative tolerance
-                for got, want in ((fe, z[key + "_fe"]), (pe, z[key + "_pe"]), (fs, z[key + "_fs"])):
+                for got, want in ((fe, z[key + "_fe"]), (pe, z[key + "_pe"])):
                     np.testing.assert_allclose(got, want, rtol=2e-5, atol=1e-6, err_msg=key)
+                first = _phong_first_draw_accepted(frame, wo, u3, params[8]) if name == "Phong" else slice(None)
+                np.testing.assert_allclose(fs[first], z[key + "_fs"][first], rtol=2e-5, atol=1e-6, err_msg=key)
                 # direction, pdf and type are defined only where the sample succeeded (f != 0)
                 ok = np.any(z[key + "_fs"] != 0, axis=1)
+                if name == "Phong":
+                    # a rejected Blinn-Phong half vector is redrawn from the reference's shared
+                    # std::mt19937 but from a hash here: compare first-draw acceptances only
+                    ok &= _phong_first_draw_accepted(frame, wo, u3, params[8])
                 np.testing.assert_allclose(ws[ok], z[key + "_ws"][ok], rtol=2e-5, atol=1e-6, err_msg=key)
                 np.testing.assert_allclose(ps[ok], z[key + "_ps"][ok], rtol=2e-5, atol=1e-6, err_msg=key)
                 assert np.array_equal(ts[ok], z[key + "_ts"][ok]), key
@@ -111,3 +131,20 @@ def test_direct_lighting_matches_reference(tmp_path):
     assert np.array_equal(got.view(np.uint32), z["samples"].view(np.uint32))
     s, q, _ = o.render_region(0, 0, o.W, o.H)
     np.testing.assert_allclose(s / o.spp, z["mean"], rtol=1e-5, atol=1e-6)
+
+
+def test_brdf_box_render_matches_reference(tmp_path):
+    """Oren-Nayar and Blinn-Phong materials (Reflections.cpp, BlinnPhongReflection.cpp): per-pixel
+    means within 3 standard errors of the reference and most samples bit-identical (a rejected
+    Blinn-Phong half vector is redrawn from a hash here, from a shared std::mt19937 there)."""
+    cp, sp = scenes.brdf_box(str(tmp_path / "b"))
+    o = B.oracle_open(cp, sp)
+    z = np.load(os.path.join(GOLDEN, "render_brdf_box.npz"))
+    s, q, _ = o.render_region(0, 0, o.W, o.H)
+    mean = s / o.spp
+    var = np.maximum(z["m2"] - z["mean"] ** 2, 0) / o.spp + np.maximum(q / o.spp - mean ** 2, 0) / o.spp
+    assert abs((mean - z["mean"]).mean()) <= 3 * np.sqrt(var.sum()) / mean.size + 1e-6
+    zt = (mean - z["mean"]) / np.sqrt(var + 1e-12)
+    assert np.mean(np.abs(zt) > 3) <= 0.01
+    got = o.render_samples(z["px"], z["py"])
+    assert np.mean(got.view(np.uint32) == z["samples"].view(np.uint32)) >= 0.9
