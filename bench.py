@@ -331,6 +331,12 @@ def run_ours(args) -> None:
             guided = guided_equal_time(args)
         except Exception as e:  # reported beside the headline, never required for it
             guided = {"unavailable": str(e)[:200]}
+    rays = None
+    if rank == 0 and world == 1 and not args.no_rays:
+        try:
+            rays = ray_microbench(args)
+        except Exception as e:  # reported beside the headline, never required for it
+            rays = {"unavailable": str(e)[:200]}
     batch = None
     if rank == 0 and world == 1 and not args.no_batch:
         try:
@@ -351,7 +357,7 @@ def run_ours(args) -> None:
                         "d2h_bytes_per_step": int(p.width * p.height * 16)},
                 "gpu_launches": int(launches), "roofline": roof, "kernel_share": share,
                 "traversal_per_step": {k: {"rays": v[0], "nodes": v[1], "prims": v[2]} for k, v in counts.items()},
-                "clocks": clk, "cpu_baseline": cpu, "guided_equal_time": guided, "batch": batch}
+                "clocks": clk, "cpu_baseline": cpu, "guided_equal_time": guided, "batch": batch, "ray_microbench": rays}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -476,6 +482,63 @@ def batch_run(args) -> dict:
     return out
 
 
+def ray_microbench(args) -> dict:
+    """Ray-intersection microbench: 1M-triangle soup (centroids U[0,1]^3, vertices +- 0.005) in the
+    SAH tree, 16M rays (8M pinhole primaries of a 4096^2 image of the cube, 8M random origins and
+    directions), closest hit and then any hit with tmax ~ U(0, 2 t_closest); device-resident rays
+    through c2g_trace_rays_dev, CUDA-event timed over `--steps` launches after 3 warm-up launches."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+    from crystal2_gb300 import Context, scenes
+    from crystal2_gb300 import _native as N
+
+    d = tempfile.mkdtemp(prefix="c2g_rays_")
+    cp, sp = scenes.tri_soup(d, n_tris=1 << 20)
+    ctx = Context(0)
+    ctx.load(cp, sp, tree=N.TREE_SAH)
+    n = args.rays
+    o, dd = scenes.microbench_rays(n)
+    dev = torch.device("cuda", 0)
+    to = torch.from_numpy(o).to(dev)
+    td = torch.from_numpy(dd).to(dev)
+    obj = torch.empty(n, dtype=torch.int32, device=dev)
+    t = torch.empty(n, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream()
+    lib = ctx._lib
+
+    def launch(any_hit, tmin=None, tmax=None):
+        p = lambda x: C.c_void_p(x.data_ptr()) if x is not None else None
+        rc = lib.c2g_trace_rays_dev(ctx.handle, n, p(to), p(td), p(tmin), p(tmax), None, int(any_hit), p(obj),
+                                    None if any_hit else p(t), C.c_void_p(stream.cuda_stream))
+        ctx.check(rc)
+
+    def timed(any_hit, tmin=None, tmax=None):
+        for _ in range(3):
+            launch(any_hit, tmin, tmax)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            launch(any_hit, tmin, tmax)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / args.steps
+
+    s_closest = timed(False)
+    tc = t.clone()
+    hit = torch.isfinite(tc) & (obj >= 0)
+    g = torch.Generator(device="cpu").manual_seed(5)
+    u = torch.rand(n, generator=g).to(dev)
+    tmax = torch.where(hit, 2.0 * tc * u, torch.full_like(u, 4.0) * u).contiguous()
+    tmin = torch.zeros(n, dtype=torch.float32, device=dev)
+    s_any = timed(True, tmin, tmax)
+    return {"scene": "1M-triangle soup (SAH tree, four-wide nodes)", "rays": n,
+            "closest_mrays_per_s": round(n / s_closest / 1e6, 1), "anyhit_mrays_per_s": round(n / s_any / 1e6, 1),
+            "closest_hit_fraction": round(float(hit.float().mean().item()), 4)}
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -497,6 +560,8 @@ def main() -> int:
     ap.add_argument("--sah-width", type=int, default=4, choices=[2, 4], help="SAH traversal variant")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0: the library default, 2^21)")
     ap.add_argument("--batch-jobs", type=int, default=64)
+    ap.add_argument("--no-rays", action="store_true", help="skip the ray-intersection microbench")
+    ap.add_argument("--rays", type=int, default=1 << 24)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
