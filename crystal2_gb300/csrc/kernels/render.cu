@@ -204,7 +204,7 @@ template <bool COUNT>
 __global__ void k_extend(DevScene S, const float4* __restrict__ qo, const float4* __restrict__ qd, float4* hit,
                          const int* qcount, int* zero_a, int* zero_b, int* zero_c, int* bucket_cnt, int* bucket_list,
                          int cap, unsigned long long* cnt) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) { *zero_a = 0; *zero_b = 0; *zero_c = 0; }
+    if (blockIdx.x == 0 && threadIdx.x == 0) { *zero_a = 0; *zero_b = 0; *zero_c = 0; zero_b[2] = 0; }  // + shadow fetch counter
     const int n = *qcount;
     const int stride = gridDim.x * blockDim.x;
     TraceCounters tc{0, 0};
@@ -538,6 +538,100 @@ __global__ void k_shadow(DevScene S, const int* __restrict__ list, const int* co
     if (COUNT) flush_counts(cnt, C2G_K_SHADOW, rays, tc);
 }
 
+// Four-wide any-hit traversal with dynamic ray fetch: a lane whose ray is finished takes the next
+// ray from a global counter at the end of every while-while round, instead of idling until the
+// slowest ray of its warp ends (persistent threads with ray replacement).  Same per-ray traversal
+// as trace_any_bvh4, so the same rays are occluded.
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_shadow_fetch(DevScene S, const int* __restrict__ list, const int* count,
+                                                      const float4* __restrict__ so, const float4* __restrict__ sd,
+                                                      float4* sc, int* fetch, unsigned long long* cnt) {
+    const int n = *count;
+    const int lane = threadIdx.x & 31;
+    TraceCounters tc{0, 0};
+    unsigned rays = 0;
+    int ray = -1;
+    bool exhausted = false;
+    RayQ r;
+    float tmax = 0.f;
+    int ign = -1;
+    int stack[kStack4];
+    int top = 0, ref = kNoRef, leaf = kNoRef;
+    while (true) {
+        // refill: lanes without a ray take consecutive rays from the counter
+        const bool need = ray < 0 && !exhausted;
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(fetch, __popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                const int idx = base + __popc(m & ((1u << lane) - 1u));
+                if (idx < n) {
+                    const float4 o = so[idx], d = sd[idx];
+                    r = make_rayq(f3(o), f3(d));
+                    tmax = d.w;
+                    ign = __float_as_int(o.w);
+                    ray = idx;
+                    top = 0;
+                    ref = 0;
+                    leaf = kNoRef;
+                    rays++;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, ray >= 0) == 0) break;
+        if (ray < 0) continue;
+        // one while-while round: inner nodes until every active lane holds a leaf, then the leaves
+        bool occluded = false;
+        while (ref >= 0) {
+            const float4* N = reinterpret_cast<const float4*>(S.nodes4 + ref);
+            const float4 lx = __ldg(N), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3), lz = __ldg(N + 4),
+                         hz = __ldg(N + 5);
+            const int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6));
+            if (COUNT) tc.nodes++;
+            float te;
+            const bool h0 = slab4(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, 0.f, tmax, te);
+            const bool h1 = slab4(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, 0.f, tmax, te);
+            const bool h2 = slab4(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, 0.f, tmax, te);
+            const bool h3 = slab4(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, 0.f, tmax, te);
+            if (top + 3 > kStack4) { dev_flag_error(S.err, DEVERR_STACK); top = 0; ref = kNoRef; leaf = kNoRef; break; }
+            int next = kNoRef;
+            if (h3) next = ch.w;
+            if (h2) { if (next != kNoRef) stack[top++] = next; next = ch.z; }
+            if (h1) { if (next != kNoRef) stack[top++] = next; next = ch.y; }
+            if (h0) { if (next != kNoRef) stack[top++] = next; next = ch.x; }
+            ref = next != kNoRef ? next : (top ? stack[--top] : kNoRef);
+            if (is_leaf(ref) && leaf == kNoRef) {
+                leaf = ref;
+                ref = top ? stack[--top] : kNoRef;
+            }
+            if (!__any_sync(__activemask(), leaf == kNoRef)) break;
+        }
+        while (leaf != kNoRef && !occluded) {
+            int first, cnt_;
+            leaf_range(leaf, first, cnt_);
+            for (int k = 0; k < cnt_; k++) {
+                if (COUNT) tc.prims++;
+                if (anyhit_prim(S, first + k, r, 0.f, tmax, ign)) { occluded = true; break; }
+            }
+            leaf = kNoRef;
+            if (!occluded && is_leaf(ref)) {
+                leaf = ref;
+                ref = top ? stack[--top] : kNoRef;
+            }
+        }
+        if (occluded || (ref == kNoRef && leaf == kNoRef)) {
+            if (occluded) sc[list[ray]] = make_float4(0.f, 0.f, 0.f, 0.f);
+            ray = -1;
+        }
+    }
+    if (COUNT) flush_counts(cnt, C2G_K_SHADOW, rays, tc);
+}
+
 // ---- mis: closest hit of the NEE BSDF sample; records the emitter it reaches ---------------------
 template <bool COUNT>
 __global__ void k_mis(DevScene S, const int* __restrict__ list, const int* count, const float4* __restrict__ mo,
@@ -866,6 +960,7 @@ int GpuScene::film_download(float* rgb_sum, float* weight, float* rgb_sumsq, std
 
 namespace {
 int g_raygen = 0, g_ext = 0, g_ext_c = 0, g_shade = 0, g_sh = 0, g_sh_c = 0, g_mis = 0, g_mis_c = 0, g_acc = 0, g_film = 0;
+int g_shf = 0, g_shf_c = 0;
 void ensure_grids() {
     if (g_raygen) return;
     g_raygen = grid_for((const void*)k_raygen, 256);
@@ -874,6 +969,8 @@ void ensure_grids() {
     g_shade = grid_for((const void*)k_shade<MAT_DIFFUSE, false>, 128);
     g_sh = grid_for((const void*)k_shadow<false>, 128);
     g_sh_c = grid_for((const void*)k_shadow<true>, 128);
+    g_shf = grid_for((const void*)k_shadow_fetch<false>, 128);
+    g_shf_c = grid_for((const void*)k_shadow_fetch<true>, 128);
     g_mis = grid_for((const void*)k_mis<false>, 128);
     g_mis_c = grid_for((const void*)k_mis<true>, 128);
     g_acc = grid_for((const void*)k_accumulate, 256);
@@ -1019,8 +1116,15 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
             launches++;
         }
         begin(C2G_K_SHADOW);
-        if (count) k_shadow<true><<<g_sh_c, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
-        else k_shadow<false><<<g_sh, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
+        if (S.tree == C2G_TREE_SAH && S.sah_width == 4) {
+            // four-wide nodes: the dynamic-fetch kernel (fetch counter C[4], zeroed by k_extend)
+            if (count) k_shadow_fetch<true><<<g_shf_c, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, C + 4, cnt);
+            else k_shadow_fetch<false><<<g_shf, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, C + 4, cnt);
+        } else if (count) {
+            k_shadow<true><<<g_sh_c, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
+        } else {
+            k_shadow<false><<<g_sh, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
+        }
         end();
         begin(C2G_K_MIS);
         if (count) k_mis<true><<<g_mis_c, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
