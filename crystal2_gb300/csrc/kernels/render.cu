@@ -229,6 +229,119 @@ __global__ void k_extend(DevScene S, const float4* __restrict__ qo, const float4
     if (COUNT) flush_counts(cnt, C2G_K_EXTEND, rays, tc);
 }
 
+// Four-wide closest-hit extension with dynamic ray fetch (see k_shadow_fetch).  A lane whose ray
+// is finished writes its hit, appends the slot to its material bucket (all lanes join the keyed
+// append of every round; idle lanes with no key) and takes the next ray.
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_extend_fetch(DevScene S, const float4* __restrict__ qo, const float4* __restrict__ qd,
+                                                      float4* hit, const int* qcount, int* zero_a, int* zero_b, int* zero_c,
+                                                      int* bucket_cnt, int* bucket_list, int cap, int* fetch,
+                                                      unsigned long long* cnt) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) { *zero_a = 0; *zero_b = 0; *zero_c = 0; zero_b[2] = 0; }  // + shadow fetch counter
+    const int n = *qcount;
+    const int lane = threadIdx.x & 31;
+    TraceCounters tc{0, 0};
+    unsigned rays = 0;
+    int ray = -1;
+    bool exhausted = false;
+    RayQ r;
+    Hit h{INFINITY, 0.f, 0.f, -1};
+    int stack[kStack4];
+    float stack_t[kStack4];
+    int top = 0, ref = kNoRef, leaf = kNoRef;
+    auto pop = [&]() -> int {
+        while (top > 0) {
+            --top;
+            if (stack_t[top] <= h.t) return stack[top];
+        }
+        return kNoRef;
+    };
+    while (true) {
+        const bool need = ray < 0 && !exhausted;
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(fetch, __popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                const int idx = base + __popc(m & ((1u << lane) - 1u));
+                if (idx < n) {
+                    const float4 o = qo[idx], d = qd[idx];
+                    r = make_rayq(f3(o), f3(d));
+                    h = Hit{INFINITY, 0.f, 0.f, -1};
+                    ray = idx;
+                    top = 0;
+                    ref = 0;
+                    leaf = kNoRef;
+                    rays++;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, ray >= 0) == 0) break;
+        int key = -1, done_ray = -1;
+        if (ray >= 0) {
+            while (ref >= 0) {
+                const float4* N = reinterpret_cast<const float4*>(S.nodes4 + ref);
+                const float4 lx = __ldg(N), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3), lz = __ldg(N + 4),
+                             hz = __ldg(N + 5);
+                const int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6));
+                if (COUNT) tc.nodes++;
+                const float lim = h.t;
+                float t[4];
+                int c[4] = {ch.x, ch.y, ch.z, ch.w};
+                if (!slab4(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, 0.f, lim, t[0])) { t[0] = INFINITY; c[0] = kNoRef; }
+                if (!slab4(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, 0.f, lim, t[1])) { t[1] = INFINITY; c[1] = kNoRef; }
+                if (!slab4(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, 0.f, lim, t[2])) { t[2] = INFINITY; c[2] = kNoRef; }
+                if (!slab4(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, 0.f, lim, t[3])) { t[3] = INFINITY; c[3] = kNoRef; }
+                cswap(t[0], c[0], t[1], c[1]);
+                cswap(t[2], c[2], t[3], c[3]);
+                cswap(t[0], c[0], t[2], c[2]);
+                cswap(t[1], c[1], t[3], c[3]);
+                cswap(t[1], c[1], t[2], c[2]);
+                if (top + 3 > kStack4) { dev_flag_error(S.err, DEVERR_STACK); top = 0; ref = kNoRef; leaf = kNoRef; break; }
+#pragma unroll
+                for (int k = 3; k >= 1; k--)
+                    if (c[k] != kNoRef) { stack[top] = c[k]; stack_t[top] = t[k]; top++; }
+                ref = c[0] != kNoRef ? c[0] : pop();
+                if (is_leaf(ref) && leaf == kNoRef) {
+                    leaf = ref;
+                    ref = pop();
+                }
+                if (!__any_sync(__activemask(), leaf == kNoRef)) break;
+            }
+            while (leaf != kNoRef) {
+                int first, count;
+                leaf_range(leaf, first, count);
+                for (int k = 0; k < count; k++) {
+                    if (COUNT) tc.prims++;
+                    closest_prim(S, first + k, r, INFINITY, h);
+                }
+                leaf = kNoRef;
+                if (is_leaf(ref)) {
+                    leaf = ref;
+                    ref = pop();
+                }
+            }
+            if (ref == kNoRef && leaf == kNoRef) {
+                hit[ray] = make_float4(h.t, h.u, h.v, __int_as_float(h.obj));
+                if (h.obj < 0) key = kBucketMiss;
+                else {
+                    const int mt = S.objs[h.obj].material;
+                    key = mt < 0 ? kBucketNone : S.mats[mt].type;
+                }
+                done_ray = ray;
+                ray = -1;
+            }
+        }
+        const int j = warp_append_keyed(bucket_cnt, key);
+        if (key >= 0) bucket_list[key * cap + j] = done_ray;
+    }
+    if (COUNT) flush_counts(cnt, C2G_K_EXTEND, rays, tc);
+}
+
 // ---- shade ---------------------------------------------------------------------------------------
 struct ShadeOut {
     PathRefs nxt;
@@ -960,7 +1073,7 @@ int GpuScene::film_download(float* rgb_sum, float* weight, float* rgb_sumsq, std
 
 namespace {
 int g_raygen = 0, g_ext = 0, g_ext_c = 0, g_shade = 0, g_sh = 0, g_sh_c = 0, g_mis = 0, g_mis_c = 0, g_acc = 0, g_film = 0;
-int g_shf = 0, g_shf_c = 0;
+int g_shf = 0, g_shf_c = 0, g_exf = 0, g_exf_c = 0;
 void ensure_grids() {
     if (g_raygen) return;
     g_raygen = grid_for((const void*)k_raygen, 256);
@@ -971,6 +1084,8 @@ void ensure_grids() {
     g_sh_c = grid_for((const void*)k_shadow<true>, 128);
     g_shf = grid_for((const void*)k_shadow_fetch<false>, 128);
     g_shf_c = grid_for((const void*)k_shadow_fetch<true>, 128);
+    g_exf = grid_for((const void*)k_extend_fetch<false>, 128);
+    g_exf_c = grid_for((const void*)k_extend_fetch<true>, 128);
     g_mis = grid_for((const void*)k_mis<false>, 128);
     g_mis_c = grid_for((const void*)k_mis<true>, 128);
     g_acc = grid_for((const void*)k_accumulate, 256);
@@ -1093,13 +1208,22 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
             if (qn == 0) break;
         }
         begin(C2G_K_EXTEND);
-        cudaMemsetAsync(C + kCntBucket, 0, sizeof(int) * kBuckets, st);
-        if (count)
+        // bucket sizes and the extension fetch counter C[5] start at zero on every level
+        cudaMemsetAsync(C + 5, 0, sizeof(int) * (kCntBucket - 5 + kBuckets), st);
+        if (S.tree == C2G_TREE_SAH && S.sah_width == 4) {
+            if (count)
+                k_extend_fetch<true><<<g_exf_c, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
+                                                              C + kCntBucket, w.bucket_list, (int)w.P, C + 5, cnt);
+            else
+                k_extend_fetch<false><<<g_exf, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
+                                                               C + kCntBucket, w.bucket_list, (int)w.P, C + 5, cnt);
+        } else if (count) {
             k_extend<true><<<g_ext_c, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
                                                     C + kCntBucket, w.bucket_list, (int)w.P, cnt);
-        else
+        } else {
             k_extend<false><<<g_ext, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
                                                      C + kCntBucket, w.bucket_list, (int)w.P, cnt);
+        }
         end();
         if (gv.sample) {
             begin(C2G_K_GUIDE);
