@@ -366,10 +366,9 @@ def run_ours(args) -> None:
 def guided_equal_time(args) -> dict:
     """Equal-time error of the guided path tracer against the plain one on the slit-lit glossy room.
 
-    Both arms render the same frame progressively in chunks of 8 spp, each in its fastest wave
-    schedule (plain: one wave of 8 samples; guided: waves of 2 samples, `--guided-train-steps`
-    Adam steps after each), for the same budget of render time (the c2g_render calls only; the
-    error is evaluated outside the timer).  relMSE = mean((I - R)^2 / (R^2 + 0.01))
+    Both arms render the same frame progressively in chunks of 8 spp, one wave of 8 samples per
+    chunk (the guided arm takes `--guided-train-steps` Adam steps after each wave), for the same
+    budget of render time (the c2g_render calls only; the error is evaluated outside the timer).  relMSE = mean((I - R)^2 / (R^2 + 0.01))
     against a plain reference of `--guided-ref-spp` samples from a disjoint sample range.
     Reported: both errors at the budget, the time the guided arm needs to reach the plain arm's
     error (linear interpolation on its error curve), and their ratio (the target is <= 0.5)."""
@@ -411,12 +410,11 @@ def guided_equal_time(args) -> dict:
 
     ctx.film_clear()
     ctx.render(params(N.INTEGRATOR_PATH, 0, 4))  # first-launch costs out of the way
-    # each arm in its fastest wave schedule: plain 8 samples per wave; guided 2 (a training
-    # step set after every wave)
+    # both arms render 8-sample waves (the guided arm trains after every wave)
     plain = progressive(N.INTEGRATOR_PATH, 8)
     ctx.load(cp, sp, tree=N.TREE_SAH)  # a fresh, untrained network
     ctx.guide_config(args.guided_lr, args.guided_bsdf_fraction, 2, args.guided_train_steps)
-    guided = progressive(N.INTEGRATOR_GUIDED, 2)
+    guided = progressive(N.INTEGRATOR_GUIDED, 8)
     target = plain[-1][2]
     reach = None
     for (t0_, _, e0), (t1_, _, e1) in zip(guided, guided[1:]):
@@ -431,7 +429,7 @@ def guided_equal_time(args) -> dict:
             "plain": {"spp": plain[-1][1], "s": round(plain[-1][0], 3), "relMSE": target, "samples_per_wave": 8},
             "guided": {"spp": guided[-1][1], "s": round(guided[-1][0], 3), "relMSE": guided[-1][2],
                        "bsdf_fraction": args.guided_bsdf_fraction, "learning_rate": args.guided_lr,
-                       "train_steps_per_wave": args.guided_train_steps, "samples_per_wave": 2,
+                       "train_steps_per_wave": args.guided_train_steps, "samples_per_wave": 8,
                        "adam_steps": steps, "last_batch": records, "last_loss": round(loss, 4)},
             "time_to_plain_relMSE_s": None if reach is None else round(reach, 3),
             "time_ratio": None if reach is None else round(reach / plain[-1][0], 3),
