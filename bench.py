@@ -195,6 +195,20 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def replica_rate(t_local: float, paths_local: float, dist=None) -> tuple[float, float]:
+    """Whole-job rate of independent replicas: (max time over ranks, Mpaths/s = all ranks' paths
+    over that time).  `dist` is torch.distributed with an initialised process group, or None."""
+    import torch
+    t_max, paths = t_local, paths_local
+    if dist is not None:
+        tt = torch.tensor([t_local], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        pp = torch.tensor([paths_local], dtype=torch.float64)
+        dist.all_reduce(pp, op=dist.ReduceOp.SUM)
+        t_max, paths = float(tt.item()), float(pp.item())
+    return t_max, paths / t_max / 1e6
+
+
 def run_ours(args) -> None:
     import ctypes as C
 
@@ -267,14 +281,8 @@ def run_ours(args) -> None:
     ms = ev0.elapsed_time(ev1)
     ctx.set_counting(0)
     t_local = ms / 1e3
-    if dist:
-        tt = torch.tensor([t_local], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    else:
-        t_max = t_local
     paths_rank = p.width * p.height * sps * args.steps
-    value = paths_rank * world / t_max / 1e6
+    t_max, value = replica_rate(t_local, paths_rank, dist)
     # end to end through the C ABI with host buffers
     film = np.zeros((p.height, p.width, 3), np.float32)
     wgt = np.zeros((p.height, p.width), np.float32)
@@ -291,12 +299,7 @@ def run_ours(args) -> None:
         q.wave_paths = args.wave_paths
         ctx.render(q)
         ctx.check(ctx._lib.c2g_film_download(ctx.handle, N.fptr(film), N.fptr(wgt)))
-    e2e_t = time.perf_counter() - t0
-    if dist:
-        tt = torch.tensor([e2e_t], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_t = float(tt.item())
-    e2e = paths_rank / args.steps * e2e_steps * world / e2e_t / 1e6
+    e2e_t, e2e = replica_rate(time.perf_counter() - t0, paths_rank / args.steps * e2e_steps, dist)
     # roofline of the dominant kernel
     peaks, peak_src = load_peaks()
     names = N.KERNEL_NAMES
