@@ -552,7 +552,7 @@ def main() -> int:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-guided", action="store_true", help="skip the guided-vs-plain equal-time measurement")
     ap.add_argument("--guided-res", default="960x540")
-    ap.add_argument("--guided-ref-spp", type=int, default=4096)
+    ap.add_argument("--guided-ref-spp", type=int, default=16384)
     ap.add_argument("--guided-seconds", type=float, default=4.0)
     ap.add_argument("--guided-lr", type=float, default=2e-3)
     ap.add_argument("--guided-bsdf-fraction", type=float, default=0.7)

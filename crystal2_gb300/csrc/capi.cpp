@@ -461,6 +461,14 @@ int c2g_guide_stats(c2g_ctx* ctx, double* loss, int* records, int* steps) {
     return C2G_OK;
 }
 
+int c2g_guide_levels(c2g_ctx* ctx, int levels) {
+    if (!ctx) return C2G_ERR_INVALID;
+    if (levels < 0) return fail(ctx, C2G_ERR_INVALID, "levels >= 0");
+    if (ctx->host_only) return fail(ctx, C2G_ERR_STATE, "host-only context");
+    ctx->gpu->set_guide_levels(levels);
+    return C2G_OK;
+}
+
 int c2g_guide_config(c2g_ctx* ctx, float learning_rate, float bsdf_fraction, int warmup_waves, int train_steps) {
     if (!ctx) return C2G_ERR_INVALID;
     if (!(learning_rate > 0.f) || !(bsdf_fraction > 0.f && bsdf_fraction <= 1.f) || warmup_waves < 0 || train_steps < 0)

@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(128) k_guide_eval(GuideNet net, const float* _
 
 // ---- records -> weighted training samples ------------------------------------------------------
 // Record (4 float4): (x, valid), (n, lum L at the vertex after its direct light), (wo, lum beta at
-// the vertex), (wi, 0).  Sample (4 float4): (x, w), (n, 0), (wo, 0), (wi, 0).
+// the vertex), (wi, BSDF density at wi).  Sample (4 float4): (x, w), (n, 0), (wo, 0), (wi, p_bsdf).
 __global__ void k_guide_batch(float4* rec, int rec_cap, int rec_depth, int rec_stride, const float4* __restrict__ out_L,
                               int wave_paths, float4* batch, int* batch_count, float* stats, int batch_cap) {
     const int stride = gridDim.x * blockDim.x;
@@ -288,7 +288,7 @@ __global__ void k_guide_batch(float4* rec, int rec_cap, int rec_depth, int rec_s
             batch[4 * j] = make_float4(r0.x, r0.y, r0.z, w);
             batch[4 * j + 1] = make_float4(r1.x, r1.y, r1.z, 0.f);
             batch[4 * j + 2] = make_float4(r2.x, r2.y, r2.z, 0.f);
-            batch[4 * j + 3] = make_float4(r3.x, r3.y, r3.z, 0.f);
+            batch[4 * j + 3] = r3;  // wi, BSDF density
         }
         float ws = keep ? w : 0.f;
         for (int o = 16; o > 0; o >>= 1) ws += __shfl_xor_sync(0xffffffffu, ws, o);
@@ -317,8 +317,8 @@ constexpr int kTDO = kTD3 + kTrainRows * kLdH;
 constexpr int kTWarpElems = kTDO + kTrainRows * kLdO;
 static_assert(kTrainRows * kLdOF * 4 <= 2 * kTrainRows * kLdH * 2, "FP32 outputs alias the d1/d2 tiles");
 constexpr size_t kTrainSmem = (size_t)(kFwElems + kBwElems + kTrainWarps * kTWarpElems) * 2;
-// dW tiles: layer 0 5 x 8, layers 1-2 4 x 8, layer 3 4 x 5 (the padded output columns are skipped)
-constexpr int kDwTiles = 40 + 32 + 32 + 20;
+// dW tiles: layer 0 5 x 8, layers 1-2 4 x 8, layer 3 4 x 6 (outputs 40..47: selection + padding)
+constexpr int kDwTiles = 40 + 32 + 32 + 24;
 constexpr int kDwPerWarp = (kDwTiles + kTrainWarps - 1) / kTrainWarps;
 
 __device__ __forceinline__ void ldsm_x4_trans(uint32_t* r, const void* p) {
@@ -335,12 +335,13 @@ __device__ __forceinline__ void dw_tile(int idx, int& l, int& mt, int& nt) {
     if (idx < 40) { l = 0; mt = idx >> 3; nt = idx & 7; }
     else if (idx < 72) { l = 1; mt = (idx - 40) >> 3; nt = (idx - 40) & 7; }
     else if (idx < 104) { l = 2; mt = (idx - 72) >> 3; nt = (idx - 72) & 7; }
-    else { l = 3; mt = (idx - 104) / 5; nt = (idx - 104) % 5; }
+    else { l = 3; mt = (idx - 104) / 6; nt = (idx - 104) % 6; }
 }
 
-// Gradient of w * -log q(wi) with respect to the 40 raw outputs o (see the oracle for the
-// formulas); returns -log q.  g[40..47] (padding) are left to the caller.
-__device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, float w, float* g) {
+// Gradient of w * -log q_mix(wi), q_mix = (1 - c) p_bsdf + c q_guide, with respect to the 41 raw
+// outputs o (see the oracle for the formulas); returns -log q_mix.  g[41..47] (padding) are left
+// to the caller.
+__device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, float w, float pb, float* g) {
     Lobe L[kGuideLobes];
     guide_lobes(o, L);
     float p[kGuideLobes], q = 0.f;
@@ -348,6 +349,12 @@ __device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, floa
     for (int k = 0; k < kGuideLobes; k++) { p[k] = L[k].w * vmf_pdf(L[k], wi); q += p[k]; }
     q = fmaxf(q, 1e-20f);
     const float inv_q = 1.f / q;
+    // the mixture with the BSDF: lobe gradients scale by c q / q_mix; the selection logit s gets
+    // -w (q - p_bsdf) dc/ds / q_mix
+    const float sg = 1.f / (1.f + __expf(-o[40]));
+    const float csel = 0.05f + 0.9f * sg;
+    const float qmix = fmaxf((1.f - csel) * pb + csel * q, 1e-20f);
+    const float rho = csel * q / qmix;
 #pragma unroll
     for (int k = 0; k < kGuideLobes; k++) {
         const float r = p[k] * inv_q;
@@ -362,18 +369,19 @@ __device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, floa
         const float3 m = f3(o[5 * k], o[5 * k + 1], o[5 * k + 2]);
         const float len = fmaxf(sqrtf(dot(m, m)), 1e-12f);
         const float3 dm = (wi - L[k].mu * c) * (kap / len);
-        g[5 * k + 0] = -w * r * dm.x;
-        g[5 * k + 1] = -w * r * dm.y;
-        g[5 * k + 2] = -w * r * dm.z;
-        g[5 * k + 3] = -w * r * dk * sig;
-        g[5 * k + 4] = -w * (r - L[k].w);
+        g[5 * k + 0] = -w * rho * r * dm.x;
+        g[5 * k + 1] = -w * rho * r * dm.y;
+        g[5 * k + 2] = -w * rho * r * dm.z;
+        g[5 * k + 3] = -w * rho * r * dk * sig;
+        g[5 * k + 4] = -w * rho * (r - L[k].w);
     }
+    g[40] = -w * (q - pb) * 0.9f * sg * (1.f - sg) / qmix;
 #pragma unroll
     for (int k = 0; k < kGuideOut; k++) {
         const float v = g[k];
         g[k] = isfinite(v) ? fminf(fmaxf(v, -1e3f), 1e3f) : 0.f;
     }
-    return -__logf(q);
+    return -__logf(qmix);
 }
 
 __global__ void __launch_bounds__(256, 1) k_guide_train(GuideNet net, const float4* __restrict__ batch, const int* batch_count,
@@ -407,13 +415,14 @@ __global__ void __launch_bounds__(256, 1) k_guide_train(GuideNet net, const floa
         const int j = base + warp * kTrainRows + s;
         const bool valid = j < n;
         float3 wi = f3(0.f, 0.f, 1.f);
-        float w = 0.f;
+        float w = 0.f, pb = 0.f;
         if (lane < 16) {
             float in[kGuideIn];
             if (valid) {
                 const float4 b0 = batch[4 * j], b1 = batch[4 * j + 1], b2 = batch[4 * j + 2], b3 = batch[4 * j + 3];
                 guide_encode(net, f3(b0), f3(b1), f3(b2), in);
                 wi = f3(b3);
+                pb = b3.w;
                 w = fminf(b0.w / fmaxf(mean_w, 1e-12f), 100.f);  // normalised, firefly-clamped weight
             } else {
 #pragma unroll
@@ -438,7 +447,7 @@ __global__ void __launch_bounds__(256, 1) k_guide_train(GuideNet net, const floa
             float o[kGuideOut];
 #pragma unroll
             for (int k = 0; k < kGuideOut; k++) o[k] = OF[s * kLdOF + k];
-            loss += w * nll_output_grad(o, wi, w, g);
+            loss += w * nll_output_grad(o, wi, w, pb, g);
             wsum += w;
         }
         __syncwarp();  // OF (aliasing d1/d2) fully read before the deltas are written
@@ -622,6 +631,11 @@ int GuideTrainer::init(DeviceArena& arena, size_t paths, int max_depth, const fl
                     h[guide_w_off(l) + k * N + n] = v;
                 }
         }
+        // selection bias: the untrained network draws from the mixture with probability
+        // 1 - alpha (the configured BSDF fraction), c = 0.05 + 0.9 sigmoid(s)
+        const float c0 = std::min(0.94f, std::max(0.06f, 1.f - alpha_));
+        const float sg = (c0 - 0.05f) / 0.9f;
+        h[guide_b_off(3) + 40] = std::log(sg / (1.f - sg));
         cudaMemcpy(params_, h.data(), kGuideParams * 4, cudaMemcpyHostToDevice);
         cudaMemset(grad_, 0, kGuideParams * 4);
         cudaMemset(adam_m_, 0, kGuideParams * 4);
@@ -756,11 +770,11 @@ int GuideTrainer::gradient(DeviceArena& arena, const float* host_samples, int n,
     if (n <= 0) { err = "empty batch"; return C2G_ERR_INVALID; }
     std::vector<float4> b((size_t)n * 4);
     for (int j = 0; j < n; j++) {
-        const float* v = host_samples + (size_t)13 * j;
+        const float* v = host_samples + (size_t)14 * j;
         b[4 * j] = make_float4(v[0], v[1], v[2], v[12]);
         b[4 * j + 1] = make_float4(v[3], v[4], v[5], 0.f);
         b[4 * j + 2] = make_float4(v[6], v[7], v[8], 0.f);
-        b[4 * j + 3] = make_float4(v[9], v[10], v[11], 0.f);
+        b[4 * j + 3] = make_float4(v[9], v[10], v[11], v[13]);
     }
     float4* db = (float4*)arena.alloc(b.size() * 16, err);
     if (!db) return C2G_ERR_OOM;

@@ -94,10 +94,13 @@ __device__ __forceinline__ float vmf_pdf(const Lobe& l, float3 w) {
 }
 
 // ---- packed mixture (inference output, read by the shading kernels) ---------------------------
-// Per slot kGuidePacked floats: 8 float4 (mean direction, concentration), the 8 lobe weights, and
-// the 8 products weight x vMF normaliser.  A non-finite network output is flagged by a NaN first
-// weight.
-constexpr int kGuidePacked = 48;
+// Per slot kGuidePacked floats: 8 float4 (mean direction, concentration), the 8 lobe weights, the 8
+// products weight x vMF normaliser, and the probability c of drawing from the mixture rather than
+// the BSDF.  A non-finite network output is flagged by a NaN first weight.
+constexpr int kGuidePacked = 52;
+
+// Technique selection: c = 0.05 + 0.9 sigmoid(s) keeps both techniques in use.
+__host__ __device__ __forceinline__ float guide_select(float s) { return 0.05f + 0.9f / (1.f + expf(-s)); }
 
 __device__ __forceinline__ void pack_lobes(const float* out, float* dst) {
     bool finite = true;
@@ -119,7 +122,11 @@ __device__ __forceinline__ void pack_lobes(const float* out, float* dst) {
     d4[9] = make_float4(w[4], w[5], w[6], w[7]);
     d4[10] = make_float4(wc[0], wc[1], wc[2], wc[3]);
     d4[11] = make_float4(wc[4], wc[5], wc[6], wc[7]);
+    d4[12] = make_float4(guide_select(out[40]), 0.f, 0.f, 0.f);
 }
+
+// Probability of drawing the continuation from the mixture (vs the BSDF).
+__device__ __forceinline__ float packed_select(const float4* p) { return __ldg(p + 12).x; }
 
 __device__ __forceinline__ bool packed_valid(const float4* p) { return isfinite(__ldg(p + 8).x); }
 

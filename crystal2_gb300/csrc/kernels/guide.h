@@ -10,7 +10,7 @@ namespace c2g {
 
 constexpr int kGuideIn = 80;
 constexpr int kGuideHidden = 64;
-constexpr int kGuideOut = 40;       // 8 lobes x 5
+constexpr int kGuideOut = 41;       // 8 lobes x 5, then the technique-selection logit
 constexpr int kGuideOutPad = 48;    // output layer padded to a multiple of 16 (backward K)
 constexpr int kGuideLobes = 8;
 constexpr int kGuideFreqs = 12;
@@ -81,8 +81,9 @@ public:
     int get_params(float* host, std::string& err);
     // Raw outputs for n explicit inputs (x, n, wo: 9 floats each) -> n x kGuideOut floats.
     int eval(DeviceArena& arena, const float* host_xnw, int n, float* host_out, std::string& err);
-    // Summed weight gradient of sum_j w_j * -log q(wi_j | x_j, n_j, wo_j) over n samples (13 floats
-    // each: x, n, wo, wi, w) with the fused training kernel; no Adam step.  loss = sum w (-log q) / sum w.
+    // Summed weight gradient of sum_j w_j * -log q_mix(wi_j | x_j, n_j, wo_j) over n samples (14
+    // floats each: x, n, wo, wi, w, p_bsdf) with the fused training kernel; no Adam step.
+    // loss = sum w (-log q_mix) / sum w.
     int gradient(DeviceArena& arena, const float* host_samples, int n, float* host_grad, double* loss, std::string& err);
 
 private:

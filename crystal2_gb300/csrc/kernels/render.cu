@@ -449,16 +449,17 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
         float2 uL = make_float2(0, 0), uB = make_float2(0, 0);
         const int nsflags = BXDF_ALL & ~BXDF_SPECULAR;
         // Guided vertex: the continuation is drawn from alpha * BSDF + (1 - alpha) * learned mixture
-        // and doubles as the BSDF technique of direct lighting (no separate MIS ray); light samples
-        // are weighted against the mixture pdf.  Before the network is trained alpha = 1.
+        // (1 - alpha: the network's selection probability at this vertex) and doubles as the BSDF
+        // technique of direct lighting (no separate MIS ray); light samples are weighted against the
+        // mixture pdf.  Before the network is trained alpha = 1.
         const bool gvert = G && do_nee && !direct && (bx.flags & BXDF_SPECULAR) == 0;
         const float4* lobes = reinterpret_cast<const float4*>(gv.out + (size_t)i * kGuidePacked);
-        float alpha = 1.f, detM = 1.f;
+        float alpha = 1.f;
+        const float detM = gvert ? fabsf(dot(fr.T, cross(fr.N, fr.B))) : 1.f;
         if (gvert && gv.sample) {
             // a non-finite network output or a degenerate shading frame leaves this vertex to
             // plain BSDF sampling
-            detM = fabsf(dot(fr.T, cross(fr.N, fr.B)));
-            alpha = (packed_valid(lobes) && detM > 1e-6f) ? gv.net.alpha : 1.f;
+            alpha = (packed_valid(lobes) && detM > 1e-6f) ? 1.f - packed_select(lobes) : 1.f;
         }
         bool nee_work = false, mis_ok = false, any_mis = false;
         float3 f2 = f3(0.f, 0.f, 0.f), wi2 = f3(0.f, 0.f, 0.f);
@@ -555,6 +556,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
             int stype = 0;
             bool ok;
             float3 f = bsdf_sample(bx, fr, u1, u2, wo, wi, pdf, BXDF_ALL, stype, ok);
+            float pb_rec = pdf;  // BSDF density of the continuation (local measure), for training
             if (gvert && alpha < 1.f) {
                 // One-sample MIS over {BSDF, learned mixture}: q = alpha p_bsdf + (1 - alpha) p_guide,
                 // both exactly evaluated, so the estimator stays unbiased.  The BSDF technique draws
@@ -580,6 +582,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                     const float lm = length(wi);
                     stype = (bx.flags & ~(BXDF_REFLECTION | BXDF_TRANSMISSION)) | BXDF_REFLECTION;
                     pdf = alpha * pb + (1.f - alpha) * packed_pdf(lobes, wg) * detM / (lm * lm * lm);
+                    pb_rec = pb;
                     ok = !is_zero(f) && pdf > 0.f;
                 } else if (ok) {
                     const float lm = length(wi);
@@ -598,8 +601,10 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                     float4* r = gv.rec + 4 * ((size_t)(pid / gv.rec_stride) * gv.rec_depth + bounce);
                     r[1] = make_float4(s.N.x, s.N.y, s.N.z, 0.2126f * L.x + 0.7152f * L.y + 0.0722f * L.z);
                     r[2] = make_float4(wo.x, wo.y, wo.z, 0.2126f * beta.x + 0.7152f * beta.y + 0.0722f * beta.z);
-                    const float3 wn = normalize(wi);
-                    r[3] = make_float4(wn.x, wn.y, wn.z, 0.f);
+                    // wi and the BSDF density in the world measure the network's mixture lives in
+                    const float lm = length(wi);
+                    const float3 wn = wi * (1.f / lm);
+                    r[3] = make_float4(wn.x, wn.y, wn.z, pb_rec * lm * lm * lm / fmaxf(detM, 1e-6f));
                     r[0] = make_float4(s.pos.x, s.pos.y, s.pos.z, 1.f);
                 }
                 beta = beta * (f * cosine / pdf);
@@ -1225,7 +1230,9 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
                                                      C + kCntBucket, w.bucket_list, (int)w.P, cnt);
         }
         end();
-        if (gv.sample) {
+        // the guide serves the first guide_levels_ bounce levels; deeper vertices shade plainly
+        const bool glevel = guided && (guide_levels_ <= 0 || b < guide_levels_);
+        if (gv.sample && glevel) {
             begin(C2G_K_GUIDE);
             guide_.infer(st, &S, buf[cur].o, buf[cur].d, w.hit, C + kCntBucket, w.bucket_list, (int)w.P, present_buckets_);
             end();
@@ -1235,7 +1242,7 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
         for (int bk = 0; bk < kBuckets; bk++) {
             if (!(present_buckets_ & (1 << bk))) continue;
             begin(C2G_K_SHADE);
-            launch_shade(bk, g_shade, st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so, gv, guided);
+            launch_shade(bk, g_shade, st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so, gv, glevel);
             end();
             launches++;
         }

@@ -85,6 +85,8 @@ public:
     GuideTrainer& guide() { return guide_; }
     // Guided integrator schedule: waves of plain BSDF sampling before the mixture is used, and
     // Adam steps per wave.
+    // Bounce levels (from the camera hit) that sample the guide and train it; 0 = every level.
+    void set_guide_levels(int levels) { guide_levels_ = levels < 0 ? 0 : levels; }
     void set_guide_schedule(int warmup_waves, int train_steps) {
         guide_warmup_ = warmup_waves < 0 ? 0 : warmup_waves;
         guide_train_steps_ = train_steps < 0 ? 0 : train_steps;
@@ -122,6 +124,7 @@ private:
     int guide_steps_ = 0;      // guided waves rendered on the loaded scene
     int guide_warmup_ = 2;     // guided waves that only record (BSDF sampling) before the mixture is used
     int guide_train_steps_ = 1;  // Adam steps per guided wave
+    int guide_levels_ = 2;       // bounce levels served by the guide (0: all)
     float box_lo_[3] = {0, 0, 0}, box_hi_[3] = {1, 1, 1};  // scene bounds (network input range)
     c2g_stats stats_{};
     int film_w_ = 0, film_h_ = 0;

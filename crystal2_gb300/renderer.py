@@ -192,12 +192,16 @@ class Context:
         return out
 
     def guide_gradient(self, samples: np.ndarray):
-        """(grad, loss) of sum w * -log q(wi) for samples (n, 13) = x, n, wo, wi, w."""
-        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 13)
+        """(grad, loss) of sum w * -log q_mix(wi) for samples (n, 14) = x, n, wo, wi, w, p_bsdf."""
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 14)
         g = np.zeros(N.GUIDE_PARAMS, np.float32)
         loss = C.c_double(0.0)
         self.check(self._lib.c2g_guide_gradient(self._h, s.shape[0], N.fptr(s), N.fptr(g), C.byref(loss)))
         return g, loss.value
+
+    def guide_levels(self, levels: int) -> None:
+        """Bounce levels (from the camera hit) served by the guide; 0 = all."""
+        self.check(self._lib.c2g_guide_levels(self._h, int(levels)))
 
     def guide_stats(self):
         """(loss, records, steps) of the last guided training step."""

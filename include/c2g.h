@@ -205,27 +205,33 @@ int c2g_batch_job_latency(c2g_batch* b, int i, double* ms);
  * No counterpart in the reference, which has no guided integrator; these calls configure and
  * inspect the network the guided path tracer trains online.  The network maps (position in the
  * scene box, shading normal, outgoing direction) to an 8-lobe von Mises-Fisher mixture over
- * directions; its weights are one flat FP32 vector of C2G_GUIDE_PARAMS values, layer by layer
- * W (inputs x outputs, row-major) then b, for layers 80->64->64->64->48 (the last 8 outputs are
- * padding, kept zero).  Loading a scene discards the network; a guided render creates one. */
+ * directions and the probability c = 0.05 + 0.9 sigmoid(s) of drawing from it rather than from the
+ * BSDF; its weights are one flat FP32 vector of C2G_GUIDE_PARAMS values, layer by layer W (inputs x
+ * outputs, row-major) then b, for layers 80->64->64->64->48 (outputs 41..47 are padding, kept
+ * zero).  Loading a scene discards the network; a guided render creates one. */
 #define C2G_GUIDE_PARAMS 16624
-#define C2G_GUIDE_OUTPUTS 40
+#define C2G_GUIDE_OUTPUTS 41
 /* Draw a fresh seeded network for the box [lo, hi] (normalises positions) and clear Adam. */
 int c2g_guide_reset(c2g_ctx* ctx, const float box_lo[3], const float box_hi[3], unsigned long long seed);
 int c2g_guide_set_params(c2g_ctx* ctx, const float* params);
 int c2g_guide_get_params(c2g_ctx* ctx, float* params);
-/* Raw outputs (per lobe: mean direction xyz unnormalised, concentration pre-softplus, weight logit)
- * for n inputs of 9 floats (x, n, wo) -> out[n * C2G_GUIDE_OUTPUTS]. */
+/* Raw outputs (per lobe: mean direction xyz unnormalised, concentration pre-softplus, weight logit;
+ * then the selection logit s) for n inputs of 9 floats (x, n, wo) -> out[n * C2G_GUIDE_OUTPUTS]. */
 int c2g_guide_eval(c2g_ctx* ctx, int n, const float* xnw, float* out);
-/* Summed gradient over n samples of 13 floats (x, n, wo, wi, w) of sum_j w_j * -log q(wi_j) as the
- * training kernel computes it (BF16 operands, FP32 accumulation), written to grad[C2G_GUIDE_PARAMS];
- * loss = sum w (-log q) / sum w.  No optimiser step. */
+/* Summed gradient over n samples of 14 floats (x, n, wo, wi, w, p_bsdf) of
+ * sum_j w_j * -log q_mix(wi_j), q_mix = (1 - c) p_bsdf + c q_guide, as the training kernel computes
+ * it (BF16 operands, FP32 accumulation), written to grad[C2G_GUIDE_PARAMS];
+ * loss = sum w (-log q_mix) / sum w.  No optimiser step. */
 int c2g_guide_gradient(c2g_ctx* ctx, int n, const float* samples, float* grad, double* loss);
 /* Training state of the last guided render: weighted NLL of the last batch, its size, Adam steps. */
 int c2g_guide_stats(c2g_ctx* ctx, double* loss, int* records, int* steps);
-/* learning_rate (Adam), bsdf_fraction (one-sample MIS probability of the BSDF technique, (0, 1]),
- * warmup_waves (guided waves that only train), train_steps (Adam steps per wave). */
+/* learning_rate (Adam), bsdf_fraction (initial one-sample MIS probability of the BSDF technique,
+ * (0, 1]; the network then learns it per vertex, within [0.05, 0.95]), warmup_waves (guided waves
+ * that only train), train_steps (Adam steps per wave). */
 int c2g_guide_config(c2g_ctx* ctx, float learning_rate, float bsdf_fraction, int warmup_waves, int train_steps);
+/* Bounce levels, from the camera hit, whose vertices sample (and train) the guide; deeper vertices
+ * use the plain tracer's estimator.  0 = every level; default 2. */
+int c2g_guide_levels(c2g_ctx* ctx, int levels);
 
 /* ---- ray queries (Scene::Intersect / Scene::IntersectTest, Scene.cpp:50-59) ---------------- */
 /* Closest hit (any_hit = 0): obj = scene index of the hit object or -1, t = distance.

@@ -13,7 +13,9 @@ restates the network defined by the library's C ABI (include/c2g.h, "learned gui
 * layers 80->64->64->64->48 with ReLU after the hidden layers; parameters are one flat vector,
   per layer W (K x N row-major) then b (N);
 * outputs 5 per lobe (8 lobes): mean direction (normalised), concentration softplus(k) + 0.05
-  (capped at 2000), weight softmax(logit); density sum_k w_k vMF(wi; mu_k, kappa_k).
+  (capped at 2000), weight softmax(logit); density q = sum_k w_k vMF(wi; mu_k, kappa_k); output 40
+  is the selection logit s: the sampler draws from q with probability c = 0.05 + 0.9 sigmoid(s)
+  and from the BSDF otherwise, so the training loss is -w log q_mix, q_mix = (1 - c) p_bsdf + c q.
 
 ``bf16=True`` rounds at the points where the kernels store BF16 (encoded inputs, weights, hidden
 activations, the output gradient and the back-propagated deltas); ``bf16=False`` is plain FP64,
@@ -23,7 +25,7 @@ from __future__ import annotations
 
 import numpy as np
 
-N_IN, HIDDEN, N_OUT, N_OUT_PAD, LOBES, FREQS = 80, 64, 40, 48, 8, 12
+N_IN, HIDDEN, N_OUT, N_OUT_PAD, LOBES, FREQS = 80, 64, 41, 48, 8, 12
 SHAPES = [(N_IN, HIDDEN), (HIDDEN, HIDDEN), (HIDDEN, HIDDEN), (HIDDEN, N_OUT_PAD)]
 N_PARAMS = sum(k * n + n for k, n in SHAPES)
 
@@ -98,7 +100,7 @@ def softplus(x):
 
 def lobes(out):
     """(mu (m, 8, 3), kappa (m, 8), w (m, 8)) from raw outputs."""
-    o = out[:, :N_OUT].reshape(-1, LOBES, 5)
+    o = out[:, :LOBES * 5].reshape(-1, LOBES, 5)
     m = o[:, :, :3]
     ln = np.linalg.norm(m, axis=2, keepdims=True)
     mu = np.where(ln > 1e-12, m / np.maximum(ln, 1e-300), np.array([0.0, 1.0, 0.0]))
@@ -119,23 +121,33 @@ def mixture_pdf(out, wi):
     return (w * vmf_pdf(mu, kappa, np.asarray(wi, np.float64))).sum(axis=1)
 
 
-def nll_gradient(params, enc, wi, weight, bf16_mode=True, clamp=1e3):
-    """(grad (N_PARAMS,), loss_sum, weight_sum) of sum_j w_j * -log q(wi_j).
+def select_prob(s):
+    return 0.05 + 0.9 / (1 + np.exp(-s))
 
-    Output-gradient formulas: d log q / d logit_k = r_k - w_k (r = posterior lobe share);
-    d log q / d kraw_k = r_k * (1/kappa - 2 e^-2kappa / (1 - e^-2kappa) + mu.wi - 1) * sigmoid(kraw)
-    (zero where kappa is capped); d log q / d m_k = r_k * kappa (wi - mu (mu.wi)) / |m_k|.
+
+def nll_gradient(params, enc, wi, weight, pb, bf16_mode=True, clamp=1e3):
+    """(grad (N_PARAMS,), loss_sum, weight_sum) of sum_j w_j * -log q_mix(wi_j).
+
+    Output-gradient formulas, with rho = c q / q_mix: d log q_mix / d logit_k = rho (r_k - w_k)
+    (r = posterior lobe share); d log q_mix / d kraw_k = rho r_k (1/kappa - 2 e^-2kappa /
+    (1 - e^-2kappa) + mu.wi - 1) sigmoid(kraw) (zero where kappa is capped); d log q_mix / d m_k =
+    rho r_k kappa (wi - mu (mu.wi)) / |m_k|; d log q_mix / d s = (q - p_bsdf) 0.9 sigmoid'(s) / q_mix.
     """
     r = bf16 if bf16_mode else (lambda v: np.asarray(v, np.float64))
     layers = unpack(params)
     out, acts = forward(params, enc, bf16_mode)
     wi = np.asarray(wi, np.float64)
     wgt = np.asarray(weight, np.float64)
-    o = out[:, :N_OUT].reshape(-1, LOBES, 5)
+    o = out[:, :LOBES * 5].reshape(-1, LOBES, 5)
     mu, kappa, w = lobes(out)
     p = w * vmf_pdf(mu, kappa, wi)
     q = np.maximum(p.sum(axis=1), 1e-20)
     rr = p / q[:, None]
+    pb = np.asarray(pb, np.float64)
+    sg = 1 / (1 + np.exp(-out[:, 40]))
+    csel = 0.05 + 0.9 * sg
+    qmix = np.maximum((1 - csel) * pb + csel * q, 1e-20)
+    rho = (csel * q / qmix)[:, None]
     c = np.einsum("mkj,mj->mk", mu, wi)
     e2 = np.exp(-2 * kappa)
     dk = 1 / kappa - 2 * e2 / np.maximum(-np.expm1(-2 * kappa), 1e-20) + (c - 1)
@@ -144,12 +156,13 @@ def nll_gradient(params, enc, wi, weight, bf16_mode=True, clamp=1e3):
     ln = np.maximum(np.linalg.norm(o[:, :, :3], axis=2), 1e-12)
     dm = (wi[:, None, :] - mu * c[:, :, None]) * (kappa / ln)[:, :, None]
     g = np.zeros((out.shape[0], N_OUT_PAD))
-    gv = g[:, :N_OUT].reshape(-1, LOBES, 5)
+    gv = g[:, :LOBES * 5].reshape(-1, LOBES, 5)
     ww = wgt[:, None]
-    gv[:, :, 0:3] = -(ww * rr)[:, :, None] * dm
-    gv[:, :, 3] = -ww * rr * dk * sig
-    gv[:, :, 4] = -ww * (rr - w)
-    g[:, :N_OUT] = gv.reshape(-1, N_OUT)
+    gv[:, :, 0:3] = -(ww * rho * rr)[:, :, None] * dm
+    gv[:, :, 3] = -ww * rho * rr * dk * sig
+    gv[:, :, 4] = -ww * rho * (rr - w)
+    g[:, :LOBES * 5] = gv.reshape(-1, LOBES * 5)
+    g[:, 40] = -wgt * (q - pb) * 0.9 * sg * (1 - sg) / qmix
     if clamp is not None:
         g = np.clip(np.where(np.isfinite(g), g, 0.0), -clamp, clamp)
     active = wgt > 0
@@ -165,14 +178,16 @@ def nll_gradient(params, enc, wi, weight, bf16_mode=True, clamp=1e3):
         dW = acts[l].T @ deltas[l]
         db = deltas[l].sum(axis=0)
         grads.append((dW, db))
-    loss = float((wgt[active] * -np.log(q[active])).sum())
+    loss = float((wgt[active] * -np.log(qmix[active])).sum())
     return pack(grads), loss, float(wgt[active].sum())
 
 
-def nll(params, enc, wi, weight) -> float:
+def nll(params, enc, wi, weight, pb) -> float:
     out, _ = forward(params, enc, bf16_mode=False)
-    q = np.maximum(mixture_pdf(out, wi), 1e-20)
-    return float((np.asarray(weight, np.float64) * -np.log(q)).sum())
+    q = mixture_pdf(out, wi)
+    c = select_prob(out[:, 40])
+    qmix = np.maximum((1 - c) * np.asarray(pb, np.float64) + c * q, 1e-20)
+    return float((np.asarray(weight, np.float64) * -np.log(qmix)).sum())
 
 
 def init_params(seed: int = 0, out_scale: float = 0.1) -> np.ndarray:
@@ -191,7 +206,8 @@ def init_params(seed: int = 0, out_scale: float = 0.1) -> np.ndarray:
 
 
 def random_samples(m: int, seed: int = 1, lo=(-1, -1, -1), hi=(1, 1, 1)):
-    """Seeded (x, n, wo, wi, w) batch: positions in the box, unit directions, weights in (0, 4)."""
+    """Seeded (x, n, wo, wi, w, p_bsdf) batch: positions in the box, unit directions, weights in
+    (0, 4), BSDF densities in (0.05, 2)."""
     rng = np.random.default_rng(seed)
     lo, hi = np.asarray(lo, np.float64), np.asarray(hi, np.float64)
     x = lo + (hi - lo) * rng.random((m, 3))
@@ -201,16 +217,16 @@ def random_samples(m: int, seed: int = 1, lo=(-1, -1, -1), hi=(1, 1, 1)):
         return v / np.linalg.norm(v, axis=1, keepdims=True)
 
     return x.astype(np.float32), unit(m).astype(np.float32), unit(m).astype(np.float32), unit(m).astype(np.float32), \
-        (4 * rng.random(m)).astype(np.float32)
+        (4 * rng.random(m)).astype(np.float32), (0.05 + 1.95 * rng.random(m)).astype(np.float32)
 
 
 def finite_difference_check(seed: int = 0, m: int = 16, n_probe: int = 64, h: float = 1e-6) -> float:
     """Max relative error between the analytic FP64 gradient and central differences on n_probe
     random parameters (no BF16 rounding, no clamping)."""
     params = init_params(seed, out_scale=1.0)
-    x, n, wo, wi, w = random_samples(m, seed + 1)
+    x, n, wo, wi, w, pb = random_samples(m, seed + 1)
     enc = encode(x, n, wo, (-1, -1, -1), (1, 1, 1))
-    g, _, _ = nll_gradient(params, enc, wi, w, bf16_mode=False, clamp=None)
+    g, _, _ = nll_gradient(params, enc, wi, w, pb, bf16_mode=False, clamp=None)
     rng = np.random.default_rng(seed + 2)
     live = [i for i in range(N_PARAMS) if not _is_pad(i)]
     idx = rng.choice(live, n_probe, replace=False)
@@ -219,7 +235,7 @@ def finite_difference_check(seed: int = 0, m: int = 16, n_probe: int = 64, h: fl
         pp, pm = params.copy(), params.copy()
         pp[i] += h
         pm[i] -= h
-        fd = (nll(pp, enc, wi, w) - nll(pm, enc, wi, w)) / (2 * h)
+        fd = (nll(pp, enc, wi, w, pb) - nll(pm, enc, wi, w, pb)) / (2 * h)
         worst = max(worst, abs(fd - g[i]) / max(1e-6, abs(fd), abs(g[i])))
     return worst
 

@@ -31,7 +31,7 @@ def test_analytic_gradient_matches_finite_differences():
 
 def test_mixture_pdf_integrates_to_one():
     params = G.init_params(3, out_scale=3.0)
-    x, n, wo, _, _ = G.random_samples(4, seed=9)
+    x, n, wo, _, _, _ = G.random_samples(4, seed=9)
     out, _ = G.forward(params, G.encode(x, n, wo, (-1, -1, -1), (1, 1, 1)), bf16_mode=False)
     # midpoint quadrature in (cos theta, phi): the measure is uniform in those coordinates
     nt, npf = 1200, 600
