@@ -69,6 +69,7 @@ struct DeviceSceneBuffers {
     std::vector<void*> owned;
     int* err = nullptr;
     unsigned long long* counts = nullptr;  // nodes/prims counters (closest, any)
+    int* fetch = nullptr;                  // ray-query fetch counter
     float4* film = nullptr;                // rgb sum, weight
     float4* film_m2 = nullptr;             // rgb sum of squares
     int n_lights = 0;
@@ -239,102 +240,39 @@ __global__ void __launch_bounds__(128) k_extend_fetch(DevScene S, const float4* 
                                                       unsigned long long* cnt) {
     if (blockIdx.x == 0 && threadIdx.x == 0) { *zero_a = 0; *zero_b = 0; *zero_c = 0; zero_b[2] = 0; }  // + shadow fetch counter
     const int n = *qcount;
-    const int lane = threadIdx.x & 31;
     TraceCounters tc{0, 0};
     unsigned rays = 0;
     int ray = -1;
     bool exhausted = false;
     RayQ r;
     Hit h{INFINITY, 0.f, 0.f, -1};
-    int stack[kStack4];
-    float stack_t[kStack4];
-    int top = 0, ref = kNoRef, leaf = kNoRef;
-    auto pop = [&]() -> int {
-        while (top > 0) {
-            --top;
-            if (stack_t[top] <= h.t) return stack[top];
-        }
-        return kNoRef;
-    };
+    Bvh4State st;
     while (true) {
         const bool need = ray < 0 && !exhausted;
-        const unsigned m = __ballot_sync(0xffffffffu, need);
-        if (m) {
-            const int leader = __ffs(m) - 1;
-            int base = 0;
-            if (lane == leader) base = atomicAdd(fetch, __popc(m));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (need) {
-                const int idx = base + __popc(m & ((1u << lane) - 1u));
-                if (idx < n) {
-                    const float4 o = qo[idx], d = qd[idx];
-                    r = make_rayq(f3(o), f3(d));
-                    h = Hit{INFINITY, 0.f, 0.f, -1};
-                    ray = idx;
-                    top = 0;
-                    ref = 0;
-                    leaf = kNoRef;
-                    rays++;
-                } else {
-                    exhausted = true;
-                }
+        const int idx = warp_fetch(fetch, need, n);
+        if (need) {
+            if (idx >= 0) {
+                const float4 o = qo[idx], d = qd[idx];
+                r = make_rayq(f3(o), f3(d));
+                h = Hit{INFINITY, 0.f, 0.f, -1};
+                ray = idx;
+                bvh4_begin(st);
+                rays++;
+            } else {
+                exhausted = true;
             }
         }
         if (__ballot_sync(0xffffffffu, ray >= 0) == 0) break;
         int key = -1, done_ray = -1;
-        if (ray >= 0) {
-            while (ref >= 0) {
-                const float4* N = reinterpret_cast<const float4*>(S.nodes4 + ref);
-                const float4 lx = __ldg(N), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3), lz = __ldg(N + 4),
-                             hz = __ldg(N + 5);
-                const int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6));
-                if (COUNT) tc.nodes++;
-                const float lim = h.t;
-                float t[4];
-                int c[4] = {ch.x, ch.y, ch.z, ch.w};
-                if (!slab4(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, 0.f, lim, t[0])) { t[0] = INFINITY; c[0] = kNoRef; }
-                if (!slab4(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, 0.f, lim, t[1])) { t[1] = INFINITY; c[1] = kNoRef; }
-                if (!slab4(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, 0.f, lim, t[2])) { t[2] = INFINITY; c[2] = kNoRef; }
-                if (!slab4(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, 0.f, lim, t[3])) { t[3] = INFINITY; c[3] = kNoRef; }
-                cswap(t[0], c[0], t[1], c[1]);
-                cswap(t[2], c[2], t[3], c[3]);
-                cswap(t[0], c[0], t[2], c[2]);
-                cswap(t[1], c[1], t[3], c[3]);
-                cswap(t[1], c[1], t[2], c[2]);
-                if (top + 3 > kStack4) { dev_flag_error(S.err, DEVERR_STACK); top = 0; ref = kNoRef; leaf = kNoRef; break; }
-#pragma unroll
-                for (int k = 3; k >= 1; k--)
-                    if (c[k] != kNoRef) { stack[top] = c[k]; stack_t[top] = t[k]; top++; }
-                ref = c[0] != kNoRef ? c[0] : pop();
-                if (is_leaf(ref) && leaf == kNoRef) {
-                    leaf = ref;
-                    ref = pop();
-                }
-                if (!__any_sync(__activemask(), leaf == kNoRef)) break;
+        if (ray >= 0 && bvh4_closest_round<COUNT>(S, r, INFINITY, h, st, &tc)) {
+            hit[ray] = make_float4(h.t, h.u, h.v, __int_as_float(h.obj));
+            if (h.obj < 0) key = kBucketMiss;
+            else {
+                const int mt = S.objs[h.obj].material;
+                key = mt < 0 ? kBucketNone : S.mats[mt].type;
             }
-            while (leaf != kNoRef) {
-                int first, count;
-                leaf_range(leaf, first, count);
-                for (int k = 0; k < count; k++) {
-                    if (COUNT) tc.prims++;
-                    closest_prim(S, first + k, r, INFINITY, h);
-                }
-                leaf = kNoRef;
-                if (is_leaf(ref)) {
-                    leaf = ref;
-                    ref = pop();
-                }
-            }
-            if (ref == kNoRef && leaf == kNoRef) {
-                hit[ray] = make_float4(h.t, h.u, h.v, __int_as_float(h.obj));
-                if (h.obj < 0) key = kBucketMiss;
-                else {
-                    const int mt = S.objs[h.obj].material;
-                    key = mt < 0 ? kBucketNone : S.mats[mt].type;
-                }
-                done_ray = ray;
-                ray = -1;
-            }
+            done_ray = ray;
+            ray = -1;
         }
         const int j = warp_append_keyed(bucket_cnt, key);
         if (key >= 0) bucket_list[key * cap + j] = done_ray;
@@ -665,7 +603,6 @@ __global__ void __launch_bounds__(128) k_shadow_fetch(DevScene S, const int* __r
                                                       const float4* __restrict__ so, const float4* __restrict__ sd,
                                                       float4* sc, int* fetch, unsigned long long* cnt) {
     const int n = *count;
-    const int lane = threadIdx.x & 31;
     TraceCounters tc{0, 0};
     unsigned rays = 0;
     int ray = -1;
@@ -673,76 +610,27 @@ __global__ void __launch_bounds__(128) k_shadow_fetch(DevScene S, const int* __r
     RayQ r;
     float tmax = 0.f;
     int ign = -1;
-    int stack[kStack4];
-    int top = 0, ref = kNoRef, leaf = kNoRef;
+    Bvh4AnyState st;
     while (true) {
-        // refill: lanes without a ray take consecutive rays from the counter
         const bool need = ray < 0 && !exhausted;
-        const unsigned m = __ballot_sync(0xffffffffu, need);
-        if (m) {
-            const int leader = __ffs(m) - 1;
-            int base = 0;
-            if (lane == leader) base = atomicAdd(fetch, __popc(m));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (need) {
-                const int idx = base + __popc(m & ((1u << lane) - 1u));
-                if (idx < n) {
-                    const float4 o = so[idx], d = sd[idx];
-                    r = make_rayq(f3(o), f3(d));
-                    tmax = d.w;
-                    ign = __float_as_int(o.w);
-                    ray = idx;
-                    top = 0;
-                    ref = 0;
-                    leaf = kNoRef;
-                    rays++;
-                } else {
-                    exhausted = true;
-                }
+        const int idx = warp_fetch(fetch, need, n);
+        if (need) {
+            if (idx >= 0) {
+                const float4 o = so[idx], d = sd[idx];
+                r = make_rayq(f3(o), f3(d));
+                tmax = d.w;
+                ign = __float_as_int(o.w);
+                ray = idx;
+                bvh4_begin(st);
+                rays++;
+            } else {
+                exhausted = true;
             }
         }
         if (__ballot_sync(0xffffffffu, ray >= 0) == 0) break;
         if (ray < 0) continue;
-        // one while-while round: inner nodes until every active lane holds a leaf, then the leaves
-        bool occluded = false;
-        while (ref >= 0) {
-            const float4* N = reinterpret_cast<const float4*>(S.nodes4 + ref);
-            const float4 lx = __ldg(N), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3), lz = __ldg(N + 4),
-                         hz = __ldg(N + 5);
-            const int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6));
-            if (COUNT) tc.nodes++;
-            float te;
-            const bool h0 = slab4(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, 0.f, tmax, te);
-            const bool h1 = slab4(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, 0.f, tmax, te);
-            const bool h2 = slab4(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, 0.f, tmax, te);
-            const bool h3 = slab4(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, 0.f, tmax, te);
-            if (top + 3 > kStack4) { dev_flag_error(S.err, DEVERR_STACK); top = 0; ref = kNoRef; leaf = kNoRef; break; }
-            int next = kNoRef;
-            if (h3) next = ch.w;
-            if (h2) { if (next != kNoRef) stack[top++] = next; next = ch.z; }
-            if (h1) { if (next != kNoRef) stack[top++] = next; next = ch.y; }
-            if (h0) { if (next != kNoRef) stack[top++] = next; next = ch.x; }
-            ref = next != kNoRef ? next : (top ? stack[--top] : kNoRef);
-            if (is_leaf(ref) && leaf == kNoRef) {
-                leaf = ref;
-                ref = top ? stack[--top] : kNoRef;
-            }
-            if (!__any_sync(__activemask(), leaf == kNoRef)) break;
-        }
-        while (leaf != kNoRef && !occluded) {
-            int first, cnt_;
-            leaf_range(leaf, first, cnt_);
-            for (int k = 0; k < cnt_; k++) {
-                if (COUNT) tc.prims++;
-                if (anyhit_prim(S, first + k, r, 0.f, tmax, ign)) { occluded = true; break; }
-            }
-            leaf = kNoRef;
-            if (!occluded && is_leaf(ref)) {
-                leaf = ref;
-                ref = top ? stack[--top] : kNoRef;
-            }
-        }
-        if (occluded || (ref == kNoRef && leaf == kNoRef)) {
+        bool occluded;
+        if (bvh4_any_round<COUNT>(S, r, 0.f, tmax, ign, st, &tc, occluded)) {
             if (occluded) sc[list[ray]] = make_float4(0.f, 0.f, 0.f, 0.f);
             ray = -1;
         }
@@ -857,6 +745,51 @@ __global__ void k_trace_rays(DevScene S, int n, const float* o, const float* d, 
         Hit h = trace_closest<false>(S, ro, rd, nullptr);
         obj[i] = h.obj;
         if (t) t[i] = h.obj >= 0 ? h.t : INFINITY;
+    }
+}
+
+// Ray queries on four-wide nodes with dynamic fetch (same results as k_trace_rays).
+__global__ void __launch_bounds__(128) k_trace_rays_fetch(DevScene S, int n, const float* o, const float* d, const float* tmin,
+                                                          const float* tmax, const int* ignore, int any_hit, int* obj,
+                                                          float* t, int* fetch) {
+    int ray = -1;
+    bool exhausted = false;
+    RayQ r;
+    float a = 0.f, b = INFINITY;
+    int ig = -1;
+    Hit h{INFINITY, 0.f, 0.f, -1};
+    Bvh4State st;
+    Bvh4AnyState sa;
+    while (true) {
+        const bool need = ray < 0 && !exhausted;
+        const int idx = warp_fetch(fetch, need, n);
+        if (need) {
+            if (idx >= 0) {
+                r = make_rayq(f3(o[3 * idx], o[3 * idx + 1], o[3 * idx + 2]), f3(d[3 * idx], d[3 * idx + 1], d[3 * idx + 2]));
+                a = tmin ? tmin[idx] : 0.f;
+                b = tmax ? tmax[idx] : INFINITY;
+                ig = ignore ? ignore[idx] : -1;
+                h = Hit{INFINITY, 0.f, 0.f, -1};
+                ray = idx;
+                if (any_hit) bvh4_begin(sa);
+                else bvh4_begin(st);
+            } else {
+                exhausted = true;
+            }
+        }
+        if (__ballot_sync(0xffffffffu, ray >= 0) == 0) break;
+        if (ray < 0) continue;
+        if (any_hit) {
+            bool occ;
+            if (bvh4_any_round<false>(S, r, a, b, ig, sa, nullptr, occ)) {
+                obj[ray] = occ ? 1 : 0;
+                ray = -1;
+            }
+        } else if (bvh4_closest_round<false>(S, r, INFINITY, h, st, nullptr)) {
+            obj[ray] = h.obj;
+            if (t) t[ray] = h.obj >= 0 ? h.t : INFINITY;
+            ray = -1;
+        }
     }
 }
 
@@ -1009,6 +942,9 @@ int GpuScene::upload(const HostScene& s, int tree, const RefTree* ref, const Sah
     sb_->counts = (unsigned long long*)arena.alloc(sizeof(unsigned long long) * 3 * C2G_K_KINDS, err);
     if (!sb_->counts) return C2G_ERR_OOM;
     sb_->owned.push_back(sb_->counts);
+    sb_->fetch = (int*)arena.alloc(256, err);
+    if (!sb_->fetch) return C2G_ERR_OOM;
+    sb_->owned.push_back(sb_->fetch);
     C2G_CUDA(cudaMemset(sb_->counts, 0, sizeof(unsigned long long) * 3 * C2G_K_KINDS));
     // film
     film_w_ = s.cfg.width;
@@ -1421,7 +1357,15 @@ int GpuScene::trace_rays_dev(int n, const float* o, const float* d, const float*
                              int any_hit, int* obj, float* t, cudaStream_t st, std::string& err) {
     if (!sb_->film) { err = "no scene loaded"; return C2G_ERR_STATE; }
     if (n <= 0) return C2G_OK;
-    k_trace_rays<<<(n + 127) / 128, 128, 0, st>>>(sb_->S, n, o, d, tmin, tmax, ignore, any_hit, obj, t);
+    const DevScene& S = sb_->S;
+    if (S.tree == C2G_TREE_SAH && S.sah_width == 4 && sb_->fetch) {
+        static int grid = 0;
+        if (!grid) grid = grid_for((const void*)k_trace_rays_fetch, 128);
+        C2G_CUDA(cudaMemsetAsync(sb_->fetch, 0, sizeof(int), st));
+        k_trace_rays_fetch<<<grid, 128, 0, st>>>(S, n, o, d, tmin, tmax, ignore, any_hit, obj, t, sb_->fetch);
+    } else {
+        k_trace_rays<<<(n + 127) / 128, 128, 0, st>>>(S, n, o, d, tmin, tmax, ignore, any_hit, obj, t);
+    }
     C2G_CUDA(cudaGetLastError());
     return C2G_OK;
 }

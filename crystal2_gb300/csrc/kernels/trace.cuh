@@ -566,6 +566,151 @@ __device__ __forceinline__ bool trace_any_bvh4(const DevScene& S, const RayQ& r,
     return false;
 }
 
+// ---- resumable four-wide traversal rounds (dynamic ray fetch) ----------------------------------
+// One while-while round of the traversal above: inner nodes until every active lane of the warp
+// holds a leaf, then the leaves.  The state survives between rounds, so a kernel can hand a lane a
+// new ray as soon as its previous one is done (see k_shadow_fetch / k_extend_fetch).
+struct Bvh4AnyState {       // any hit: no entry distances
+    int stack[kStack4];
+    int top, ref, leaf;
+};
+struct Bvh4State {          // closest hit: entry distance per stacked subtree
+    int stack[kStack4];
+    float stack_t[kStack4];
+    int top, ref, leaf;
+};
+
+template <class St>
+__device__ __forceinline__ void bvh4_begin(St& st) {
+    st.top = 0;
+    st.ref = 0;
+    st.leaf = kNoRef;
+}
+
+// Any hit in (tmin, tmax); returns true when the ray is finished (occluded or exhausted).
+template <bool COUNT>
+__device__ __forceinline__ bool bvh4_any_round(const DevScene& S, const RayQ& r, float tmin, float tmax, int ignore,
+                                               Bvh4AnyState& st, TraceCounters* cnt, bool& occluded) {
+    occluded = false;
+    int top = st.top, ref = st.ref, leaf = st.leaf;
+    while (ref >= 0) {
+        const float4* N = reinterpret_cast<const float4*>(S.nodes4 + ref);
+        const float4 lx = __ldg(N), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3), lz = __ldg(N + 4),
+                     hz = __ldg(N + 5);
+        const int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6));
+        if (COUNT) cnt->nodes++;
+        float te;
+        const bool h0 = slab4(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, tmin, tmax, te);
+        const bool h1 = slab4(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, tmin, tmax, te);
+        const bool h2 = slab4(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, tmin, tmax, te);
+        const bool h3 = slab4(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, tmin, tmax, te);
+        if (top + 3 > kStack4) { dev_flag_error(S.err, DEVERR_STACK); top = 0; ref = kNoRef; leaf = kNoRef; break; }
+        int next = kNoRef;
+        if (h3) next = ch.w;
+        if (h2) { if (next != kNoRef) st.stack[top++] = next; next = ch.z; }
+        if (h1) { if (next != kNoRef) st.stack[top++] = next; next = ch.y; }
+        if (h0) { if (next != kNoRef) st.stack[top++] = next; next = ch.x; }
+        ref = next != kNoRef ? next : (top ? st.stack[--top] : kNoRef);
+        if (is_leaf(ref) && leaf == kNoRef) {
+            leaf = ref;
+            ref = top ? st.stack[--top] : kNoRef;
+        }
+        if (!__any_sync(__activemask(), leaf == kNoRef)) break;
+    }
+    while (leaf != kNoRef && !occluded) {
+        int first, count;
+        leaf_range(leaf, first, count);
+        for (int k = 0; k < count; k++) {
+            if (COUNT) cnt->prims++;
+            if (anyhit_prim(S, first + k, r, tmin, tmax, ignore)) { occluded = true; break; }
+        }
+        leaf = kNoRef;
+        if (!occluded && is_leaf(ref)) {
+            leaf = ref;
+            ref = top ? st.stack[--top] : kNoRef;
+        }
+    }
+    st.top = top;
+    st.ref = ref;
+    st.leaf = leaf;
+    return occluded || (ref == kNoRef && leaf == kNoRef);
+}
+
+// Closest hit (h carries the running result); returns true when the ray is finished.
+template <bool COUNT>
+__device__ __forceinline__ bool bvh4_closest_round(const DevScene& S, const RayQ& r, float tmax, Hit& h, Bvh4State& st,
+                                                   TraceCounters* cnt) {
+    int top = st.top, ref = st.ref, leaf = st.leaf;
+    auto pop = [&]() -> int {
+        while (top > 0) {
+            --top;
+            if (st.stack_t[top] <= h.t) return st.stack[top];
+        }
+        return kNoRef;
+    };
+    while (ref >= 0) {
+        const float4* N = reinterpret_cast<const float4*>(S.nodes4 + ref);
+        const float4 lx = __ldg(N), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3), lz = __ldg(N + 4),
+                     hz = __ldg(N + 5);
+        const int4 ch = __ldg(reinterpret_cast<const int4*>(N + 6));
+        if (COUNT) cnt->nodes++;
+        const float lim = smin(tmax, h.t);
+        float t[4];
+        int c[4] = {ch.x, ch.y, ch.z, ch.w};
+        if (!slab4(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, 0.f, lim, t[0])) { t[0] = INFINITY; c[0] = kNoRef; }
+        if (!slab4(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, 0.f, lim, t[1])) { t[1] = INFINITY; c[1] = kNoRef; }
+        if (!slab4(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, 0.f, lim, t[2])) { t[2] = INFINITY; c[2] = kNoRef; }
+        if (!slab4(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, 0.f, lim, t[3])) { t[3] = INFINITY; c[3] = kNoRef; }
+        cswap(t[0], c[0], t[1], c[1]);
+        cswap(t[2], c[2], t[3], c[3]);
+        cswap(t[0], c[0], t[2], c[2]);
+        cswap(t[1], c[1], t[3], c[3]);
+        cswap(t[1], c[1], t[2], c[2]);
+        if (top + 3 > kStack4) { dev_flag_error(S.err, DEVERR_STACK); top = 0; ref = kNoRef; leaf = kNoRef; break; }
+#pragma unroll
+        for (int k = 3; k >= 1; k--)
+            if (c[k] != kNoRef) { st.stack[top] = c[k]; st.stack_t[top] = t[k]; top++; }
+        ref = c[0] != kNoRef ? c[0] : pop();
+        if (is_leaf(ref) && leaf == kNoRef) {
+            leaf = ref;
+            ref = pop();
+        }
+        if (!__any_sync(__activemask(), leaf == kNoRef)) break;
+    }
+    while (leaf != kNoRef) {
+        int first, count;
+        leaf_range(leaf, first, count);
+        for (int k = 0; k < count; k++) {
+            if (COUNT) cnt->prims++;
+            closest_prim(S, first + k, r, tmax, h);
+        }
+        leaf = kNoRef;
+        if (is_leaf(ref)) {
+            leaf = ref;
+            ref = pop();
+        }
+    }
+    st.top = top;
+    st.ref = ref;
+    st.leaf = leaf;
+    return ref == kNoRef && leaf == kNoRef;
+}
+
+// Warp-wide refill: lanes that need a ray take consecutive indices from *fetch.  Returns the index
+// for this lane (-1: none left) and must be called by all 32 lanes.
+__device__ __forceinline__ int warp_fetch(int* fetch, bool need, int n) {
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (!m) return -1;
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(fetch, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (!need) return -1;
+    const int idx = base + __popc(m & ((1u << lane) - 1u));
+    return idx < n ? idx : -1;
+}
+
 // Brute semantics (Brute.cpp:19-55): every object, no box tests.
 __device__ __forceinline__ Hit trace_closest_brute(const DevScene& S, const RayQ& r) {
     Hit h{INFINITY, 0.f, 0.f, -1};
