@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -297,6 +298,28 @@ int c2g_film_image(c2g_ctx* ctx, float* rgb) {
         for (int j = 0; j < W; j++) {
             size_t orig = (size_t)(H - i - 1) * W + j, dest = (size_t)i * W + j;
             for (int k = 0; k < 3; k++) rgb[3 * dest + k] = sum[3 * orig + k] / wgt[orig];
+        }
+    return C2G_OK;
+}
+
+int c2g_film_rgb8(c2g_ctx* ctx, float gamma, unsigned char* rgb8) {
+    if (!ctx || !rgb8) return fail(ctx, C2G_ERR_INVALID, "null argument");
+    if (!ctx->loaded) return fail(ctx, C2G_ERR_STATE, "no scene loaded");
+    int W = ctx->scene->cfg.width, H = ctx->scene->cfg.height;
+    std::vector<float> sum((size_t)W * H * 3), wgt((size_t)W * H);
+    int rc = c2g_film_download(ctx, sum.data(), wgt.data());
+    if (rc) return rc;
+    // GetImageDataRGB8 (FrameBuffer.cpp:42-56): flipped rows, pow(mean, gamma), clamp to
+    // [0, 0.999], floor(x * 256); a NaN mean (empty pixel) becomes 0
+    for (int i = 0; i < H; i++)
+        for (int j = 0; j < W; j++) {
+            size_t orig = (size_t)(H - i - 1) * W + j, dest = (size_t)i * W + j;
+            for (int k = 0; k < 3; k++) {
+                float c = std::pow(sum[3 * orig + k] / wgt[orig], gamma);
+                if (!(c == c)) c = 0.f;
+                c = std::min(std::max(c, 0.f), 0.999f);
+                rgb8[3 * dest + k] = (unsigned char)std::floor(c * 256);
+            }
         }
     return C2G_OK;
 }

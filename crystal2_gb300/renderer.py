@@ -125,6 +125,13 @@ class Context:
         self.check(self._lib.c2g_film_image(self._h, N.fptr(img)))
         return img
 
+    def image_rgb8(self, gamma: float = 1 / 2.2) -> np.ndarray:
+        """GetImageDataRGB8: (height, width, 3) uint8, rows flipped like image()."""
+        p = self.render_params()
+        out = np.zeros((p.height, p.width, 3), np.uint8)
+        self.check(self._lib.c2g_film_rgb8(self._h, float(gamma), out.ctypes.data_as(C.POINTER(C.c_ubyte))))
+        return out
+
     def stats(self) -> N.Stats:
         s = N.Stats()
         self.check(self._lib.c2g_get_stats(self._h, C.byref(s)))

@@ -142,6 +142,9 @@ int c2g_film_clear(c2g_ctx* ctx, void* stream);
 int c2g_film_download(c2g_ctx* ctx, float* rgb_sum, float* weight);
 /* FrameBuffer::GetImageDataRGB32F (FrameBuffer.cpp:58-75): sum/weight, rows flipped. */
 int c2g_film_image(c2g_ctx* ctx, float* rgb);
+/* GetImageDataRGB8(gamma) (FrameBuffer.cpp:42-56): rows flipped like c2g_film_image, each channel
+ * pow(mean, gamma) clamped to [0, 0.999] and scaled by 256; 3 bytes per pixel. */
+int c2g_film_rgb8(c2g_ctx* ctx, float gamma, unsigned char* rgb8);
 /* Per-pixel sum of squares of the samples (variance estimates for parity tests). */
 int c2g_film_download_m2(c2g_ctx* ctx, float* rgb_sumsq);
 int c2g_get_stats(c2g_ctx* ctx, c2g_stats* out);

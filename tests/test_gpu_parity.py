@@ -375,3 +375,20 @@ def test_oren_nayar_blinn_phong_vs_reference_and_oracle(tmp_path):
     gs = _per_sample(ctx_ref, p.spp)[:, z["py"], z["px"]].transpose(1, 0, 2)
     close = np.abs(gs - ref).max(-1) <= 1e-6 * (1 + np.abs(ref).max(-1))
     assert close.mean() >= 0.85
+
+
+def test_film_rgb8_follows_frame_buffer(tmp_path):
+    """c2g_film_rgb8 = GetImageDataRGB8 (FrameBuffer.cpp:42-56) restated: flipped rows,
+    pow(mean, gamma), clamp to [0, 0.999], floor(x * 256)."""
+    cp, sp = scenes.cornell(str(tmp_path / "c"), width=40, height=24, spp=4)
+    ctx = _ctx(cp, sp)
+    p = ctx.render_params()
+    ctx.render(p)
+    img = ctx.image().astype(np.float32)
+    for gamma in (1 / 2.2, 1.0):
+        got = ctx.image_rgb8(gamma)
+        c = np.power(img, np.float32(gamma))
+        c = np.where(np.isnan(c), 0, c)
+        want = np.floor(np.clip(c, 0, np.float32(0.999)) * 256).astype(np.uint8)
+        assert got.shape == (24, 40, 3)
+        assert np.array_equal(got, want)
