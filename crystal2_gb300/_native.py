@@ -99,6 +99,7 @@ SIGNATURES = {
     "c2g_film_download": (_I, [_P, _FP, _FP]),
     "c2g_film_image": (_I, [_P, _FP]),
     "c2g_film_rgb8": (_I, [_P, C.c_float, C.POINTER(C.c_ubyte)]),
+    "c2g_register_image": (_I, [_P, C.c_char_p, _I, _I, C.POINTER(C.c_ubyte)]),
     "c2g_film_download_m2": (_I, [_P, _FP]),
     "c2g_get_stats": (_I, [_P, C.POINTER(Stats)]),
     "c2g_set_counting": (_I, [_P, _I]),

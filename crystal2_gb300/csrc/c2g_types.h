@@ -49,6 +49,8 @@ struct alignas(16) Material {
     float ax, ay;          // roughness used directly as alpha (MicrofacetMaterial.cpp:18-42)
     float color[4];        // Color / Kd
     float ks[4];           // Ks (Plastic)
+    int tex;               // Kd texture (UVTexture) index, -1: the constant color
+    int pad[3];
 };
 
 enum LightType : int { LIGHT_AREA = 0, LIGHT_POINT = 1 };

@@ -29,6 +29,7 @@ struct c2g_ctx {
     bool loaded = false;       // scene uploaded to the device
     bool host_loaded = false;  // scene parsed and trees built on the host
     bool host_only = false;    // created with device < 0: no CUDA calls at all
+    ImageRegistry images;      // decoded images registered by path (textures, skybox faces)
     cudaStream_t stream = nullptr;
 };
 
@@ -70,7 +71,7 @@ int load_texts(c2g_ctx* ctx, const std::string& cfg, const std::string& scn, int
     ctx->host_loaded = false;
     try {
         auto s = std::make_unique<HostScene>();
-        load_scene(*s, cfg, scn);
+        load_scene(*s, cfg, scn, &ctx->images);
         ctx->scene = std::move(s);
     } catch (const SceneError& e) {
         return fail(ctx, e.code, e.what());
@@ -299,6 +300,16 @@ int c2g_film_image(c2g_ctx* ctx, float* rgb) {
             size_t orig = (size_t)(H - i - 1) * W + j, dest = (size_t)i * W + j;
             for (int k = 0; k < 3; k++) rgb[3 * dest + k] = sum[3 * orig + k] / wgt[orig];
         }
+    return C2G_OK;
+}
+
+int c2g_register_image(c2g_ctx* ctx, const char* path, int width, int height, const unsigned char* rgb8) {
+    if (!ctx || !path || !rgb8 || width <= 0 || height <= 0) return fail(ctx, C2G_ERR_INVALID, "invalid image");
+    Image im;
+    im.width = width;
+    im.height = height;
+    im.rgb.assign(rgb8, rgb8 + (size_t)width * height * 3);
+    ctx->images[path] = std::move(im);
     return C2G_OK;
 }
 

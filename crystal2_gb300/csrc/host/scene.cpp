@@ -1,4 +1,7 @@
 #include "scene.h"
+#include <cstdlib>
+#include <cmath>
+#include <cctype>
 
 #include <algorithm>
 #include <cstdio>
@@ -128,9 +131,64 @@ void store_m3(float* dst, const fm::M3& m) {
     }
 }
 
+// An 8-bit RGB image: a registered decode, else a binary PPM (P6, maxval 255) file.  stb_image, which
+// the reference uses (Texel.cpp:4-13), detects the format from the content; this loader reads PPM
+// content under any file name and leaves other formats to the caller's registry.
+Image load_image(const std::string& path, const ImageRegistry* reg) {
+    if (reg) {
+        auto it = reg->find(path);
+        if (it != reg->end()) return it->second;
+    }
+    std::string data = read_text_file(path);
+    Image im;
+    size_t pos = 0;
+    auto token = [&]() -> std::string {
+        while (pos < data.size()) {
+            char ch = data[pos];
+            if (ch == '#') { while (pos < data.size() && data[pos] != '\n') pos++; }
+            else if (std::isspace((unsigned char)ch)) pos++;
+            else break;
+        }
+        size_t b = pos;
+        while (pos < data.size() && !std::isspace((unsigned char)data[pos])) pos++;
+        return data.substr(b, pos - b);
+    };
+    if (data.size() < 2 || data[0] != 'P' || data[1] != '6')
+        throw SceneError(C2G_ERR_UNSUPPORTED, "Failed to load image: " + path +
+                                                 " (binary PPM only; register other formats decoded with c2g_register_image)");
+    pos = 2;
+    im.width = std::atoi(token().c_str());
+    im.height = std::atoi(token().c_str());
+    int maxval = std::atoi(token().c_str());
+    pos++;  // the single whitespace byte before the raster
+    size_t need = (size_t)im.width * im.height * 3;
+    if (im.width <= 0 || im.height <= 0 || maxval != 255 || data.size() < pos + need)
+        throw SceneError(C2G_ERR_PARSE, "Failed to load image: " + path);
+    im.rgb.assign(data.begin() + pos, data.begin() + pos + need);
+    return im;
+}
+
 struct Loader {
     HostScene& s;
-    explicit Loader(HostScene& sc) : s(sc) {}
+    const ImageRegistry* images = nullptr;
+    explicit Loader(HostScene& sc, const ImageRegistry* reg = nullptr) : s(sc), images(reg) {}
+
+    // ImageTexels::CreateImageTexels (Texel.cpp:4-38): texel = (byte / 255)^2.2 in float.
+    int add_texture(const std::string& path) {
+        Image im = load_image(path, images);
+        int idx = (int)s.tex_info.size() / 4;
+        s.tex_info.push_back(im.width);
+        s.tex_info.push_back(im.height);
+        s.tex_info.push_back((int)s.texels.size());
+        s.tex_info.push_back(0);
+        for (size_t i = 0; i < im.rgb.size(); i++) s.texels.push_back(std::pow((float)im.rgb[i] / 255.f, 2.2f));
+        return idx;
+    }
+    int texture_by_name(const std::string& name) {  // Scene::GetTextureByName (Scene.cpp:69-77)
+        auto it = s.tex_names.find(name);
+        if (it == s.tex_names.end()) throw SceneError(C2G_ERR_INVALID, "Texture name doesn't exist");
+        return it->second;
+    }
 
     int add_material(const Json& n) {
         Material m{};
@@ -139,10 +197,11 @@ struct Loader {
             V3 c = parse_vec3(n.at(key));
             m.color[0] = c.x; m.color[1] = c.y; m.color[2] = c.z; m.color[3] = 0.f;
         };
+        m.tex = -1;
         if (type == "Diffuse") {
-            if (n.has("Kd")) throw SceneError(C2G_ERR_UNSUPPORTED, "texture-mapped Diffuse (Kd) is not supported");
             m.type = MAT_DIFFUSE;
-            color("Color");
+            if (n.has("Kd")) m.tex = texture_by_name(n.at("Kd").as_string());  // UVTexture Kd
+            else color("Color");
         } else if (type == "Mirror") {
             m.type = MAT_MIRROR;
             color("Color");
@@ -170,9 +229,9 @@ struct Loader {
             else throw SceneError(C2G_ERR_INVALID, "Cannot find NDF Type: " + ndf);
         } else if (type == "Phong") {
             // PhongMaterial -> BlinnPhongReflection(color, K) (Material.cpp:86-99, PhongMaterial.cpp:11-19)
-            if (n.has("Kd")) throw SceneError(C2G_ERR_UNSUPPORTED, "texture-mapped Phong (Kd) is not supported");
             m.type = MAT_BLINNPHONG;
-            color("Color");
+            if (n.has("Kd")) m.tex = texture_by_name(n.at("Kd").as_string());
+            else color("Color");
             m.ior = (float)n.at("K").as_int();
         } else if (type == "OrenNayar") {
             // OrenNayarMaterial -> OrenNayarReflection(color, sigma) (Material.cpp:100-121); the
@@ -270,6 +329,7 @@ struct Loader {
                 ts.n1[0] = b.nrm.x; ts.n1[1] = b.nrm.y; ts.n1[2] = b.nrm.z; ts.n1[3] = dpdu.y;
                 ts.n2[0] = c.nrm.x; ts.n2[1] = c.nrm.y; ts.n2[2] = c.nrm.z; ts.n2[3] = dpdu.z;
                 s.tri_shade.push_back(ts);
+                for (const ObjVertex* v : {&a, &b, &c}) { s.tri_uv.push_back(v->uv[0]); s.tri_uv.push_back(v->uv[1]); }
                 out.push_back({SHAPE_TRI, (int)s.tri_shade.size() - 1});
             }
         } else {
@@ -362,7 +422,7 @@ void HostScene::object_box(int obj, float out[6]) const {
     }
 }
 
-void load_scene(HostScene& s, const std::string& config_text, const std::string& scene_text) {
+void load_scene(HostScene& s, const std::string& config_text, const std::string& scene_text, const ImageRegistry* images) {
     s = HostScene();
     auto cfgp = Json::parse(config_text);
     auto scnp = Json::parse(scene_text);
@@ -394,12 +454,18 @@ void load_scene(HostScene& s, const std::string& config_text, const std::string&
     }
     // Scene::CreateScene (Scene.cpp:23-45)
     const Json& sc = scn.at("Scene");
+    Loader ld(s, images);
+    // Scene::loadTextures (Scene.cpp:84-92): name -> UVTexture over the image's texels
     const Json& tex = sc.at("Textures");
-    (void)tex;
-    Loader ld(s);
+    if (tex.kind != Json::OBJECT) throw SceneError(C2G_ERR_INVALID, "Textures must be an object");
+    for (const auto& kv : tex.obj) s.tex_names[kv.first] = ld.add_texture(kv.second->at("Path").as_string());
     ld.load_objects(sc.at("Objects"));
-    if (sc.has("Skybox") && sc.at("Skybox").kind != Json::NUL)
-        throw SceneError(C2G_ERR_UNSUPPORTED, "skybox textures are not supported");
+    // Scene::loadSkybox (Scene.cpp:128-144): six faces <Path>/{pos,neg}{x,y,z}.jpg
+    if (sc.has("Skybox") && sc.at("Skybox").kind != Json::NUL) {
+        const std::string dir = sc.at("Skybox").at("Path").as_string();
+        const char* face[6] = {"posx.jpg", "negx.jpg", "posy.jpg", "negy.jpg", "posz.jpg", "negz.jpg"};
+        for (int k = 0; k < 6; k++) s.sky[k] = ld.add_texture(dir + "/" + face[k]);
+    }
     // Camera::CreateCamera (Camera.cpp:7-22) + PerspCamera ctor (PerspCamera.cpp:3-13)
     const Json& cam = scn.at("Camera");
     if (cam.at("Type").as_string() != "Normal") throw SceneError(C2G_ERR_INVALID, "Invalid Camera Type!");

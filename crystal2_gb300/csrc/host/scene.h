@@ -5,6 +5,7 @@
 #pragma once
 #include <memory>
 #include <stdexcept>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -38,14 +39,28 @@ struct HostScene {
     std::vector<float> quad_box;       // 6 per quadric (GetBoundingBox)
     std::vector<Material> mats;
     std::vector<Light> lights;         // Scene::_lights order
+    std::vector<float> tri_uv;         // 6 per triangle: texture coordinates of its vertices
+    std::vector<float> texels;         // RGB float texels of every texture (ImageTexels)
+    std::vector<int> tex_info;         // 4 per texture: width, height, first texel (float index), 0
+    std::map<std::string, int> tex_names;
+    int sky[6] = {-1, -1, -1, -1, -1, -1};  // skybox faces: +x, -x, +y, -y, +z, -z
 
     size_t num_objects() const { return objs.size(); }
     // Object bounding box (IIntersectable::GetBoundingBox) as min xyz, max xyz.
     void object_box(int obj, float out[6]) const;
 };
 
+// Decoded 8-bit RGB images the caller registered by path (c2g_register_image); scene texture and
+// skybox paths are looked up here before the file system.
+struct Image {
+    int width = 0, height = 0;
+    std::vector<unsigned char> rgb;
+};
+using ImageRegistry = std::map<std::string, Image>;
+
 // Parse config + scene JSON (already loaded as text).  Throws SceneError / JsonError.
-void load_scene(HostScene& s, const std::string& config_text, const std::string& scene_text);
+void load_scene(HostScene& s, const std::string& config_text, const std::string& scene_text,
+                const ImageRegistry* images = nullptr);
 std::string read_text_file(const std::string& path);  // throws SceneError(C2G_ERR_IO)
 
 // Halton sampler tables (HaltonSampler.cpp:164-229).

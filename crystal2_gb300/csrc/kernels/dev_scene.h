@@ -33,6 +33,10 @@ struct DevScene {
     const int* perm_off;          // table offsets
     uint64_t seed;
     int* err;                     // device error word (C2G_DEVERR_*)
+    const float2* tri_uv;         // 3 texture coordinates per scene triangle
+    const float* texels;          // RGB float texels of every texture, back to back
+    const int4* tex_info;         // per texture: width, height, first texel (float index), 0
+    int sky[6];                   // cubemap skybox faces (+x, -x, +y, -y, +z, -z), -1: none
 };
 
 // Shading buckets: 0..9 = MatType of the hit's material, 10 = no material, 11 = miss.

@@ -323,7 +323,10 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
         float3 beta = f3(b4), L = f3(L4);
         Hit h{h4.x, h4.y, h4.z, __float_as_int(h4.w)};
 
-        bool alive = valid && MT != kBucketMiss;  // miss: the path ends (no skybox)
+        bool alive = valid && MT != kBucketMiss;  // miss: the path ends
+        // a miss adds the skybox, if any (PathTracingIntegrator.cpp:39-46, DirectLightingIntegrator.cpp:34-38);
+        // not for a guided vertex's ray traced past the depth only for emitter MIS
+        if (MT == kBucketMiss && valid && S.sky[0] >= 0 && bounce < a.max_depth) L = L + beta * sky_lookup(S, rd);
         // a guided path's ray past the depth limit only collects the emission it reaches
         const bool emit_only = mis_emit && bounce >= a.max_depth;
         bool do_nee = false;
@@ -372,6 +375,8 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                 }
             } else {
                 bx = make_bxdf(S.mats[s.mat], s.front);
+                const int tex = S.mats[s.mat].tex;
+                if (tex >= 0) bx.R = tex_lookup(S, tex, surface_uv(S, ro, rd, h));  // Kd texture
                 bx.mtype = MT;  // compile-time material: the BxDF switches fold away
                 bx.flags = material_flags(MT);
                 fr.T = s.dpdu; fr.N = s.N; fr.B = s.dpdv;
@@ -893,6 +898,20 @@ int GpuScene::upload(const HostScene& s, int tree, const RefTree* ref, const Sah
     S.quads = upload_vec(s.quads, arena, sb_->owned, err, rc);
     if (rc) return rc;
     S.mats = upload_vec(s.mats, arena, sb_->owned, err, rc);
+    if (rc) return rc;
+    {
+        std::vector<float2> uv(s.tri_uv.size() / 2);
+        for (size_t k = 0; k < uv.size(); k++) uv[k] = make_float2(s.tri_uv[2 * k], s.tri_uv[2 * k + 1]);
+        S.tri_uv = upload_vec(uv, arena, sb_->owned, err, rc);
+        if (rc) return rc;
+        S.texels = upload_vec(s.texels, arena, sb_->owned, err, rc);
+        if (rc) return rc;
+        std::vector<int4> ti(s.tex_info.size() / 4);
+        for (size_t k = 0; k < ti.size(); k++)
+            ti[k] = make_int4(s.tex_info[4 * k], s.tex_info[4 * k + 1], s.tex_info[4 * k + 2], 0);
+        S.tex_info = upload_vec(ti, arena, sb_->owned, err, rc);
+        for (int k = 0; k < 6; k++) S.sky[k] = s.sky[k];
+    }
     if (rc) return rc;
     S.lights = upload_vec(s.lights, arena, sb_->owned, err, rc);
     if (rc) return rc;

@@ -95,6 +95,53 @@ __device__ __forceinline__ void make_surface(const DevScene& S, float3 o, float3
     }
 }
 
+// ---- textures (Texel.cpp:15-19, UVTexture.h, CubemapTexture.cpp:17-57) ------------------------
+// ImageTexels::GetTexel: uv clamped to [0, 0.99999], nearest texel, v measured from the last row.
+__device__ __forceinline__ float3 tex_lookup(const DevScene& S, int tex, float2 uv) {
+    const int4 ti = __ldg(S.tex_info + tex);
+    const float u = fminf(fmaxf(uv.x, 0.f), .99999f), v = fminf(fmaxf(uv.y, 0.f), .99999f);
+    const int x = (int)__fmul_rn(u, (float)ti.x), y = ti.y - (int)__fmul_rn(v, (float)ti.y) - 1;
+    const float* p = S.texels + ti.z + 3 * ((size_t)y * ti.x + x);
+    return f3(__ldg(p), __ldg(p + 1), __ldg(p + 2));
+}
+
+// ImageCubemapTexture::Evaluate(dir): face by the dominant axis, face uv in [0, 1].
+__device__ __forceinline__ float3 sky_lookup(const DevScene& S, float3 p) {
+    const float ax = fabsf(p.x), ay = fabsf(p.y), az = fabsf(p.z);
+    int id;
+    float2 uv;
+    if (ax >= ay && ax >= az) { id = p.x >= 0 ? 0 : 1; uv = make_float2(__fdiv_rn(-p.z, p.x), __fdiv_rn(p.y, ax)); }
+    else if (ay >= az) { id = p.y >= 0 ? 2 : 3; uv = make_float2(__fdiv_rn(p.x, ay), __fdiv_rn(-p.z, p.y)); }
+    else { id = p.z >= 0 ? 4 : 5; uv = make_float2(__fdiv_rn(p.x, p.z), __fdiv_rn(p.y, az)); }
+    uv.x = __fadd_rn(__fmul_rn(uv.x, 0.5f), 0.5f);
+    uv.y = __fadd_rn(__fmul_rn(uv.y, 0.5f), 0.5f);
+    return tex_lookup(S, S.sky[id], uv);
+}
+
+// Texture coordinates of a hit: triangles interpolate the vertex uvs at (1-u-v, u, v)
+// (Triangle.cpp:9-16,43), spheres use (atan2(-z, x) / pi, acos(y / r) / pi + 1) of the local hit
+// (Sphere.cpp:55-59), disks (|hit| / r, (atan2(-z, x) + pi) / 2pi) (Disk.cpp:61-62).
+__device__ __forceinline__ float2 surface_uv(const DevScene& S, float3 o, float3 d, const Hit& h) {
+    const ObjInfo oi = S.objs[h.obj];
+    if (oi.type == SHAPE_TRI) {
+        const float2* t = S.tri_uv + 3 * oi.shape;
+        const float2 t0 = __ldg(t), t1 = __ldg(t + 1), t2 = __ldg(t + 2);
+        const float b0 = __fsub_rn(__fsub_rn(1.f, h.u), h.v), b1 = h.u, b2 = h.v;
+        return make_float2(__fadd_rn(__fadd_rn(__fmul_rn(b0, t0.x), __fmul_rn(b1, t1.x)), __fmul_rn(b2, t2.x)),
+                           __fadd_rn(__fadd_rn(__fmul_rn(b0, t0.y), __fmul_rn(b1, t1.y)), __fmul_rn(b2, t2.y)));
+    }
+    const Quadric& q = S.quads[oi.shape];
+    RayQ r;
+    r.o = o;
+    r.d = d;
+    float3 P, dl;
+    quadric_local(q, r, P, dl);
+    const float3 hp = P + dl * h.t;
+    if (oi.type == SHAPE_SPHERE)
+        return make_float2(atan2f(-hp.z, hp.x) / kPiF, acosf(hp.y / q.c[3]) / kPiF + 1.0f);
+    return make_float2(length(hp) / q.c[3], (atan2f(-hp.z, hp.x) + kPiF) / kTwoPiF);
+}
+
 // SurfaceInteraction::SpawnRay / SpawnRayTo (SurfaceInteraction.cpp:12-22)
 __device__ __forceinline__ float3 spawn_origin(const Surface& s, float3 dir) {
     bool back = dot(dir, s.N) < 0;

@@ -61,6 +61,12 @@ class Context:
         self.close()
 
     # ---- scene
+    def register_image(self, path: str, rgb8: np.ndarray) -> None:
+        """Decoded (height, width, 3) uint8 pixels used for a texture or skybox file path."""
+        a = np.ascontiguousarray(rgb8, np.uint8)
+        self.check(self._lib.c2g_register_image(self._h, path.encode(), a.shape[1], a.shape[0],
+                                                a.ctypes.data_as(C.POINTER(C.c_ubyte))))
+
     def load(self, config_path: str, scene_path: str, tree: int = N.TREE_SAH) -> None:
         self.check(self._lib.c2g_load_json(self._h, config_path.encode(), scene_path.encode(), tree))
 

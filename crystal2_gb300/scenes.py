@@ -12,6 +12,8 @@ reference ships scenes whose OBJ models are absent, so the workloads are generat
 * ``many_material``  400 subdivision-4 icospheres (5120 triangles each) on a jittered 20 x 20 grid
                      over a 40 x 40 ground quad, five material families, two area quads of radiance
                      20 and a point light of intensity 50; 1920 x 1080, 256 spp, depth 16.
+* ``textured_yard``  UV-textured floor quad, sphere and disk (Diffuse and Phong ``Kd`` textures),
+                     an area light, a point light and a six-face skybox; textures are binary PPM.
 * ``slit_room``      closed 10 x 4 x 10 room lit through a 0.2-wide slit by an exterior 2 x 2 light
                      of radiance 200; 512 x 512 value-noise heightfield floor; GGX everywhere.
 
@@ -52,6 +54,32 @@ def write_obj(path: str, V: np.ndarray, N: np.ndarray, F: np.ndarray, FN: np.nda
         ff = np.stack([F[:, 0], FN[:, 0], F[:, 1], FN[:, 1], F[:, 2], FN[:, 2]], axis=1)
         fh.write("\n".join("f %d//%d %d//%d %d//%d" % tuple(r) for r in ff.tolist()))
         fh.write("\n")
+
+
+def write_obj_uv(path: str, V, N, T, F) -> None:
+    """Triangles F (m,3, 0-based) that index positions V, texture coordinates T and normals N alike."""
+    V = np.asarray(V, dtype=np.float32)
+    N = np.asarray(N, dtype=np.float32)
+    T = np.asarray(T, dtype=np.float32)
+    F = np.asarray(F, dtype=np.int64) + 1
+    with open(path, "w") as fh:
+        for r in V.tolist():
+            fh.write("v %.9g %.9g %.9g\n" % tuple(r))
+        for r in T.tolist():
+            fh.write("vt %.9g %.9g\n" % tuple(r))
+        for r in N.tolist():
+            fh.write("vn %.9g %.9g %.9g\n" % tuple(r))
+        for r in F.tolist():
+            fh.write("f %d/%d/%d %d/%d/%d %d/%d/%d\n" % (r[0], r[0], r[0], r[1], r[1], r[1], r[2], r[2], r[2]))
+
+
+def write_ppm(path: str, rgb) -> None:
+    """Binary PPM (P6, maxval 255) of an (h, w, 3) uint8 array; row 0 is the top of the image."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.uint8)
+    h, w, _ = rgb.shape
+    with open(path, "wb") as fh:
+        fh.write(b"P6\n%d %d\n255\n" % (w, h))
+        fh.write(rgb.tobytes())
 
 
 def quad_obj(path: str, corners, normal) -> None:
@@ -134,14 +162,27 @@ def point_light(pos, flux) -> dict:
     return {"Type": "Light", "LightType": "Point", "Position": _v(pos), "Flux": _v(flux)}
 
 
-def write_scene(out_dir: str, cfg: dict, cam: dict, objects: list, name: str = "scene") -> tuple[str, str]:
+def diffuse_tex(name: str) -> dict:
+    return {"Type": "Diffuse", "Kd": name}
+
+
+def phong_tex(name: str, k: int) -> dict:
+    return {"Type": "Phong", "Kd": name, "K": int(k)}
+
+
+def write_scene(out_dir: str, cfg: dict, cam: dict, objects: list, name: str = "scene",
+                textures: dict | None = None, skybox: str | None = None) -> tuple[str, str]:
+    """textures: name -> image path (the scene's "Textures"); skybox: folder of the six faces."""
     os.makedirs(out_dir, exist_ok=True)
     cpath = os.path.join(out_dir, f"{name}_config.json")
     spath = os.path.join(out_dir, f"{name}.json")
     with open(cpath, "w") as fh:
         json.dump(cfg, fh, indent=1)
+    sc = {"Textures": {k: {"Path": v} for k, v in (textures or {}).items()}, "Objects": objects}
+    if skybox is not None:
+        sc["Skybox"] = {"Path": skybox}
     with open(spath, "w") as fh:
-        json.dump({"Camera": cam, "Scene": {"Textures": {}, "Objects": objects}}, fh, indent=1)
+        json.dump({"Camera": cam, "Scene": sc}, fh, indent=1)
     return cpath, spath
 
 
@@ -253,6 +294,48 @@ def brdf_box(out_dir: str, width=48, height=48, spp=16, depth=6, accel="BVH", th
     ]
     cfg = config_json(width, height, spp, depth, accel=accel, threads=threads)
     return write_scene(d, cfg, camera((0, 1, -3.8), (0, 1, 0), 40), objs, "brdf_box")
+
+
+def textured_yard(out_dir: str, width=64, height=48, spp=16, depth=6, accel="BVH", threads=8, seed=5,
+                  integrator="PathTracer", skybox=True) -> tuple[str, str]:
+    """Open scene for the texture and skybox paths: a 4 x 4 floor quad whose uvs run from -0.1 to 1.1
+    (the texel lookup clamps), a sphere and a disk with Diffuse / Phong ``Kd`` textures, a 1 x 1 area
+    light, a point light, and a six-face skybox seen above the horizon.  Textures are seeded random
+    binary PPM images; the faces are named ``posx.jpg`` ... ``negz.jpg`` as the scene format expects
+    (both loaders detect PPM by content)."""
+    d = os.path.abspath(out_dir)
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    checker = np.kron((np.indices((8, 8)).sum(0) % 2)[..., None], np.ones((2, 2, 1)))  # 16 x 16
+    ca, cb = rng.integers(40, 250, 3), rng.integers(10, 120, 3)
+    write_ppm(os.path.join(d, "floor.ppm"), np.where(checker > 0, ca, cb))
+    write_ppm(os.path.join(d, "noise.ppm"), rng.integers(0, 256, (24, 32, 3)))
+    ramp = np.linspace(20, 235, 16)
+    write_ppm(os.path.join(d, "ramp.ppm"), np.stack([np.tile(ramp, (12, 1)), np.tile(ramp[:12, None], (1, 16)),
+                                                     np.full((12, 16), 90.0)], axis=-1))
+    sky = os.path.join(d, "sky")
+    os.makedirs(sky, exist_ok=True)
+    for k, face in enumerate(("posx", "negx", "posy", "negy", "posz", "negz")):
+        tint = np.array([60 + 30 * k, 200 - 25 * k, 120 + 15 * (k % 3)])
+        img = np.clip(tint + rng.integers(-40, 40, (8, 8, 3)), 0, 255)
+        write_ppm(os.path.join(sky, face + ".jpg"), img)
+    fp = os.path.join(d, "floor.obj")
+    write_obj_uv(fp, [(-2, 0, -1), (2, 0, -1), (2, 0, 3), (-2, 0, 3)], [(0, 1, 0)] * 4,
+                 [(-0.1, -0.1), (1.1, -0.1), (1.1, 1.1), (-0.1, 1.1)], [[0, 2, 1], [0, 3, 2]])
+    lp = os.path.join(d, "light.obj")
+    quad_obj(lp, [(-0.5, 2.5, 0.5), (-0.5, 2.5, 1.5), (0.5, 2.5, 1.5), (0.5, 2.5, 0.5)], (0, -1, 0))
+    objs = [
+        mesh(fp, diffuse_tex("floor")),
+        sphere((-0.6, 0.5, 1.0), 0.5, diffuse_tex("noise"), rotation=(0, 35, 0)),
+        disk((0.8, 0.6, 1.2), 0.5, phong_tex("ramp", 12), rotation=(-70, 20, 0)),
+        mesh(lp, diffuse((0, 0, 0)), area_light=(6, 6, 6)),
+        point_light((1.5, 1.8, -0.5), (3, 3, 3)),
+    ]
+    cfg = config_json(width, height, spp, depth, accel=accel, threads=threads, integrator=integrator)
+    tex = {"floor": os.path.join(d, "floor.ppm"), "noise": os.path.join(d, "noise.ppm"),
+           "ramp": os.path.join(d, "ramp.ppm")}
+    return write_scene(d, cfg, camera((0, 1.0, -2.5), (0, 0.7, 1.0), 60), objs, "textured_yard",
+                       textures=tex, skybox=sky if skybox else None)
 
 
 def material_box(out_dir: str, width=64, height=64, spp=16, depth=8, accel="BVH", threads=8) -> tuple[str, str]:

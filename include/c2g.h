@@ -122,6 +122,11 @@ const char* c2g_version(void);
 int c2g_load_json(c2g_ctx* ctx, const char* config_path, const char* scene_path, int tree);
 /* Same, from in-memory JSON text. */
 int c2g_load_json_text(c2g_ctx* ctx, const char* config_json, const char* scene_json, int tree);
+/* Register a decoded 8-bit RGB image (width x height x 3 bytes, row 0 = the file's first row) under
+ * a path: scene textures ("Textures": {name: {"Path": ...}}) and skybox faces (<Path>/posx.jpg ...)
+ * with that path use it instead of reading the file.  Stands in for the reference's stb_image
+ * decode (Texel.cpp:4-13); the library itself reads binary PPM files.  Register before loading. */
+int c2g_register_image(c2g_ctx* ctx, const char* path, int width, int height, const unsigned char* rgb8);
 /* Rebuild the acceleration structure of the loaded scene (BVH::Build, BVH.cpp:45-54). */
 int c2g_bvh_build(c2g_ctx* ctx, int tree);
 /* Render parameters implied by the loaded config (Width, Height, SamplesPerPixel, Depth ...). */

@@ -259,8 +259,9 @@ static V3 vec3(const JNode& n) { return V3((float)n.a.at(0)->F(), (float)n.a.at(
 // ---------------------------------------------------------------- scene
 enum { TRI = 0, SPH = 1, DSK = 2 };
 enum { M_DIFF, M_MIRROR, M_GLASS_R, M_GLASS_S, M_MICRO_GGX, M_MICRO_BECK, M_PLAST_GGX, M_PLAST_BECK, M_OREN, M_PHONG };
-struct Mat { int type; V3 R, S; float ax = 0, ay = 0, ior = 1; };
-struct Tri { V3 p[3], n[3]; V3 dpdu; };
+struct Mat { int type; V3 R, S; float ax = 0, ay = 0, ior = 1; int tex = -1; };
+struct Tri { V3 p[3], n[3]; V3 dpdu; float uv[6]; };
+struct Tex { int w, h; std::vector<V3> texels; };  // ImageTexels (Texel.cpp)
 struct Quad { V3 pos; float r; M3 l2w, w2l; };
 struct Obj { int type, shape, mat, light; };
 struct Light { int type; int obj; int st, si; V3 Le, pos; float area; bool zero; };
@@ -278,6 +279,9 @@ struct Scene {
     std::vector<Mat> mats;
     std::vector<Obj> objs;
     std::vector<Light> lights;
+    std::vector<Tex> texs;
+    std::map<std::string, int> tex_names;
+    int sky[6] = {-1, -1, -1, -1, -1, -1};
     std::vector<Box> boxes;
     std::vector<int> order;
     std::vector<Node> nodes;
@@ -325,10 +329,78 @@ static void read_obj(const std::string& path, std::vector<V3>& pos, std::vector<
     fclose(f);
 }
 
+// ImageTexels::CreateImageTexels + ImageTexels ctor (Texel.cpp:4-38).  The reference decodes with
+// stb_image, which picks the format from the content; the restatement reads binary PPM (P6, 255).
+static int add_tex(Scene& s, const std::string& path) {
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) throw std::runtime_error("Failed to load image: " + path);
+    std::string d;
+    char buf[65536];
+    size_t k;
+    while ((k = fread(buf, 1, sizeof buf, f)) > 0) d.append(buf, k);
+    fclose(f);
+    if (d.size() < 2 || d[0] != 'P' || d[1] != '6') throw std::runtime_error("not a binary PPM: " + path);
+    size_t pos = 2;
+    int hdr[3];
+    for (int i = 0; i < 3; i++) {
+        for (;;) {
+            while (pos < d.size() && isspace((unsigned char)d[pos])) pos++;
+            if (pos < d.size() && d[pos] == '#') { while (pos < d.size() && d[pos] != '\n') pos++; continue; }
+            break;
+        }
+        hdr[i] = 0;
+        while (pos < d.size() && isdigit((unsigned char)d[pos])) hdr[i] = hdr[i] * 10 + (d[pos++] - '0');
+    }
+    pos++;
+    Tex t;
+    t.w = hdr[0]; t.h = hdr[1];
+    if (t.w <= 0 || t.h <= 0 || hdr[2] != 255 || d.size() < pos + (size_t)t.w * t.h * 3)
+        throw std::runtime_error("bad PPM: " + path);
+    for (size_t i = 0; i < (size_t)t.w * t.h; i++) {
+        V3 c;
+        c.x = std::pow((float)(unsigned char)d[pos + 3 * i] / 255.f, 2.2f);
+        c.y = std::pow((float)(unsigned char)d[pos + 3 * i + 1] / 255.f, 2.2f);
+        c.z = std::pow((float)(unsigned char)d[pos + 3 * i + 2] / 255.f, 2.2f);
+        t.texels.push_back(c);
+    }
+    s.texs.push_back(t);
+    return (int)s.texs.size() - 1;
+}
+
+// ImageTexels::GetTexel (Texel.cpp:15-19): nearest texel, uv clamped to [0, .99999], v flipped.
+static V3 texel(const Scene& s, int tex, float u, float v) {
+    const Tex& t = s.texs[tex];
+    u = std::min(std::max(u, 0.f), .99999f);
+    v = std::min(std::max(v, 0.f), .99999f);
+    int x = (int)(u * t.w), y = t.h - (int)(v * t.h) - 1;
+    return t.texels[(size_t)y * t.w + x];
+}
+
+// ImageCubemapTexture::Evaluate via XYZ2CubeUV (CubemapTexture.cpp:24-58)
+static V3 sky(const Scene& s, V3 p) {
+    float ax = std::fabs(p.x), ay = std::fabs(p.y), az = std::fabs(p.z);
+    int id;
+    float u, v;
+    if (ax >= ay && ax >= az) { id = p.x >= 0 ? 0 : 1; u = -p.z / p.x; v = p.y / ax; }
+    else if (ay >= az) { id = p.y >= 0 ? 2 : 3; u = p.x / ay; v = -p.z / p.y; }
+    else { id = p.z >= 0 ? 4 : 5; u = p.x / p.z; v = p.y / az; }
+    return texel(s, s.sky[id], u * 0.5f + 0.5f, v * 0.5f + 0.5f);
+}
+
+static int tex_by_name(const Scene& s, const std::string& name) {  // Scene::GetTextureByName
+    auto it = s.tex_names.find(name);
+    if (it == s.tex_names.end()) throw std::runtime_error("Texture name doesn't exist");
+    return it->second;
+}
+
 static int add_mat(Scene& s, const JNode& n) {
     Mat m;
     std::string t = n.m("Type").s;
-    if (t == "Diffuse") { m.type = M_DIFF; m.R = vec3(n.m("Color")); }
+    if (t == "Diffuse") {
+        m.type = M_DIFF;
+        if (n.has("Kd")) m.tex = tex_by_name(s, n.m("Kd").s);
+        else m.R = vec3(n.m("Color"));
+    }
     else if (t == "Mirror") { m.type = M_MIRROR; m.R = vec3(n.m("Color")); }
     else if (t == "Glass") {
         m.R = vec3(n.m("Color"));
@@ -350,7 +422,8 @@ static int add_mat(Scene& s, const JNode& n) {
         m.ior = (float)n.m("Sigma").F();
     } else if (t == "Phong") {      // Material.cpp:86-99 -> BlinnPhongReflection(color, K)
         m.type = M_PHONG;
-        m.R = vec3(n.m("Color"));
+        if (n.has("Kd")) m.tex = tex_by_name(s, n.m("Kd").s);
+        else m.R = vec3(n.m("Color"));
         m.ior = (float)n.m("K").I();
     } else throw std::runtime_error("material " + t + " not restated");
     s.mats.push_back(m);
@@ -381,6 +454,9 @@ static void load(Scene& s, const std::string& cfgp, const std::string& scnp) {
     s.closest_box = acc != "Brute";
     s.depth = (int)cfg->m("Integrator").m("Depth").I();
     s.direct = cfg->m("Integrator").m("Type").s == "DirectLight";
+    // Scene::CreateScene (Scene.cpp:23-45): textures, objects, then the skybox
+    const JNode& texn = scn->m("Scene").m("Textures");
+    for (auto& kv : texn.o) s.tex_names[kv.first] = add_tex(s, kv.second->m("Path").s);
     const JNode& objs = scn->m("Scene").m("Objects");
     for (auto& np : objs.a) {
         const JNode& n = *np;
@@ -423,6 +499,7 @@ static void load(Scene& s, const std::string& cfgp, const std::string& scnp) {
                 Tri t;
                 for (int k = 0; k < 3; k++) { t.p[k] = P[f + k]; t.n[k] = Nn[f + k]; }
                 const float* u = &UV[2 * f];
+                for (int k = 0; k < 6; k++) t.uv[k] = u[k];
                 float a00 = u[0] - u[4], a01 = u[1] - u[5], a10 = u[2] - u[4], a11 = u[3] - u[5];
                 float ood = 1.0f / (a00 * a11 - a10 * a01);
                 float i00 = a11 * ood, i01 = -a01 * ood, i10 = -a10 * ood, i11 = a00 * ood;
@@ -452,6 +529,12 @@ static void load(Scene& s, const std::string& cfgp, const std::string& scnp) {
         }
     }
     // camera
+    // Scene::loadSkybox (Scene.cpp:128-144)
+    if (scn->m("Scene").has("Skybox") && scn->m("Scene").m("Skybox").k != JNode::NUL) {
+        const std::string dir = scn->m("Scene").m("Skybox").m("Path").s;
+        const char* face[6] = {"posx.jpg", "negx.jpg", "posy.jpg", "negy.jpg", "posz.jpg", "negz.jpg"};
+        for (int k = 0; k < 6; k++) s.sky[k] = add_tex(s, dir + "/" + face[k]);
+    }
     const JNode& cam = scn->m("Camera");
     V3 la = vec3(cam.m("LookAt")), up = vec3(cam.m("Up")), eye = vec3(cam.m("Position"));
     float fov = (float)(cam.m("FOV").F() / 180.f * PI);
@@ -531,22 +614,32 @@ static void build_tree(Scene& s) {
 }
 
 // ---------------------------------------------------------------- Halton
+// Both tables are built once by a thread-safe static initialiser (render threads may race to the
+// first call).
 static int prime(int i) {
-    static std::vector<int> P;
-    if (P.empty()) for (int v = 2; (int)P.size() < 100; v++) { bool ok = true; for (int d = 2; d * d <= v; d++) if (v % d == 0) { ok = false; break; } if (ok) P.push_back(v); }
+    static const std::vector<int> P = [] {
+        std::vector<int> p;
+        for (int v = 2; (int)p.size() < 100; v++) {
+            bool ok = true;
+            for (int d = 2; d * d <= v; d++) if (v % d == 0) { ok = false; break; }
+            if (ok) p.push_back(v);
+        }
+        return p;
+    }();
     return P[i];
 }
 static const std::vector<std::vector<int>>& perm_tables() {
-    static std::vector<std::vector<int>> T;
-    if (T.empty()) {
+    static const std::vector<std::vector<int>> T = [] {
+        std::vector<std::vector<int>> tabs;
         std::mt19937 mt;
         for (int i = 0; i < 100; i++) {
             std::vector<int> t(prime(i));
             for (int j = 0; j < prime(i); j++) t[j] = j;
             std::shuffle(t.begin(), t.end(), mt);
-            T.push_back(t);
+            tabs.push_back(t);
         }
-    }
+        return tabs;
+    }();
     return T;
 }
 static void extgcd(uint64_t a, uint64_t b, uint64_t& d, uint64_t& x, uint64_t& y) {
@@ -639,6 +732,7 @@ struct Hit {
     int obj = -1;
     V3 pos, N, dpdu, dpdv;
     bool front = false;
+    float u = 0, v = 0;  // texture coordinates (SurfaceInteraction UV)
 };
 static V3 tri_normal(const Tri& t, float u, float v) {
     V3 b(1 - u - v, u, v);
@@ -661,6 +755,10 @@ static bool shape_intersect(const Scene& s, int type, int idx, const Ray& r, Hit
                 if (!zero(tt)) { dpdu = normalize(tt); break; }
             }
         h.t = res.z; h.pos = r.o + r.d * res.z; h.N = N; h.dpdu = dpdu; h.dpdv = cross(N, dpdu);
+        // bary_interp (Triangle.cpp:13-16, 43)
+        float b0 = 1 - res.x - res.y, b1 = res.x, b2 = res.y;
+        h.u = b0 * t.uv[0] + b1 * t.uv[2] + b2 * t.uv[4];
+        h.v = b0 * t.uv[1] + b1 * t.uv[3] + b2 * t.uv[5];
         return true;
     }
     const Quad& q = s.quads[idx];
@@ -684,6 +782,8 @@ static bool shape_intersect(const Scene& s, int type, int idx, const Ray& r, Hit
         h.N = mul(q.l2w, N);
         h.dpdv = cross(h.N, h.dpdu);
         h.t = t;
+        h.u = std::atan2(-hp.z, hp.x) / PI;  // Sphere.cpp:57-58
+        h.v = std::acos(hp.y / q.r) / PI + 1.0f;
         return true;
     }
     if (d.y == 0.f) return false;
@@ -698,6 +798,8 @@ static bool shape_intersect(const Scene& s, int type, int idx, const Ray& r, Hit
     h.N = N;
     h.dpdu = normalize(q.pos - h.pos);
     h.dpdv = cross(N, h.dpdu);
+    h.u = length(hit) / q.r;  // Disk.cpp:61-62
+    h.v = (std::atan2(-hit.z, hit.x) + PI) / TWO_PI;
     h.t = t;
     return true;
 }
@@ -1144,7 +1246,10 @@ static V3 evaluate(const Scene& s, Ray ray, Sampler& smp) {
     V3 beta(1, 1, 1), L(0, 0, 0);
     for (int bounce = 0; bounce < s.depth; bounce++) {
         Hit h;
-        if (!intersect(s, ray, h)) break;
+        if (!intersect(s, ray, h)) {
+            if (s.sky[0] >= 0) L = L + beta * sky(s, ray.d);  // PathTracingIntegrator.cpp:39-46
+            break;
+        }
         const Obj& ob = s.objs[h.obj];
         if (lightPath && ob.light >= 0) {
             V3 na = h.front ? h.N : -h.N;
@@ -1152,6 +1257,7 @@ static V3 evaluate(const Scene& s, Ray ray, Sampler& smp) {
         }
         if (ob.mat < 0) { ray = Ray{spawn(h, ray.d), ray.d}; continue; }
         BxDF b = make_bxdf(s.mats[ob.mat], h.front);
+        if (s.mats[ob.mat].tex >= 0) b.R = texel(s, s.mats[ob.mat].tex, h.u, h.v);  // UVTexture Kd
         Frame fr{h.dpdu, h.N, h.dpdv};
         V3 wo = -ray.d;
         // UniformSampleAllLights
@@ -1235,7 +1341,7 @@ static V3 evaluate_direct(const Scene& s, Ray ray, Sampler& smp) {
     if (s.depth <= 0) return L;
     for (int hop = 0; hop < 1 << 20; hop++) {
         Hit h;
-        if (!intersect(s, ray, h)) return L;
+        if (!intersect(s, ray, h)) return s.sky[0] >= 0 ? L + sky(s, ray.d) : L;  // DirectLightingIntegrator.cpp:34-38
         const Obj& ob = s.objs[h.obj];
         if (ob.light >= 0) {
             V3 na = h.front ? h.N : -h.N;
@@ -1247,6 +1353,7 @@ static V3 evaluate_direct(const Scene& s, Ray ray, Sampler& smp) {
             continue;
         }
         BxDF b = make_bxdf(s.mats[ob.mat], h.front);
+        if (s.mats[ob.mat].tex >= 0) b.R = texel(s, s.mats[ob.mat].tex, h.u, h.v);  // UVTexture Kd
         Frame fr{h.dpdu, h.N, h.dpdv};
         V3 wo = -ray.d;
         float lx = smp.get(), ly = smp.get(), bx = smp.get(), by = smp.get();

@@ -15,7 +15,9 @@ Fixtures:
   isect_<scene>.npz  Scene::Intersect (object, t) and Scene::IntersectTest results for seeded rays
   bsdf.npz       BSDF f/pdf and sampled (f, wi, pdf, type) for every material kind
   render_<scene>.npz per-sample radiance of a pixel subset and the per-pixel mean image
-                 (cornell, material_box, spheres, direct_cornell, brdf_box: Oren-Nayar + Blinn-Phong)
+                 (cornell, material_box, spheres, direct_cornell, brdf_box: Oren-Nayar + Blinn-Phong,
+                 textured_yard[_direct]: uv textures and the cubemap skybox; ``--only-textured``
+                 regenerates just these two)
 """
 from __future__ import annotations
 
@@ -95,9 +97,32 @@ def bsdf_kind(name: str) -> str:
     return "MicroGGX" if name == "MicroGGXAniso" else name
 
 
+def render_fixture(out: str, name: str, cp: str, sp: str, row_step: int = 5) -> None:
+    """Mean and second moment of every pixel and the per-sample radiance of 16 pixels."""
+    r = B.ref_open(cp, sp)
+    s, q, _ = r.render_region(0, 0, r.W, r.H)
+    px = np.arange(0, r.W, 3)[:16].astype(np.int32)
+    py = ((np.arange(px.shape[0]) * row_step) % r.H).astype(np.int32)
+    np.savez_compressed(os.path.join(out, f"render_{name}.npz"), mean=(s / r.spp).astype(np.float32),
+                        m2=(q / r.spp).astype(np.float32), spp=r.spp, px=px, py=py, samples=r.render_samples(px, py))
+    r.close()
+
+
+def textured_goldens(out: str, work: str) -> None:
+    """UV textures (Texel.cpp, UVTexture.h) and the cubemap skybox (CubemapTexture.cpp) under both
+    integrators."""
+    cp, sp = scenes.textured_yard(os.path.join(work, "textured_yard"))
+    render_fixture(out, "textured_yard", cp, sp)
+    cp, sp = scenes.textured_yard(os.path.join(work, "textured_yard_direct"), integrator="DirectLight")
+    render_fixture(out, "textured_yard_direct", cp, sp)
+
+
 def main() -> None:
     out = HERE
     work = tempfile.mkdtemp(prefix="c2g_golden_")
+    if "--only-textured" in sys.argv:
+        textured_goldens(out, work)
+        return
     rng = np.random.default_rng(0)
     # Halton
     H = {}
@@ -171,6 +196,7 @@ def main() -> None:
                 key = f"{name}_{front}_{flags}"
                 Bz[key + "_fe"], Bz[key + "_pe"], Bz[key + "_fs"], Bz[key + "_ws"], Bz[key + "_ps"], Bz[key + "_ts"] = fe, pe, fs, ws, ps, ts
     np.savez_compressed(os.path.join(out, "bsdf.npz"), **Bz)
+    textured_goldens(out, work)
     print("goldens written to", out)
 
 

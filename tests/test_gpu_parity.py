@@ -377,6 +377,32 @@ def test_oren_nayar_blinn_phong_vs_reference_and_oracle(tmp_path):
     assert close.mean() >= 0.85
 
 
+@pytest.mark.parametrize("integrator,name", [("PathTracer", "textured_yard"), ("DirectLight", "textured_yard_direct")])
+def test_textures_and_skybox_vs_reference_and_oracle(tmp_path, integrator, name):
+    """Kd textures on a mesh (interpolated vertex uvs), a sphere and a disk, and the cubemap skybox
+    on escaping rays: image means within 3 standard errors of the reference's golden render and
+    per-sample radiance equal to the oracle's."""
+    cp, sp = scenes.textured_yard(str(tmp_path / "t"), integrator=integrator)
+    ctx = _ctx(cp, sp)
+    p = ctx.render_params()
+    ctx.render(p)
+    s, w = ctx.film()
+    m2 = ctx.film_m2()
+    z = np.load(os.path.join(GOLDEN, f"render_{name}.npz"))
+    gm = s / w[..., None]
+    gv = np.maximum(m2 / w[..., None] - gm ** 2, 0) / p.spp
+    rv = np.maximum(z["m2"] - z["mean"] ** 2, 0) / int(z["spp"])
+    zt = (gm - z["mean"]) / np.sqrt(gv + rv + 1e-12)
+    assert (np.abs(zt) > 3).mean() <= 0.01
+    assert abs(gm.mean() - z["mean"].mean()) <= 3 * np.sqrt((gv + rv).sum()) / gm.size + 1e-6
+    o = B.oracle_open(cp, sp)
+    ref = o.render_samples(z["px"], z["py"])
+    ctx_ref = _ctx(cp, sp, N.TREE_REF_EQUAL_COUNT)
+    gs = _per_sample(ctx_ref, p.spp)[:, z["py"], z["px"]].transpose(1, 0, 2)
+    close = np.abs(gs - ref).max(-1) <= 1e-6 * (1 + np.abs(ref).max(-1))
+    assert close.mean() >= 0.9
+
+
 def test_film_rgb8_follows_frame_buffer(tmp_path):
     """c2g_film_rgb8 = GetImageDataRGB8 (FrameBuffer.cpp:42-56) restated: flipped rows,
     pow(mean, gamma), clamp to [0, 0.999], floor(x * 256)."""

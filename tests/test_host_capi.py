@@ -90,9 +90,20 @@ def test_error_codes(tmp_path):
     s2 = json.loads(json.dumps(scn))
     s2["Scene"]["Objects"][0]["Material"] = {"Type": "Velvet"}
     _expect(N.C2G_ERR_INVALID, lambda: ctx.load_text(json.dumps(cfg), json.dumps(s2)))
-    # texture-mapped diffuse: reported as unsupported, never silently dropped
+    # a Kd texture name the scene does not define -> invalid (Scene.cpp:69-77)
     s3 = json.loads(json.dumps(scn))
     s3["Scene"]["Objects"][0]["Material"] = {"Type": "Diffuse", "Kd": "Test"}
+    _expect(N.C2G_ERR_INVALID, lambda: ctx.load_text(json.dumps(cfg), json.dumps(s3)))
+    # an image in a format the loader does not decode (and nobody registered) -> unsupported
+    jpg = tmp_path / "photo.jpg"
+    jpg.write_bytes(bytes([0xFF, 0xD8, 0xFF, 0xE0]) + bytes(60))
+    s3["Scene"]["Textures"] = {"Test": {"Path": str(jpg)}}
+    _expect(N.C2G_ERR_UNSUPPORTED, lambda: ctx.load_text(json.dumps(cfg), json.dumps(s3)))
+    # the same file decoded by the caller loads (c2g_register_image)
+    ctx.register_image(str(jpg), np.full((2, 3, 3), 128, np.uint8))
+    ctx.load_text(json.dumps(cfg), json.dumps(s3))
+    # textured Oren-Nayar is unimplemented in the reference too (Material.cpp:103-108)
+    s3["Scene"]["Objects"][0]["Material"] = {"Type": "OrenNayar", "Kd": "Test", "Sigma": 0.3}
     _expect(N.C2G_ERR_UNSUPPORTED, lambda: ctx.load_text(json.dumps(cfg), json.dumps(s3)))
     # unknown integrator / accelerator -> invalid (Integrator.cpp:37-43, Accelerator.cpp:20-23)
     c2 = json.loads(json.dumps(cfg))
@@ -122,3 +133,20 @@ def test_json_numbers_follow_reference_parser(tmp_path):
     ctx = Context(device=-1)
     ctx.load_text(json.dumps(cfg), open(sp).read())
     assert ctx.render_params().spp == 3
+
+
+def test_textured_scene_loads_on_host(tmp_path):
+    """Textures, per-triangle uvs and the six skybox faces load without a device; a truncated PPM
+    raster is a parse error."""
+    cp, sp = scenes.textured_yard(str(tmp_path / "t"))
+    ctx = Context(device=-1)
+    ctx.load(cp, sp)
+    assert ctx.num_objects() == 6 and ctx.num_lights() == 3  # two area-light triangles + the point light
+    scn = json.load(open(sp))
+    bad = tmp_path / "short.ppm"
+    bad.write_bytes(b"P6\n4 4\n255\n" + bytes(10))
+    scn["Scene"]["Textures"]["floor"]["Path"] = str(bad)
+    _expect(N.C2G_ERR_PARSE, lambda: ctx.load_text(open(cp).read(), json.dumps(scn)))
+    scn = json.load(open(sp))
+    scn["Scene"]["Skybox"]["Path"] = str(tmp_path / "nowhere")
+    _expect(N.C2G_ERR_IO, lambda: ctx.load_text(open(cp).read(), json.dumps(scn)))
