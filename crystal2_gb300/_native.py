@@ -99,6 +99,8 @@ SIGNATURES = {
     "c2g_film_download": (_I, [_P, _FP, _FP]),
     "c2g_film_image": (_I, [_P, _FP]),
     "c2g_film_rgb8": (_I, [_P, C.c_float, C.POINTER(C.c_ubyte)]),
+    "c2g_film_write_hdr": (_I, [_P, C.c_char_p]),
+    "c2g_write_hdr": (_I, [C.c_char_p, _I, _I, _FP]),
     "c2g_register_image": (_I, [_P, C.c_char_p, _I, _I, C.POINTER(C.c_ubyte)]),
     "c2g_film_download_m2": (_I, [_P, _FP]),
     "c2g_get_stats": (_I, [_P, C.POINTER(Stats)]),
@@ -108,6 +110,7 @@ SIGNATURES = {
     "c2g_trace_rays_dev": (_I, [_P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
     "c2g_halton": (_I, [_P, _I, _I, _I, _IP, _IP, _IP, _I, _FP]),
     "c2g_camera_rays": (_I, [_P, _I, _FP, _FP, _FP]),
+    "c2g_sampler_values": (_I, [_P, _I, _IP, _IP, _IP, _I, _I, _FP]),
     "c2g_guide_reset": (_I, [_P, _FP, _FP, C.c_uint64]),
     "c2g_guide_set_params": (_I, [_P, _FP]),
     "c2g_guide_get_params": (_I, [_P, _FP]),

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -335,6 +336,83 @@ int c2g_film_rgb8(c2g_ctx* ctx, float gamma, unsigned char* rgb8) {
     return C2G_OK;
 }
 
+// Radiance RGBE (Ward's shared-exponent pixels; the new-style run-length scanlines of the
+// Radiance format): what stbi_write_hdr produces for RayTracer.cpp:40.
+static void rgbe_pixel(const float* c, unsigned char* out) {
+    const float r = std::max(c[0], 0.f), g = std::max(c[1], 0.f), b = std::max(c[2], 0.f);
+    const float mx = std::max(r, std::max(g, b));
+    if (!(mx >= 1e-32f)) { out[0] = out[1] = out[2] = out[3] = 0; return; }
+    int e = 0;
+    const float scale = (float)std::frexp(mx, &e) * 256.0f / mx;
+    out[0] = (unsigned char)(r * scale);
+    out[1] = (unsigned char)(g * scale);
+    out[2] = (unsigned char)(b * scale);
+    out[3] = (unsigned char)(e + 128);
+}
+// One channel of a scanline: runs of 4..127 equal bytes as (128 + n, byte), the rest as literal
+// blocks of up to 128 bytes (n, bytes...).
+static void rle_channel(const unsigned char* v, int n, std::string& out) {
+    int i = 0;
+    while (i < n) {
+        int j = i;
+        while (j < n && j - i < 127 && v[j] == v[i]) j++;
+        if (j - i >= 4) {
+            out.push_back((char)(unsigned char)(128 + (j - i)));
+            out.push_back((char)v[i]);
+            i = j;
+            continue;
+        }
+        int k = i;
+        while (k < n && k - i < 128) {
+            int r = k;
+            while (r < n && r - k < 4 && v[r] == v[k]) r++;
+            if (r - k >= 4) break;
+            k++;
+        }
+        out.push_back((char)(unsigned char)(k - i));
+        out.append((const char*)v + i, (size_t)(k - i));
+        i = k;
+    }
+}
+
+int c2g_write_hdr(const char* path, int width, int height, const float* rgb) {
+    if (!path || !rgb || width <= 0 || height <= 0) return C2G_ERR_INVALID;
+    std::string buf = "#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y " + std::to_string(height) + " +X " +
+                      std::to_string(width) + "\n";
+    std::vector<unsigned char> px((size_t)width * 4), ch((size_t)width);
+    for (int y = 0; y < height; y++) {
+        for (int x = 0; x < width; x++) rgbe_pixel(rgb + 3 * ((size_t)y * width + x), &px[4 * (size_t)x]);
+        if (width < 8 || width > 32767) {
+            buf.append((const char*)px.data(), px.size());
+            continue;
+        }
+        buf.push_back(2);
+        buf.push_back(2);
+        buf.push_back((char)(unsigned char)(width >> 8));
+        buf.push_back((char)(unsigned char)(width & 255));
+        for (int c = 0; c < 4; c++) {
+            for (int x = 0; x < width; x++) ch[x] = px[4 * (size_t)x + c];
+            rle_channel(ch.data(), width, buf);
+        }
+    }
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return C2G_ERR_IO;
+    const bool ok = std::fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+    return (std::fclose(f) == 0 && ok) ? C2G_OK : C2G_ERR_IO;
+}
+
+int c2g_film_write_hdr(c2g_ctx* ctx, const char* path) {
+    if (!ctx || !path) return fail(ctx, C2G_ERR_INVALID, "null argument");
+    if (!ctx->loaded) return fail(ctx, C2G_ERR_STATE, "no scene loaded");
+    const int W = ctx->scene->cfg.width, H = ctx->scene->cfg.height;
+    std::vector<float> img((size_t)W * H * 3);
+    int rc = c2g_film_image(ctx, img.data());
+    if (rc) return rc;
+    rc = c2g_write_hdr(path, W, H, img.data());
+    if (rc) return fail(ctx, rc, std::string("cannot write ") + path);
+    return C2G_OK;
+}
+
 int c2g_get_stats(c2g_ctx* ctx, c2g_stats* out) {
     if (!ctx || !out) return fail(ctx, C2G_ERR_INVALID, "null argument");
     *out = ctx->gpu->stats();
@@ -418,6 +496,18 @@ int c2g_halton(c2g_ctx* ctx, int width, int height, int n, const int* px, const 
     if (rc) return rc;
     std::string err;
     rc = ctx->gpu->halton(width, height, n, px, py, sample, ndim, out, *ctx->arena, err);
+    if (rc) return fail(ctx, rc, err);
+    return C2G_OK;
+}
+
+int c2g_sampler_values(c2g_ctx* ctx, int n, const int* px, const int* py, const int* sample, int dim, int two_d,
+                       float* out) {
+    if (!ctx || n < 0 || dim < 0 || (n > 0 && (!px || !py || !sample || !out))) return fail(ctx, C2G_ERR_INVALID, "null argument");
+    if (!ctx->loaded) return fail(ctx, C2G_ERR_STATE, "no scene loaded");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    std::string err;
+    rc = ctx->gpu->sampler_values(ctx->scene->cfg.width, n, px, py, sample, dim, two_d ? 1 : 0, out, *ctx->arena, err);
     if (rc) return fail(ctx, rc, err);
     return C2G_OK;
 }

@@ -447,10 +447,12 @@ void load_scene(HostScene& s, const std::string& config_text, const std::string&
     if (s.cfg.integrator != "PathTracer" && s.cfg.integrator != "DirectLight" && s.cfg.integrator != "GuidedPathTracer")
         throw SceneError(C2G_ERR_INVALID, "Invalid Integrator Type!");
     s.cfg.depth = (int)integ.at("Depth").as_int();
-    if (s.cfg.sampler != "Halton") {
-        if (s.cfg.sampler == "Default" || s.cfg.sampler == "Stratified")
-            throw SceneError(C2G_ERR_UNSUPPORTED, "sampler " + s.cfg.sampler + " is not supported (Halton only)");
+    if (s.cfg.sampler != "Halton" && s.cfg.sampler != "Default" && s.cfg.sampler != "Stratified")
         throw SceneError(C2G_ERR_INVALID, "Invalid Sampler Type!");
+    if (s.cfg.sampler == "Stratified") {  // Sampler.cpp:21-40: a square sample count
+        bool square = false;
+        for (long long i = 1; i * i <= s.cfg.spp; i++) square |= i * i == s.cfg.spp;
+        if (!square) throw SceneError(C2G_ERR_INVALID, "Stratified sampler should have a square number of SamplesPerPixel");
     }
     // Scene::CreateScene (Scene.cpp:23-45)
     const Json& sc = scn.at("Scene");

@@ -25,7 +25,7 @@ struct HostConfig {
     std::string accel;            // "BVH" | "Brute" | "KDTree"
     std::string integrator;       // "PathTracer" | "DirectLight" | "GuidedPathTracer"
     int depth = 0;
-    std::string sampler;          // "Halton" (others: Default, Stratified)
+    std::string sampler;          // "Halton" | "Default" | "Stratified"
     long long seed = 0;
 };
 

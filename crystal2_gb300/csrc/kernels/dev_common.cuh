@@ -127,6 +127,65 @@ __device__ __forceinline__ float halton_sample(const DevScene& S, int vidx, int 
     return hash_uniform(pixel, sample, (uint32_t)dim, S.seed);
 }
 
+// ---- Default and Stratified samplers (DefaultSampler.cpp, StratifiedSampler.cpp) -------------
+// The reference draws both from one std::mt19937 per 32 x 32 tile that every path of the tile
+// advances in turn, so a value depends on how many draws all earlier paths of the tile made: a
+// sequential stream.  Here every (pixel, sample, dimension) has its own counter-based value, which
+// keeps each draw uniform and independent like the reference's (Default), or stratified over the
+// pixel's samples (Stratified), with no order between paths.
+//
+// Stratified: for each pixel and dimension the samples 0..spp-1 visit the spp strata (1D) or the
+// side x side cells (2D) in a keyed random order and jitter uniformly inside them, as the
+// reference's StratifiedSample1D/2D + std::shuffle tables do.  Every dimension is stratified (the
+// reference stratifies the first 18 one- and two-dimensional requests of a sample and draws the
+// rest plainly).  Sample indices past spp start a fresh stratified set per block of spp.
+
+// A keyed bijection of [0, n): rounds of (xor key, odd multiply, xorshift) on the smallest
+// power-of-two domain holding n, repeated while the value falls outside [0, n) (cycle walking;
+// the cycle through i returns into range within 2^k rounds).
+__device__ __forceinline__ uint32_t permute_index(uint32_t i, uint32_t n, uint32_t key) {
+    if (n <= 1) return 0;
+    uint32_t mask = n - 1;
+    mask |= mask >> 1; mask |= mask >> 2; mask |= mask >> 4; mask |= mask >> 8; mask |= mask >> 16;
+    const int bits = 32 - __clz(mask);
+    const int sh = bits > 1 ? (bits + 1) / 2 : 1;
+    uint32_t x = i;
+    for (uint32_t it = 0; it <= mask; it++) {
+        x = ((x ^ key) * 0x9E3779B1u) & mask;
+        x ^= x >> sh;
+        x = ((x ^ (key >> 16)) * 0x85EBCA77u) & mask;
+        x ^= x >> sh;
+        if (x < n) break;
+    }
+    return x;
+}
+__device__ __forceinline__ uint32_t strata_key(uint32_t pixel, uint32_t block, uint32_t dim, uint64_t seed) {
+    return hash32(pixel * 0x9E3779B9U ^ hash32(dim * 0x632BE5ABU ^ hash32(block ^ (uint32_t)seed)));
+}
+__device__ __forceinline__ float path_sample1(const DevScene& S, int vidx, int dim, uint32_t pixel, uint32_t sample) {
+    if (S.sampler == SAMPLER_HALTON) return halton_sample(S, vidx, dim, pixel, sample);
+    const float j = hash_uniform(pixel, sample, (uint32_t)dim, S.seed);
+    if (S.sampler == SAMPLER_DEFAULT) return j;
+    const uint32_t n = (uint32_t)S.spp, s = sample % n;
+    const uint32_t cell = permute_index(s, n, strata_key(pixel, sample / n, (uint32_t)dim, S.seed));
+    return fminf(__fmul_rn(__frcp_rn((float)n), __fadd_rn((float)cell, j)), kOneMinusEps);
+}
+__device__ __forceinline__ float2 path_sample2(const DevScene& S, int vidx, int dim, uint32_t pixel, uint32_t sample) {
+    if (S.sampler == SAMPLER_HALTON) {
+        if (dim == 0) return make_float2(halton_dim0(vidx, S.hp), halton_dim1(vidx, S.hp));
+        return make_float2(halton_sample(S, vidx, dim, pixel, sample), halton_sample(S, vidx, dim + 1, pixel, sample));
+    }
+    const float jx = hash_uniform(pixel, sample, (uint32_t)dim, S.seed);
+    const float jy = hash_uniform(pixel, sample, (uint32_t)dim + 1u, S.seed);
+    if (S.sampler == SAMPLER_DEFAULT) return make_float2(jx, jy);
+    const uint32_t n = (uint32_t)S.spp, s = sample % n, side = (uint32_t)S.strata_side;
+    const uint32_t cell = permute_index(s, n, strata_key(pixel, sample / n, (uint32_t)dim, S.seed));
+    const uint32_t row = cell / side, col = cell - row * side;
+    const float inv = __frcp_rn((float)side);
+    return make_float2(fminf(__fmul_rn(inv, __fadd_rn((float)col, jx)), kOneMinusEps),
+                       fminf(__fmul_rn(inv, __fadd_rn((float)row, jy)), kOneMinusEps));
+}
+
 // GetVectorIndexForSample (HaltonSampler.cpp:251-270), integer arithmetic as the reference.
 __device__ __forceinline__ int halton_vector_index(const HaltonParams& hp, int px, int py, int sample) {
     long long off = 0;

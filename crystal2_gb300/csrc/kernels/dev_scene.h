@@ -32,12 +32,17 @@ struct DevScene {
     const uint16_t* perm;         // 100 concatenated permutation tables
     const int* perm_off;          // table offsets
     uint64_t seed;
+    int sampler;                  // SAMPLER_HALTON / SAMPLER_DEFAULT / SAMPLER_STRATIFIED
+    int spp;                      // SamplesPerPixel (the stratified sampler's strata per dimension)
+    int strata_side;              // sqrt(spp): the 2D strata grid of the stratified sampler
     int* err;                     // device error word (C2G_DEVERR_*)
     const float2* tri_uv;         // 3 texture coordinates per scene triangle
     const float* texels;          // RGB float texels of every texture, back to back
     const int4* tex_info;         // per texture: width, height, first texel (float index), 0
     int sky[6];                   // cubemap skybox faces (+x, -x, +y, -y, +z, -z), -1: none
 };
+
+enum : int { SAMPLER_HALTON = 0, SAMPLER_DEFAULT = 1, SAMPLER_STRATIFIED = 2 };
 
 // Shading buckets: 0..9 = MatType of the hit's material, 10 = no material, 11 = miss.
 constexpr int kBuckets = 12;

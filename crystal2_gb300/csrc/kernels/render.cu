@@ -178,9 +178,9 @@ __global__ void k_raygen(DevScene S, WaveArgs a, PathRefs out, float4* out_L, in
         int j = warp_append(qcount, valid);
         if (valid) {
             int sample = wave_sample0(a) + s_local;
-            int vidx = halton_vector_index(S.hp, x, y, sample);
-            float sx = halton_dim0(vidx, S.hp);
-            float sy = halton_dim1(vidx, S.hp);
+            int vidx = S.sampler == SAMPLER_HALTON ? halton_vector_index(S.hp, x, y, sample) : 0;
+            const float2 sj = path_sample2(S, vidx, 0, (uint32_t)(y * a.W + x), (uint32_t)sample);
+            float sx = sj.x, sy = sj.y;
             float nx, ny;
             pixel_ndc(x, y, sx, sy, a.W, a.H, nx, ny);
             float3 o, d;
@@ -408,8 +408,8 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
         float3 f2 = f3(0.f, 0.f, 0.f), wi2 = f3(0.f, 0.f, 0.f);
         float pdf_b2 = 0.f;
         if (do_nee) {
-            uL = make_float2(halton_sample(S, vidx, dim, pixel, sample), halton_sample(S, vidx, dim + 1, pixel, sample));
-            uB = make_float2(halton_sample(S, vidx, dim + 2, pixel, sample), halton_sample(S, vidx, dim + 3, pixel, sample));
+            uL = path_sample2(S, vidx, dim, pixel, sample);
+            uB = path_sample2(S, vidx, dim + 2, pixel, sample);
             dim += 4;
             int n_area = 0;
             for (int l = 0; l < S.n_lights; l++) {
@@ -491,8 +491,8 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
         // ---- continuation: BSDF sample (PathTracingIntegrator.cpp:73-102); none for direct lighting
         if (do_nee && !direct) {
             // GCC evaluates SampleDirection(Get1D(), Get2D(), ...) right to left: Get2D first.
-            float2 u2 = make_float2(halton_sample(S, vidx, dim, pixel, sample), halton_sample(S, vidx, dim + 1, pixel, sample));
-            float u1 = halton_sample(S, vidx, dim + 2, pixel, sample);
+            float2 u2 = path_sample2(S, vidx, dim, pixel, sample);
+            float u1 = path_sample1(S, vidx, dim + 2, pixel, sample);
             dim += 3;
             float3 wi = f3(0.f, 0.f, 0.f);
             float pdf = 0.f;
@@ -554,7 +554,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                 cont = true;
                 if (bounce > 3) {
                     float q = fmaxf(.05f, 1.f - length(beta));
-                    float u = halton_sample(S, vidx, dim, pixel, sample);
+                    float u = path_sample1(S, vidx, dim, pixel, sample);
                     dim += 1;
                     if (u < q) cont = false;
                     else beta = beta / (1 - q);
@@ -811,6 +811,23 @@ __global__ void k_halton(DevScene S, HaltonParams hp, int W, int n, const int* p
     }
 }
 
+// Values of the scene's sampler: the camera pair (dim 0) and the integrator's draws use the same
+// path_sample1/2 calls.  out: n * (1 + two_d) floats.
+__global__ void k_sampler_values(DevScene S, int W, int n, const int* px, const int* py, const int* sample, int dim, int two_d,
+                                 float* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int vidx = S.sampler == SAMPLER_HALTON ? halton_vector_index(S.hp, px[i], py[i], sample[i]) : 0;
+    const uint32_t pixel = (uint32_t)(py[i] * W + px[i]);
+    if (two_d) {
+        const float2 v = path_sample2(S, vidx, dim, pixel, (uint32_t)sample[i]);
+        out[2 * i] = v.x;
+        out[2 * i + 1] = v.y;
+    } else {
+        out[i] = path_sample1(S, vidx, dim, pixel, (uint32_t)sample[i]);
+    }
+}
+
 __global__ void k_camera(Camera c, int n, const float* pos2, float* o, float* d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -948,6 +965,10 @@ int GpuScene::upload(const HostScene& s, int tree, const RefTree* ref, const Sah
     S.perm_off = upload_vec(off, arena, sb_->owned, err, rc);
     if (rc) return rc;
     S.seed = (uint64_t)s.cfg.seed;
+    S.sampler = s.cfg.sampler == "Default" ? SAMPLER_DEFAULT : s.cfg.sampler == "Stratified" ? SAMPLER_STRATIFIED : SAMPLER_HALTON;
+    S.spp = std::max(1, s.cfg.spp);
+    S.strata_side = 1;
+    while ((S.strata_side + 1) * (S.strata_side + 1) <= S.spp) S.strata_side++;
     const int* primes = halton_primes();
     uint64_t magic[kHaltonDims];
     for (int i = 0; i < kHaltonDims; i++) magic[i] = UINT64_MAX / (uint64_t)primes[i] + 1;
@@ -1407,6 +1428,28 @@ int GpuScene::halton(int width, int height, int n, const int* px, const int* py,
         if (cudaGetLastError() != cudaSuccess || cudaMemcpy(out, dout, bytes_o, cudaMemcpyDeviceToHost) != cudaSuccess) rc = C2G_ERR_CUDA;
     } while (0);
     if (rc) err = "halton query failed";
+    arena.free(dpx);
+    arena.free(dout);
+    return rc;
+}
+
+int GpuScene::sampler_values(int width, int n, const int* px, const int* py, const int* sample, int dim, int two_d, float* out,
+                             DeviceArena& arena, std::string& err) {
+    if (!sb_->S.perm) { err = "no scene loaded"; return C2G_ERR_STATE; }
+    if (n <= 0) return C2G_OK;
+    size_t bytes_i = (size_t)n * 4, bytes_o = (size_t)n * (two_d ? 2 : 1) * 4;
+    int* dpx = (int*)arena.alloc(bytes_i * 3, err);
+    float* dout = (float*)arena.alloc(bytes_o, err);
+    if (!dpx || !dout) { arena.free(dpx); arena.free(dout); return C2G_ERR_OOM; }
+    int rc = C2G_OK;
+    do {
+        if (cudaMemcpy(dpx, px, bytes_i, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(dpx + n, py, bytes_i, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(dpx + 2 * n, sample, bytes_i, cudaMemcpyHostToDevice) != cudaSuccess) { rc = C2G_ERR_CUDA; break; }
+        k_sampler_values<<<(n + 127) / 128, 128>>>(sb_->S, width, n, dpx, dpx + n, dpx + 2 * n, dim, two_d, dout);
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(out, dout, bytes_o, cudaMemcpyDeviceToHost) != cudaSuccess) rc = C2G_ERR_CUDA;
+    } while (0);
+    if (rc) err = "sampler query failed";
     arena.free(dpx);
     arena.free(dout);
     return rc;

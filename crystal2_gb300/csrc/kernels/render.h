@@ -75,6 +75,8 @@ public:
     int film_download(float* rgb_sum, float* weight, float* rgb_sumsq, std::string& err);
     int trace_rays_dev(int n, const float* o, const float* d, const float* tmin, const float* tmax, const int* ignore,
                        int any_hit, int* obj, float* t, cudaStream_t st, std::string& err);
+    int sampler_values(int width, int n, const int* px, const int* py, const int* sample, int dim, int two_d, float* out,
+                       DeviceArena& arena, std::string& err);
     int halton(int width, int height, int n, const int* px, const int* py, const int* sample, int ndim, float* out,
                DeviceArena& arena, std::string& err);
     int camera_rays(int n, const float* pos2, float* o, float* d, DeviceArena& arena, std::string& err);

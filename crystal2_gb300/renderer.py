@@ -138,6 +138,10 @@ class Context:
         self.check(self._lib.c2g_film_rgb8(self._h, float(gamma), out.ctypes.data_as(C.POINTER(C.c_ubyte))))
         return out
 
+    def write_hdr(self, path: str) -> None:
+        """Radiance .hdr of the film image (what the reference writes as result.hdr)."""
+        self.check(self._lib.c2g_film_write_hdr(self._h, path.encode()))
+
     def stats(self) -> N.Stats:
         s = N.Stats()
         self.check(self._lib.c2g_get_stats(self._h, C.byref(s)))
@@ -171,6 +175,16 @@ class Context:
         sample = np.ascontiguousarray(sample, np.int32)
         out = np.zeros((px.shape[0], ndim), np.float32)
         self.check(self._lib.c2g_halton(self._h, width, height, px.shape[0], N.iptr(px), N.iptr(py), N.iptr(sample), ndim, N.fptr(out)))
+        return out
+
+    def sampler_values(self, px, py, sample, dim: int, two_d: bool = True) -> np.ndarray:
+        """Draws of the scene's sampler at flat dimension ``dim``: (n, 2) pairs or (n,) values."""
+        px = np.ascontiguousarray(px, np.int32)
+        py = np.ascontiguousarray(py, np.int32)
+        sample = np.ascontiguousarray(sample, np.int32)
+        out = np.zeros((px.shape[0], 2) if two_d else (px.shape[0],), np.float32)
+        self.check(self._lib.c2g_sampler_values(self._h, px.shape[0], N.iptr(px), N.iptr(py), N.iptr(sample), int(dim),
+                                                1 if two_d else 0, N.fptr(out)))
         return out
 
     def camera_rays(self, pos2: np.ndarray):
@@ -308,8 +322,8 @@ class Integrator:
         t = node["Type"]
         if t not in cls.TYPES:
             raise ValueError("Invalid Integrator Type!")
-        if node["Sampler"]["Type"] != "Halton":
-            raise ValueError(f"sampler {node['Sampler']['Type']} is not supported (Halton only)")
+        if node["Sampler"]["Type"] not in ("Halton", "Default", "Stratified"):
+            raise ValueError("Invalid Sampler Type!")
         return cls(cls.TYPES[t], int(node["Depth"]))
 
     def render(self, ctx: Context, sample_begin: int = 0, sample_count: int | None = None, wave_paths: int = 0) -> None:
@@ -342,23 +356,13 @@ class RayTracer:
         return self.ctx.image()
 
     def write_hdr(self, path: str = "result.hdr") -> None:
-        write_hdr(path, self.image())
+        self.ctx.write_hdr(path)
 
 
 def write_hdr(path: str, rgb: np.ndarray) -> None:
-    """Radiance RGBE file (flat, uncompressed scanlines) of an (H, W, 3) float image, top row first."""
-    rgb = np.nan_to_num(np.asarray(rgb, np.float32), nan=0.0, posinf=0.0, neginf=0.0)
-    h, w, _ = rgb.shape
-    m = rgb.max(axis=2)
-    e = np.zeros_like(m, dtype=np.int32)
-    mant, ex = np.frexp(m)
-    nz = m > 1e-32
-    e[nz] = ex[nz]
-    scale = np.where(nz, 256.0 / np.ldexp(1.0, e), 0.0)
-    out = np.zeros((h, w, 4), np.uint8)
-    out[..., :3] = np.clip(rgb * scale[..., None], 0, 255).astype(np.uint8)
-    out[..., 3] = np.where(nz, e + 128, 0).astype(np.uint8)
-    with open(path, "wb") as fh:
-        fh.write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n")
-        fh.write(f"-Y {h} +X {w}\n".encode())
-        fh.write(out.tobytes())
+    """Radiance .hdr of an (height, width, 3) float image, row 0 written first (no context needed)."""
+    a = np.ascontiguousarray(rgb, np.float32)
+    rc = N.load_library().c2g_write_hdr(path.encode(), a.shape[1], a.shape[0], N.fptr(a))
+    if rc:
+        raise N.C2GError(rc, "c2g_write_hdr failed: " + path)
+

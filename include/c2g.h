@@ -150,6 +150,13 @@ int c2g_film_image(c2g_ctx* ctx, float* rgb);
 /* GetImageDataRGB8(gamma) (FrameBuffer.cpp:42-56): rows flipped like c2g_film_image, each channel
  * pow(mean, gamma) clamped to [0, 0.999] and scaled by 256; 3 bytes per pixel. */
 int c2g_film_rgb8(c2g_ctx* ctx, float gamma, unsigned char* rgb8);
+/* Radiance RGBE file of the film image (GetImageDataRGB32F order), the output RayTracer.cpp:40
+ * writes with stbi_write_hdr: "-Y H +X W" header, run-length-encoded scanlines for widths
+ * 8..32767, flat RGBE otherwise. */
+int c2g_film_write_hdr(c2g_ctx* ctx, const char* path);
+/* The same writer on caller data: rgb = height x width x 3 floats, row 0 written first.  Needs no
+ * context or device; negative components are written as 0. */
+int c2g_write_hdr(const char* path, int width, int height, const float* rgb);
 /* Per-pixel sum of squares of the samples (variance estimates for parity tests). */
 int c2g_film_download_m2(c2g_ctx* ctx, float* rgb_sumsq);
 int c2g_get_stats(c2g_ctx* ctx, c2g_stats* out);
@@ -258,6 +265,12 @@ int c2g_trace_rays_dev(c2g_ctx* ctx, int n, const float* o_dev, const float* d_d
  * [0, ndim); film size width x height. Dims >= 100 come from the hash RNG. out: n * ndim. */
 int c2g_halton(c2g_ctx* ctx, int width, int height, int n, const int* px, const int* py,
                const int* sample, int ndim, float* out);
+/* Draws of the loaded scene's sampler (Config Integrator.Sampler: Halton, Default or Stratified;
+ * Sampler::Get1D / Get2D, Sampler.cpp:10-53) at flat dimension `dim` for n (pixel, sample)
+ * pairs: one float each (two_d = 0) or the pair (dim, dim + 1) (two_d = 1).  Dimension 0 is the
+ * camera's pixel jitter.  out: n * (1 + two_d). */
+int c2g_sampler_values(c2g_ctx* ctx, int n, const int* px, const int* py, const int* sample, int dim, int two_d,
+                       float* out);
 /* PerspCamera::GenerateRay for NDC points pos2 (n x 2) of the loaded camera. */
 int c2g_camera_rays(c2g_ctx* ctx, int n, const float* pos2, float* o, float* d);
 

@@ -170,6 +170,12 @@ class OracleScene(_Scene):
         secs = self.lib.orc_render_region(self.h, threads, x0, y0, x1, y1, s0, ns, C.c_ulonglong(seed), _d(s), _d(q))
         return s, q, secs
 
+    def render_frame(self, threads=8):
+        """(float sum (H, W, 3), float weight (H, W)) accumulated like the reference's FrameBuffer."""
+        rgbw = np.zeros((self.H, self.W, 4), np.float32)
+        self.lib.orc_render_frame(self.h, threads, _f(rgbw))
+        return rgbw[..., :3].copy(), rgbw[..., 3].copy()
+
     def render_samples(self, px, py, spp=None, seed=0):
         spp = self.spp if spp is None else spp
         px = np.ascontiguousarray(px, np.int32)
@@ -215,6 +221,8 @@ def ref_library():
         lib.ref_render_region.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _D, _D]
         lib.ref_render_region.restype = C.c_double
         lib.ref_render_samples.argtypes = [C.c_void_p, C.c_int, _I, _I, _F]
+        lib.ref_write_hdr.argtypes = [C.c_char_p, C.c_int, C.c_int, _F]
+        lib.ref_write_hdr.restype = C.c_int
         lib.ref_halton_index.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _I, _I, _I, _L]
         lib.ref_bsdf.argtypes = [C.c_char_p, C.c_int, _F, C.c_int, _F, _F, _F, C.c_int, _F, _F, _F, _F, _F, _I]
         lib.ref_bsdf.restype = C.c_int
@@ -237,6 +245,7 @@ def oracle_library():
                                           C.c_ulonglong, _D, _D]
         lib.orc_render_region.restype = C.c_double
         lib.orc_render_samples.argtypes = [C.c_void_p, C.c_int, _I, _I, C.c_int, C.c_ulonglong, _F]
+        lib.orc_render_frame.argtypes = [C.c_void_p, C.c_int, _F]
         lib.orc_bsdf.argtypes = [C.c_char_p, _F, C.c_int, _F, C.c_int, _F, _F, _F, C.c_int, _F, _F, _F, _F, _F, _I]
         lib.orc_bsdf.restype = C.c_int
         _orc_lib = lib
@@ -328,3 +337,10 @@ def bsdf_eval(which: str, kind: str, params, front: int, frame, wo, wi, u3, flag
     if rc < 0:
         raise RuntimeError("bsdf harness failed")
     return fe, pe, fs, ws, ps, ts
+
+
+def ref_write_hdr(path: str, rgb: np.ndarray) -> None:
+    """The reference's stbi_write_hdr on an (h, w, 3) float image (row 0 written first)."""
+    a = np.ascontiguousarray(rgb, np.float32)
+    if not ref_library().ref_write_hdr(path.encode(), a.shape[1], a.shape[0], _f(a)):
+        raise OSError("stbi_write_hdr failed: " + path)

@@ -271,6 +271,8 @@ struct Node { Box b; int a, c; int axis; };  // internal: a=ch0, c=ch1; leaf: a=
 struct Scene {
     int W, H, spp, depth;
     bool direct = false;  // Integrator.Type == "DirectLight"
+    int sampler = 0;      // Sampler.Type: 0 Halton, 1 Default, 2 Stratified (Sampler.cpp:10-53)
+    int side = 0;         // Stratified: sqrt(SamplesPerPixel)
     bool anyclip = true, closest_box = true;
     V3 eye, look, up, right;
     float CW, CH;
@@ -454,6 +456,16 @@ static void load(Scene& s, const std::string& cfgp, const std::string& scnp) {
     s.closest_box = acc != "Brute";
     s.depth = (int)cfg->m("Integrator").m("Depth").I();
     s.direct = cfg->m("Integrator").m("Type").s == "DirectLight";
+    {
+        const std::string st = cfg->m("Integrator").m("Sampler").m("Type").s;
+        if (st == "Halton") s.sampler = 0;
+        else if (st == "Default") s.sampler = 1;
+        else if (st == "Stratified") {
+            s.sampler = 2;
+            for (int i = 1; (long long)i * i <= s.spp; i++) if (i * i == s.spp) s.side = i;
+            if (!s.side) throw std::runtime_error("Stratified sampler should have a square number of SamplesPerPixel");
+        } else throw std::runtime_error("Invalid Sampler Type!");
+    }
     // Scene::CreateScene (Scene.cpp:23-45): textures, objects, then the skybox
     const JNode& texn = scn->m("Scene").m("Textures");
     for (auto& kv : texn.o) s.tex_names[kv.first] = add_tex(s, kv.second->m("Path").s);
@@ -1232,13 +1244,67 @@ static float ph(float f, float g) { return (f * f) / (f * f + g * g); }
 static V3 spawn(const Hit& h, V3 dir) { bool back = dot(dir, h.N) < 0; return h.pos + (back ? -h.N : h.N) * 1e-4f; }
 
 // ---------------------------------------------------------------- integrator
+// DefaultSampler / StratifiedSampler (DefaultSampler.cpp:13-29, StratifiedSampler.cpp:22-100,
+// PixelSampler.cpp:14-40): a std::mt19937 per 32 x 32 tile, seeded with the tile index by Clone
+// (SamplerIntegrator.cpp:40); every draw is min(1 - 2^-24, mt() * 2^-32) in float (Utils.h:12-15).
+// A two-float draw takes the y value first: g++ evaluates the two calls in Point2f(a(), b()) from
+// right to left.  The stratified sampler fills 18 one-dimensional and 18 two-dimensional tables of
+// SamplesPerPixel entries at StartPixel (jittered strata, then std::shuffle with the same engine);
+// requests past the 18th of a kind fall back to plain draws.  The stream is shared by every path of
+// the tile, so a value depends on everything the tile traced before it.
+struct PixelRng {
+    static constexpr int kDims = 18;
+    std::mt19937 mt;
+    int kind = 1, spp = 1, side = 1;
+    int cur = 0, d1 = 0, d2 = 0;
+    std::vector<float> t1[kDims];
+    std::vector<std::pair<float, float>> t2[kDims];
+    PixelRng(int kind_, int spp_, int side_, unsigned tile) : mt(tile), kind(kind_), spp(spp_), side(side_) {
+        if (kind == 2)
+            for (int i = 0; i < kDims; i++) { t1[i].resize(spp); t2[i].resize(spp); }
+    }
+    float uni() { return std::min(0x1.fffffep-1f, (float)mt() * 2.3283064365386963e-10f); }
+    void pair(float& x, float& y) { y = uni(); x = uni(); }
+    void start_pixel() {
+        cur = d1 = d2 = 0;
+        if (kind != 2) return;
+        for (int i = 0; i < kDims; i++) {
+            const float inv = 1.f / spp;
+            for (int k = 0; k < spp; k++) t1[i][k] = std::min(0x1.fffffep-1f, inv * (k + uni()));
+            std::shuffle(t1[i].begin(), t1[i].begin() + spp, mt);
+        }
+        for (int i = 0; i < kDims; i++) {
+            const float inv = 1.f / side;
+            int k = 0;
+            for (int r = 0; r < side; r++)
+                for (int c = 0; c < side; c++, k++) {
+                    t2[i][k].first = std::min(0x1.fffffep-1f, inv * (c + uni()));
+                    t2[i][k].second = std::min(0x1.fffffep-1f, inv * (r + uni()));
+                }
+            std::shuffle(t2[i].begin(), t2[i].begin() + spp, mt);
+        }
+    }
+    bool next_sample() { d1 = d2 = 0; return ++cur < spp; }
+    float get1() { return (kind == 2 && d1 < kDims) ? t1[d1++][cur] : uni(); }
+    void get2(float& x, float& y) {
+        if (kind == 2 && d2 < kDims) { x = t2[d2][cur].first; y = t2[d2][cur].second; d2++; }
+        else pair(x, y);
+    }
+};
+
 struct Sampler {
     const Scene& s;
     int vidx;
     uint32_t pixel, sample;
     uint64_t seed;
     int dim = 0;
-    float get() { return halton_value(s, vidx, dim++, pixel, sample, seed); }
+    PixelRng* pr = nullptr;  // Default / Stratified; Halton when null
+    float get1() { return pr ? pr->get1() : halton_value(s, vidx, dim++, pixel, sample, seed); }
+    void get2(float& x, float& y) {
+        if (pr) { pr->get2(x, y); return; }
+        x = halton_value(s, vidx, dim++, pixel, sample, seed);
+        y = halton_value(s, vidx, dim++, pixel, sample, seed);
+    }
 };
 
 static V3 evaluate(const Scene& s, Ray ray, Sampler& smp) {
@@ -1261,7 +1327,9 @@ static V3 evaluate(const Scene& s, Ray ray, Sampler& smp) {
         Frame fr{h.dpdu, h.N, h.dpdv};
         V3 wo = -ray.d;
         // UniformSampleAllLights
-        float lx = smp.get(), ly = smp.get(), bx = smp.get(), by = smp.get();
+        float lx, ly, bx, by;
+        smp.get2(lx, ly);
+        smp.get2(bx, by);
         V3 Ld(0, 0, 0);
         const int ns = BALL & ~BS;
         for (int li = 0; li < (int)s.lights.size(); li++) {
@@ -1283,7 +1351,7 @@ static V3 evaluate(const Scene& s, Ray ray, Sampler& smp) {
                 }
             }
             if (Lg.type != 1) {
-                float u1 = smp.get();
+                float u1 = smp.get1();
                 V3 wi2;
                 float pb2 = 0;
                 int st = 0;
@@ -1314,7 +1382,9 @@ static V3 evaluate(const Scene& s, Ray ray, Sampler& smp) {
         }
         L = L + beta * Ld;
         // continuation: SampleDirection(Get1D(), Get2D(), ...) evaluates Get2D first
-        float cx = smp.get(), cy = smp.get(), c1 = smp.get();
+        float cx, cy;
+        smp.get2(cx, cy);
+        float c1 = smp.get1();
         V3 wi;
         float pdf = 0;
         int st = 0;
@@ -1327,7 +1397,7 @@ static V3 evaluate(const Scene& s, Ray ray, Sampler& smp) {
         beta = beta * (f * cosv / pdf);
         if (bounce > 3) {
             float q = std::max(.05f, 1.f - length(beta));
-            if (smp.get() < q) break;
+            if (smp.get1() < q) break;
             beta = beta / (1 - q);
         }
     }
@@ -1356,7 +1426,9 @@ static V3 evaluate_direct(const Scene& s, Ray ray, Sampler& smp) {
         if (s.mats[ob.mat].tex >= 0) b.R = texel(s, s.mats[ob.mat].tex, h.u, h.v);  // UVTexture Kd
         Frame fr{h.dpdu, h.N, h.dpdv};
         V3 wo = -ray.d;
-        float lx = smp.get(), ly = smp.get(), bx = smp.get(), by = smp.get();
+        float lx, ly, bx, by;
+        smp.get2(lx, ly);
+        smp.get2(bx, by);
         V3 Ld(0, 0, 0);
         const int ns = BALL & ~BS;
         for (int li = 0; li < (int)s.lights.size(); li++) {
@@ -1377,7 +1449,7 @@ static V3 evaluate_direct(const Scene& s, Ray ray, Sampler& smp) {
                 }
             }
             if (Lg.type != 1) {
-                float u1 = smp.get();
+                float u1 = smp.get1();
                 V3 wi2;
                 float pb2 = 0;
                 int st = 0;
@@ -1417,6 +1489,43 @@ static Ray camera_ray(const Scene& s, float px, float py) {
 }  // namespace orc
 
 using namespace orc;
+
+// One camera sample of pixel (x, y): the sampler's first 2D draw jitters the pixel
+// (SamplerIntegrator.cpp:49-55), then the integrator's Evaluate.
+static V3 trace_sample(const Scene& s, Sampler& smp, int x, int y) {
+    float sx, sy;
+    smp.get2(sx, sy);
+    Ray cr = camera_ray(s, ((float)x + sx) / s.W, ((float)y + sy) / s.H);
+    return s.direct ? evaluate_direct(s, cr, smp) : evaluate(s, cr, smp);
+}
+
+// Every sample of one 32 x 32 tile in SamplerIntegrator::Render's order (SamplerIntegrator.cpp:25-69):
+// columns outer, rows inner, samples innermost, one sampler clone per tile.  f(x, y, sample, L).
+template <class F>
+static void run_tile(const Scene& s, int tx, int ty, F&& f) {
+    const int nty = (s.H + 31) / 32;
+    PixelRng pr(s.sampler, s.spp, s.side, (unsigned)(tx * nty + ty));
+    const int x0 = 32 * tx, x1 = std::min(x0 + 32, s.W), y0 = 32 * ty, y1 = std::min(y0 + 32, s.H);
+    for (int x = x0; x < x1; x++)
+        for (int y = y0; y < y1; y++) {
+            pr.start_pixel();
+            do {
+                Sampler smp{s, 0, (uint32_t)(y * s.W + x), (uint32_t)pr.cur, 0};
+                smp.pr = &pr;
+                f(x, y, pr.cur, trace_sample(s, smp, x, y));
+            } while (pr.next_sample());
+        }
+}
+
+// Runs `task(i)` for i in [0, n) on `threads` workers.
+template <class F>
+static void parallel_for(int n, int threads, F&& task) {
+    std::atomic<int> next{0};
+    std::vector<std::thread> th;
+    for (int k = 0; k < std::max(1, threads); k++)
+        th.emplace_back([&]() { for (int i; (i = next.fetch_add(1)) < n;) task(i); });
+    for (auto& t : th) t.join();
+}
 
 extern "C" {
 
@@ -1477,46 +1586,90 @@ void orc_intersect_test(void* h, int n, const float* o, const float* d, const fl
                                 tmin[i], tmax[i], ign ? ign[i] : -1) ? 1 : 0;
 }
 // Per-pixel sum and sum of squares over [x0,x1)x[y0,y1) at samples [s0, s0+ns) (NaN/Inf -> 0).
+// Default / Stratified samplers run whole tiles (the stream of a tile is sequential) and need
+// s0 = 0, ns = spp; returns -1 otherwise.
 double orc_render_region(void* h, int threads, int x0, int y0, int x1, int y1, int s0, int ns, unsigned long long seed,
                          double* sum, double* sumsq) {
     auto* s = static_cast<Scene*>(h);
     int rw = x1 - x0;
-    std::atomic<int> row{y0};
-    auto work = [&]() {
-        while (true) {
-            int y = row.fetch_add(1);
-            if (y >= y1) break;
-            for (int x = x0; x < x1; x++) {
-                double a[3] = {0, 0, 0}, q[3] = {0, 0, 0};
-                for (int k = 0; k < ns; k++) {
-                    int sample = s0 + k;
-                    Sampler smp{*s, halton_index(*s, x, y, sample), (uint32_t)(y * s->W + x), (uint32_t)sample, seed};
-                    float sx = smp.get(), sy = smp.get();
-                    float px = ((float)x + sx) / s->W, py = ((float)y + sy) / s->H;
-                    V3 c = s->direct ? evaluate_direct(*s, camera_ray(*s, px, py), smp) : evaluate(*s, camera_ray(*s, px, py), smp);
-                    if (bad(c)) c = V3();
-                    for (int j = 0; j < 3; j++) { a[j] += c[j]; q[j] += (double)c[j] * c[j]; }
-                }
-                size_t idx = (size_t)(y - y0) * rw + (x - x0);
-                for (int j = 0; j < 3; j++) { sum[3 * idx + j] = a[j]; sumsq[3 * idx + j] = q[j]; }
-            }
-        }
-    };
     auto t0 = std::chrono::steady_clock::now();
-    std::vector<std::thread> th;
-    for (int k = 0; k < std::max(1, threads); k++) th.emplace_back(work);
-    for (auto& t : th) t.join();
+    if (s->sampler != 0) {
+        if (s0 != 0 || ns != s->spp) return -1.0;
+        std::memset(sum, 0, sizeof(double) * 3 * (size_t)rw * (y1 - y0));
+        std::memset(sumsq, 0, sizeof(double) * 3 * (size_t)rw * (y1 - y0));
+        const int ntx = (s->W + 31) / 32, nty = (s->H + 31) / 32;
+        parallel_for(ntx * nty, threads, [&](int t) {
+            const int tx = t / nty, ty = t % nty;
+            if (32 * tx >= x1 || 32 * tx + 32 <= x0 || 32 * ty >= y1 || 32 * ty + 32 <= y0) return;
+            run_tile(*s, tx, ty, [&](int x, int y, int, V3 c) {
+                if (x < x0 || x >= x1 || y < y0 || y >= y1) return;
+                if (bad(c)) c = V3();
+                size_t idx = (size_t)(y - y0) * rw + (x - x0);
+                for (int j = 0; j < 3; j++) { sum[3 * idx + j] += c[j]; sumsq[3 * idx + j] += (double)c[j] * c[j]; }
+            });
+        });
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    parallel_for(y1 - y0, threads, [&](int r) {
+        const int y = y0 + r;
+        for (int x = x0; x < x1; x++) {
+            double a[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+            for (int k = 0; k < ns; k++) {
+                int sample = s0 + k;
+                Sampler smp{*s, halton_index(*s, x, y, sample), (uint32_t)(y * s->W + x), (uint32_t)sample, seed};
+                V3 c = trace_sample(*s, smp, x, y);
+                if (bad(c)) c = V3();
+                for (int j = 0; j < 3; j++) { a[j] += c[j]; q[j] += (double)c[j] * c[j]; }
+            }
+            size_t idx = (size_t)r * rw + (x - x0);
+            for (int j = 0; j < 3; j++) { sum[3 * idx + j] = a[j]; sumsq[3 * idx + j] = q[j]; }
+        }
+    });
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
+
+// The whole frame as FrameBuffer holds it (FrameBuffer.cpp:20-32): per pixel a float sum of the
+// samples in sampling order (NaN/Inf -> 0) and a float weight; rgbw[4 * (y * W + x) + c].
+void orc_render_frame(void* h, int threads, float* rgbw) {
+    auto* s = static_cast<Scene*>(h);
+    std::memset(rgbw, 0, sizeof(float) * 4 * (size_t)s->W * s->H);
+    auto add = [&](int x, int y, V3 c) {
+        if (bad(c)) c = V3();
+        float* p = rgbw + 4 * ((size_t)y * s->W + x);
+        p[0] += c.x; p[1] += c.y; p[2] += c.z; p[3] += 1.f;
+    };
+    const int ntx = (s->W + 31) / 32, nty = (s->H + 31) / 32;
+    parallel_for(ntx * nty, threads, [&](int t) {
+        const int tx = t / nty, ty = t % nty;
+        if (s->sampler != 0) { run_tile(*s, tx, ty, [&](int x, int y, int, V3 c) { add(x, y, c); }); return; }
+        for (int x = 32 * tx; x < std::min(32 * tx + 32, s->W); x++)
+            for (int y = 32 * ty; y < std::min(32 * ty + 32, s->H); y++)
+                for (int k = 0; k < s->spp; k++) {
+                    Sampler smp{*s, halton_index(*s, x, y, k), (uint32_t)(y * s->W + x), (uint32_t)k, 0};
+                    add(x, y, trace_sample(*s, smp, x, y));
+                }
+    });
+}
+
 // Per-sample radiance of pixels (px, py) for samples 0..spp-1: out[(p*spp+s)*3+c].
 void orc_render_samples(void* h, int n, const int* px, const int* py, int spp, unsigned long long seed, float* out) {
     auto* s = static_cast<Scene*>(h);
+    if (s->sampler != 0) {
+        const int nty = (s->H + 31) / 32;
+        std::map<int, std::vector<int>> tiles;  // tile -> requested pixel slots
+        for (int p = 0; p < n; p++) tiles[(px[p] / 32) * nty + py[p] / 32].push_back(p);
+        for (auto& kv : tiles)
+            run_tile(*s, kv.first / nty, kv.first % nty, [&](int x, int y, int k, V3 c) {
+                for (int p : kv.second)
+                    if (px[p] == x && py[p] == y && k < spp)
+                        for (int j = 0; j < 3; j++) out[((size_t)p * spp + k) * 3 + j] = c[j];
+            });
+        return;
+    }
     for (int p = 0; p < n; p++)
         for (int k = 0; k < spp; k++) {
             Sampler smp{*s, halton_index(*s, px[p], py[p], k), (uint32_t)(py[p] * s->W + px[p]), (uint32_t)k, seed};
-            float sx = smp.get(), sy = smp.get();
-            Ray cr = camera_ray(*s, ((float)px[p] + sx) / s->W, ((float)py[p] + sy) / s->H);
-            V3 c = s->direct ? evaluate_direct(*s, cr, smp) : evaluate(*s, cr, smp);
+            V3 c = trace_sample(*s, smp, px[p], py[p]);
             for (int j = 0; j < 3; j++) out[((size_t)p * spp + k) * 3 + j] = c[j];
         }
 }

@@ -83,6 +83,23 @@ struct RefCtx {
     std::unordered_map<const void*, int> lightIndex;           // light  -> index in Scene::_lights
 };
 
+// FixedThreadPool's workers are detached and still lock the pool's queue after its destructor has
+// returned (FixedThreadPool.cpp:5-43), a use-after-free once the integrator that owns the pool is
+// freed.  Before an integrator is destroyed here its workers are told to end, given time to leave,
+// and only then is the pool freed.
+void retire_integrator(std::unique_ptr<crystal::Integrator>& integ) {
+    auto* si = dynamic_cast<crystal::SamplerIntegrator*>(integ.get());
+    if (si && si->_threadPool) {
+        {
+            std::lock_guard<std::mutex> lock(si->_threadPool->_queue.Mutex);
+            si->_threadPool->_queue.ShouldEnd = true;
+        }
+        si->_threadPool->_queue.Condition.notify_all();
+        std::this_thread::sleep_for(std::chrono::milliseconds(50));
+    }
+    integ.reset();
+}
+
 void set_err(char* err, int errlen, const char* msg) {
     if (err && errlen > 0) { std::snprintf(err, errlen, "%s", msg); }
 }
@@ -121,7 +138,11 @@ void* ref_open(const char* cfg_path, const char* scene_path, char* err, int errl
     return nullptr;
 }
 
-void ref_close(void* h) { delete static_cast<RefCtx*>(h); }
+void ref_close(void* h) {
+    auto ctx = static_cast<RefCtx*>(h);
+    retire_integrator(ctx->integrator);
+    delete ctx;
+}
 
 int ref_num_objects(void* h) { return (int)static_cast<RefCtx*>(h)->objects.size(); }
 int ref_num_lights(void* h) { return (int)static_cast<RefCtx*>(h)->scene->_lights.size(); }
@@ -231,6 +252,7 @@ double ref_render(void* h, int threads, float* rgb_sum, float* weight) {
     auto t0 = std::chrono::steady_clock::now();
     integ->Render(ctx->scene.get(), ctx->camera.get(), &fb);
     auto t1 = std::chrono::steady_clock::now();
+    retire_integrator(integ);
     int W = info.Width, H = info.Height;
     for (int i = 0; i < W * H; i++) {
         auto& p = fb._hdrData[i];
@@ -239,6 +261,10 @@ double ref_render(void* h, int threads, float* rgb_sum, float* weight) {
     }
     return std::chrono::duration<double>(t1 - t0).count();
 }
+
+// The reference's Radiance writer (stb_image_write, called by RayTracer.cpp:40) on caller data.
+extern "C" int stbi_write_hdr(char const* filename, int w, int h, int comp, const float* data);
+int ref_write_hdr(const char* path, int w, int h, const float* rgb) { return stbi_write_hdr(path, w, h, 3, rgb); }
 
 // Per-pixel statistics over the rectangle [x0,x1) x [y0,y1) at `spp` samples: the same loop as
 // SamplerIntegrator::Render (SamplerIntegrator.cpp:42-59) calling the integrator's own Evaluate,

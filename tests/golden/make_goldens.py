@@ -18,6 +18,9 @@ Fixtures:
                  (cornell, material_box, spheres, direct_cornell, brdf_box: Oren-Nayar + Blinn-Phong,
                  textured_yard[_direct]: uv textures and the cubemap skybox; ``--only-textured``
                  regenerates just these two)
+  render_sampler_*.npz  float frame sums and weights of SamplerIntegrator::Render with the Default
+                 and Stratified samplers (``--only-samplers`` regenerates these and hdr_writer.npz)
+  hdr_writer.npz stbi_write_hdr output bytes for synthetic float images
 """
 from __future__ import annotations
 
@@ -117,11 +120,65 @@ def textured_goldens(out: str, work: str) -> None:
     render_fixture(out, "textured_yard_direct", cp, sp)
 
 
+SAMPLER_CASES = {  # fixture name -> (sampler, spp, integrator)
+    "sampler_default": ("Default", 8, "PathTracer"),
+    "sampler_stratified": ("Stratified", 9, "PathTracer"),
+    "sampler_default_direct": ("Default", 8, "DirectLight"),
+}
+
+
+def sampler_scene(work: str, name: str):
+    """The Cornell box at 40 x 36 with the case's sampler and integrator."""
+    import json
+    smp, spp, integ = SAMPLER_CASES[name]
+    cp, sp = scenes.cornell(os.path.join(work, name), width=40, height=36, spp=spp)
+    cfg = json.load(open(cp))
+    cfg["Integrator"]["Sampler"]["Type"] = smp
+    cfg["Integrator"]["Type"] = integ
+    json.dump(cfg, open(cp, "w"))
+    return cp, sp
+
+
+def hdr_images():
+    """Float images for the Radiance writer: widths below, inside and at the edges of the
+    run-length range, zeros, tiny and huge values, and flat runs."""
+    rng = np.random.default_rng(21)
+    out = {}
+    for w, h in ((5, 3), (8, 4), (64, 6), (300, 5)):
+        a = rng.random((h, w, 3)).astype(np.float32) * np.float32(4.0)
+        a[0, : w // 2] = 0.0
+        a[1 % h, :] = np.float32(0.25)
+        a[2 % h, w // 3:] = rng.choice(np.array([1e-35, 3e-10, 7.5, 65000.0, 1e20], np.float32), size=(w - w // 3, 3))
+        out[f"{w}x{h}"] = a
+    return out
+
+
+def sampler_goldens(out: str, work: str) -> None:
+    """DefaultSampler / StratifiedSampler frames (the reference's own SamplerIntegrator::Render
+    into a FrameBuffer) and stbi_write_hdr files of synthetic images."""
+    for name in SAMPLER_CASES:
+        cp, sp = sampler_scene(work, name)
+        r = B.ref_open(cp, sp)
+        s, w, _ = r.render(threads=8)
+        r.close()
+        np.savez_compressed(os.path.join(out, f"render_{name}.npz"), sum=s, weight=w)
+    Hz = {}
+    for key, img in hdr_images().items():
+        path = os.path.join(work, f"{key}.hdr")
+        B.ref_write_hdr(path, img)
+        Hz["img_" + key] = img
+        Hz["file_" + key] = np.frombuffer(open(path, "rb").read(), np.uint8)
+    np.savez_compressed(os.path.join(out, "hdr_writer.npz"), **Hz)
+
+
 def main() -> None:
     out = HERE
     work = tempfile.mkdtemp(prefix="c2g_golden_")
     if "--only-textured" in sys.argv:
         textured_goldens(out, work)
+        return
+    if "--only-samplers" in sys.argv:
+        sampler_goldens(out, work)
         return
     rng = np.random.default_rng(0)
     # Halton
@@ -197,6 +254,7 @@ def main() -> None:
                 Bz[key + "_fe"], Bz[key + "_pe"], Bz[key + "_fs"], Bz[key + "_ws"], Bz[key + "_ps"], Bz[key + "_ts"] = fe, pe, fs, ws, ps, ts
     np.savez_compressed(os.path.join(out, "bsdf.npz"), **Bz)
     textured_goldens(out, work)
+    sampler_goldens(out, work)
     print("goldens written to", out)
 
 

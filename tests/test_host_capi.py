@@ -10,7 +10,7 @@ import pytest
 from crystal2_gb300 import Context, scenes
 from crystal2_gb300 import _native as N
 
-from golden_util import GOLDEN, SCENES
+from golden_util import GOLDEN, SCENES, SAMPLER_CASES, read_rgbe, sampler_scene
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -150,3 +150,43 @@ def test_textured_scene_loads_on_host(tmp_path):
     scn = json.load(open(sp))
     scn["Scene"]["Skybox"]["Path"] = str(tmp_path / "nowhere")
     _expect(N.C2G_ERR_IO, lambda: ctx.load_text(open(cp).read(), json.dumps(scn)))
+
+
+def test_hdr_writer_matches_reference_writer(tmp_path):
+    """c2g_write_hdr against the reference's stbi_write_hdr (RayTracer.cpp:40) on the same float
+    images: identical dimensions and identical RGBE pixels after decoding (flat scanlines below
+    width 8, run-length scanlines otherwise)."""
+    from crystal2_gb300 import write_hdr
+    z = np.load(os.path.join(GOLDEN, "hdr_writer.npz"))
+    keys = [k[4:] for k in z.files if k.startswith("img_")]
+    assert len(keys) == 4
+    for key in keys:
+        img = z["img_" + key]
+        path = str(tmp_path / f"{key}.hdr")
+        write_hdr(path, img)
+        ours = open(path, "rb").read()
+        ref = z["file_" + key].tobytes()
+        assert ours.startswith(b"#?RADIANCE\n")
+        a, b = read_rgbe(ours), read_rgbe(ref)
+        assert a.shape == b.shape == img.shape[:2] + (4,)
+        assert np.array_equal(a, b), key
+    with pytest.raises(N.C2GError):
+        write_hdr(str(tmp_path / "no_such_dir" / "x.hdr"), np.zeros((2, 2, 3), np.float32))
+
+
+def test_sampler_types_follow_reference_factory(tmp_path):
+    """Sampler::LoadSampler (Sampler.cpp:10-53): Halton, Default and Stratified load; Stratified
+    needs a square sample count; any other name is invalid."""
+    for name in SAMPLER_CASES:
+        cp, sp = sampler_scene(str(tmp_path), name)
+        Context(device=-1).load(cp, sp)
+    cfg = json.load(open(cp))
+    scn = open(sp).read()
+    ctx = Context(device=-1)
+    cfg["Integrator"]["Sampler"]["Type"] = "Stratified"
+    cfg["SamplesPerPixel"] = 8
+    _expect(N.C2G_ERR_INVALID, lambda: ctx.load_text(json.dumps(cfg), scn))
+    cfg["SamplesPerPixel"] = 16
+    ctx.load_text(json.dumps(cfg), scn)
+    cfg["Integrator"]["Sampler"]["Type"] = "Sobol"
+    _expect(N.C2G_ERR_INVALID, lambda: ctx.load_text(json.dumps(cfg), scn))

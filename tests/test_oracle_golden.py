@@ -167,3 +167,17 @@ def test_textured_render_matches_reference(tmp_path, integrator, name):
     assert np.mean(mean.astype(np.float32) == z["mean"]) >= 0.95
     got = o.render_samples(z["px"], z["py"])
     assert np.mean(got.view(np.uint32) == z["samples"].view(np.uint32)) >= 0.95
+
+
+@pytest.mark.parametrize("name", ["sampler_default", "sampler_stratified", "sampler_default_direct"])
+def test_oracle_samplers_match_reference_frames(tmp_path, name):
+    """DefaultSampler and StratifiedSampler restated (a std::mt19937 per 32 x 32 tile seeded with
+    the tile index, stratified tables filled and shuffled at StartPixel): the oracle's frame is the
+    reference's SamplerIntegrator::Render frame to the bit."""
+    from golden_util import sampler_scene
+    cp, sp = sampler_scene(str(tmp_path), name)
+    o = B.oracle_open(cp, sp)
+    s, w = o.render_frame()
+    z = np.load(os.path.join(GOLDEN, f"render_{name}.npz"))
+    assert np.array_equal(w, z["weight"])
+    assert np.array_equal(s.view(np.uint32), z["sum"].view(np.uint32))
