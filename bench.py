@@ -417,6 +417,7 @@ def guided_equal_time(args) -> dict:
     plain = progressive(N.INTEGRATOR_PATH, 8)
     ctx.load(cp, sp, tree=N.TREE_SAH)  # a fresh, untrained network
     ctx.guide_config(args.guided_lr, args.guided_bsdf_fraction, 2, args.guided_train_steps)
+    ctx.guide_levels(args.guided_levels)
     guided = progressive(N.INTEGRATOR_GUIDED, 8)
     target = plain[-1][2]
     reach = None
@@ -433,6 +434,7 @@ def guided_equal_time(args) -> dict:
             "guided": {"spp": guided[-1][1], "s": round(guided[-1][0], 3), "relMSE": guided[-1][2],
                        "bsdf_fraction": args.guided_bsdf_fraction, "learning_rate": args.guided_lr,
                        "train_steps_per_wave": args.guided_train_steps, "samples_per_wave": 8,
+                       "guided_levels": args.guided_levels,
                        "adam_steps": steps, "last_batch": records, "last_loss": round(loss, 4)},
             "time_to_plain_relMSE_s": None if reach is None else round(reach, 3),
             "time_ratio": None if reach is None else round(reach / plain[-1][0], 3),
@@ -557,6 +559,7 @@ def main() -> int:
     ap.add_argument("--guided-lr", type=float, default=2e-3)
     ap.add_argument("--guided-bsdf-fraction", type=float, default=0.7)
     ap.add_argument("--guided-train-steps", type=int, default=4)
+    ap.add_argument("--guided-levels", type=int, default=2, help="bounce levels served by the guide (0 = all)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-job measurement")
     ap.add_argument("--sah-width", type=int, default=4, choices=[2, 4], help="SAH traversal variant")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0: the library default, 2^21)")

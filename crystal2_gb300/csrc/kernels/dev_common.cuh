@@ -140,21 +140,32 @@ __device__ __forceinline__ float halton_sample(const DevScene& S, int vidx, int 
 // reference stratifies the first 18 one- and two-dimensional requests of a sample and draws the
 // rest plainly).  Sample indices past spp start a fresh stratified set per block of spp.
 
-// A keyed bijection of [0, n): rounds of (xor key, odd multiply, xorshift) on the smallest
-// power-of-two domain holding n, repeated while the value falls outside [0, n) (cycle walking;
-// the cycle through i returns into range within 2^k rounds).
+// A keyed bijection of [0, n): a four-round Feistel network (hash32 round function) on the
+// smallest even bit width holding n, repeated while the value falls outside [0, n) (cycle
+// walking; the cycle through i re-enters [0, n) within 2^bits rounds).  Different keys give
+// statistically independent permutations, so the strata orders of two dimensions are unrelated
+// and every sample stays jointly uniform over the dimensions.
 __device__ __forceinline__ uint32_t permute_index(uint32_t i, uint32_t n, uint32_t key) {
     if (n <= 1) return 0;
-    uint32_t mask = n - 1;
-    mask |= mask >> 1; mask |= mask >> 2; mask |= mask >> 4; mask |= mask >> 8; mask |= mask >> 16;
-    const int bits = 32 - __clz(mask);
-    const int sh = bits > 1 ? (bits + 1) / 2 : 1;
+    int bits = 32 - __clz(n - 1);
+    bits = bits < 2 ? 2 : bits + (bits & 1);
+    if (bits > 30) return i;  // sample counts beyond 2^30 are not stratified
+    const int half = bits >> 1;
+    const uint32_t hmask = (1u << half) - 1u;
+    uint32_t rk[4];
+#pragma unroll
+    for (uint32_t r = 0; r < 4; r++) rk[r] = hash32(key ^ r);
     uint32_t x = i;
-    for (uint32_t it = 0; it <= mask; it++) {
-        x = ((x ^ key) * 0x9E3779B1u) & mask;
-        x ^= x >> sh;
-        x = ((x ^ (key >> 16)) * 0x85EBCA77u) & mask;
-        x ^= x >> sh;
+    for (uint32_t it = 0; it < (1u << bits); it++) {
+        uint32_t L = x >> half, R = x & hmask;
+#pragma unroll
+        for (uint32_t r = 0; r < 4; r++) {
+            const uint32_t F = hash32(R * 0x27d4eb2dU ^ rk[r]) & hmask;
+            const uint32_t t = L ^ F;
+            L = R;
+            R = t;
+        }
+        x = (L << half) | R;
         if (x < n) break;
     }
     return x;

@@ -170,6 +170,10 @@ class OracleScene(_Scene):
         secs = self.lib.orc_render_region(self.h, threads, x0, y0, x1, y1, s0, ns, C.c_ulonglong(seed), _d(s), _d(q))
         return s, q, secs
 
+    def set_counter_sampler(self, on: bool) -> None:
+        """Draw Default / Stratified values per (pixel, sample, dim) as the library does."""
+        self.lib.orc_set_counter_sampler(self.h, 1 if on else 0)
+
     def render_frame(self, threads=8):
         """(float sum (H, W, 3), float weight (H, W)) accumulated like the reference's FrameBuffer."""
         rgbw = np.zeros((self.H, self.W, 4), np.float32)
@@ -246,6 +250,7 @@ def oracle_library():
         lib.orc_render_region.restype = C.c_double
         lib.orc_render_samples.argtypes = [C.c_void_p, C.c_int, _I, _I, C.c_int, C.c_ulonglong, _F]
         lib.orc_render_frame.argtypes = [C.c_void_p, C.c_int, _F]
+        lib.orc_set_counter_sampler.argtypes = [C.c_void_p, C.c_int]
         lib.orc_bsdf.argtypes = [C.c_char_p, _F, C.c_int, _F, C.c_int, _F, _F, _F, C.c_int, _F, _F, _F, _F, _F, _I]
         lib.orc_bsdf.restype = C.c_int
         _orc_lib = lib

@@ -273,6 +273,7 @@ struct Scene {
     bool direct = false;  // Integrator.Type == "DirectLight"
     int sampler = 0;      // Sampler.Type: 0 Halton, 1 Default, 2 Stratified (Sampler.cpp:10-53)
     int side = 0;         // Stratified: sqrt(SamplesPerPixel)
+    bool counter = false; // Default / Stratified drawn per (pixel, sample, dim) as the library does
     bool anyclip = true, closest_box = true;
     V3 eye, look, up, right;
     float CW, CH;
@@ -696,6 +697,55 @@ static float hash_u(uint32_t pixel, uint32_t sample, uint32_t dim, uint64_t seed
     float u = (float)(h >> 8) * 0x1p-24f;
     return std::min(u, OME);
 }
+// The library's parallel realisation of the Default and Stratified samplers (the reference's
+// tile-sequential std::mt19937 streams cannot be split across parallel paths): uniform draws
+// hash_u(pixel, sample, dim); stratified draws visit the strata of each dimension in the order of
+// a keyed four-round Feistel permutation (cycle-walked into [0, spp)) and jitter inside them.
+// Restated here so the tests can compare the GPU with it draw for draw.
+static uint32_t permute_index(uint32_t i, uint32_t n, uint32_t key) {
+    if (n <= 1) return 0;
+    int bits = 32 - __builtin_clz(n - 1);
+    bits = bits < 2 ? 2 : bits + (bits & 1);
+    if (bits > 30) return i;
+    const int half = bits >> 1;
+    const uint32_t hmask = (1u << half) - 1u;
+    uint32_t rk[4];
+    for (uint32_t r = 0; r < 4; r++) rk[r] = h32(key ^ r);
+    uint32_t x = i;
+    for (uint32_t it = 0; it < (1u << bits); it++) {
+        uint32_t L = x >> half, R = x & hmask;
+        for (uint32_t r = 0; r < 4; r++) {
+            const uint32_t F = h32(R * 0x27d4eb2dU ^ rk[r]) & hmask;
+            const uint32_t t = L ^ F;
+            L = R;
+            R = t;
+        }
+        x = (L << half) | R;
+        if (x < n) break;
+    }
+    return x;
+}
+static uint32_t strata_key(uint32_t pixel, uint32_t block, uint32_t dim, uint64_t seed) {
+    return h32(pixel * 0x9E3779B9U ^ h32(dim * 0x632BE5ABU ^ h32(block ^ (uint32_t)seed)));
+}
+static float counter_1d(const Scene& s, int dim, uint32_t pixel, uint32_t sample, uint64_t seed) {
+    const float j = hash_u(pixel, sample, (uint32_t)dim, seed);
+    if (s.sampler == 1) return j;
+    const uint32_t n = (uint32_t)s.spp, k = sample % n;
+    const uint32_t cell = permute_index(k, n, strata_key(pixel, sample / n, (uint32_t)dim, seed));
+    return std::min((1.0f / (float)n) * ((float)cell + j), OME);
+}
+static void counter_2d(const Scene& s, int dim, uint32_t pixel, uint32_t sample, uint64_t seed, float& x, float& y) {
+    const float jx = hash_u(pixel, sample, (uint32_t)dim, seed), jy = hash_u(pixel, sample, (uint32_t)dim + 1u, seed);
+    if (s.sampler == 1) { x = jx; y = jy; return; }
+    const uint32_t n = (uint32_t)s.spp, k = sample % n, side = (uint32_t)s.side;
+    const uint32_t cell = permute_index(k, n, strata_key(pixel, sample / n, (uint32_t)dim, seed));
+    const uint32_t row = cell / side, col = cell - row * side;
+    const float inv = 1.0f / (float)side;
+    x = std::min(inv * ((float)col + jx), OME);
+    y = std::min(inv * ((float)row + jy), OME);
+}
+
 static float halton_value(const Scene& s, int vidx, int dim, uint32_t pixel, uint32_t sample, uint64_t seed) {
     if (dim == 0) return (float)((double)rev64((uint64_t)(int64_t)(vidx >> s.exps[0])) * 0x1p-64);
     if (dim == 1) {
@@ -1298,10 +1348,15 @@ struct Sampler {
     uint32_t pixel, sample;
     uint64_t seed;
     int dim = 0;
-    PixelRng* pr = nullptr;  // Default / Stratified; Halton when null
-    float get1() { return pr ? pr->get1() : halton_value(s, vidx, dim++, pixel, sample, seed); }
+    PixelRng* pr = nullptr;  // the reference's Default / Stratified stream; else per-draw values
+    float get1() {
+        if (pr) return pr->get1();
+        if (s.sampler != 0) return counter_1d(s, dim++, pixel, sample, seed);
+        return halton_value(s, vidx, dim++, pixel, sample, seed);
+    }
     void get2(float& x, float& y) {
         if (pr) { pr->get2(x, y); return; }
+        if (s.sampler != 0) { counter_2d(s, dim, pixel, sample, seed, x, y); dim += 2; return; }
         x = halton_value(s, vidx, dim++, pixel, sample, seed);
         y = halton_value(s, vidx, dim++, pixel, sample, seed);
     }
@@ -1593,7 +1648,7 @@ double orc_render_region(void* h, int threads, int x0, int y0, int x1, int y1, i
     auto* s = static_cast<Scene*>(h);
     int rw = x1 - x0;
     auto t0 = std::chrono::steady_clock::now();
-    if (s->sampler != 0) {
+    if (s->sampler != 0 && !s->counter) {
         if (s0 != 0 || ns != s->spp) return -1.0;
         std::memset(sum, 0, sizeof(double) * 3 * (size_t)rw * (y1 - y0));
         std::memset(sumsq, 0, sizeof(double) * 3 * (size_t)rw * (y1 - y0));
@@ -1641,7 +1696,7 @@ void orc_render_frame(void* h, int threads, float* rgbw) {
     const int ntx = (s->W + 31) / 32, nty = (s->H + 31) / 32;
     parallel_for(ntx * nty, threads, [&](int t) {
         const int tx = t / nty, ty = t % nty;
-        if (s->sampler != 0) { run_tile(*s, tx, ty, [&](int x, int y, int, V3 c) { add(x, y, c); }); return; }
+        if (s->sampler != 0 && !s->counter) { run_tile(*s, tx, ty, [&](int x, int y, int, V3 c) { add(x, y, c); }); return; }
         for (int x = 32 * tx; x < std::min(32 * tx + 32, s->W); x++)
             for (int y = 32 * ty; y < std::min(32 * ty + 32, s->H); y++)
                 for (int k = 0; k < s->spp; k++) {
@@ -1651,10 +1706,13 @@ void orc_render_frame(void* h, int threads, float* rgbw) {
     });
 }
 
+// 0: Default / Stratified follow the reference's tile streams; 1: the library's per-draw values.
+void orc_set_counter_sampler(void* h, int on) { static_cast<Scene*>(h)->counter = on != 0; }
+
 // Per-sample radiance of pixels (px, py) for samples 0..spp-1: out[(p*spp+s)*3+c].
 void orc_render_samples(void* h, int n, const int* px, const int* py, int spp, unsigned long long seed, float* out) {
     auto* s = static_cast<Scene*>(h);
-    if (s->sampler != 0) {
+    if (s->sampler != 0 && !s->counter) {
         const int nty = (s->H + 31) / 32;
         std::map<int, std::vector<int>> tiles;  // tile -> requested pixel slots
         for (int p = 0; p < n; p++) tiles[(px[p] / 32) * nty + py[p] / 32].push_back(p);

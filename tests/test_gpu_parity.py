@@ -423,24 +423,29 @@ def test_film_rgb8_follows_frame_buffer(tmp_path):
 # ---- Default and Stratified samplers ----------------------------------------------------------
 
 @pytest.mark.parametrize("name", ["sampler_default", "sampler_stratified", "sampler_default_direct"])
-def test_default_and_stratified_samplers_vs_reference(tmp_path, name):
-    """The reference's Default and Stratified streams are sequential per 32 x 32 tile (one
-    std::mt19937 advanced by every path of the tile); the GPU draws the same distributions per
-    (pixel, sample, dimension).  Per-pixel means agree with the reference's frame within 3
-    standard errors (the variance estimated from the GPU's own second moment, for both arms)."""
+def test_default_and_stratified_samplers_match_oracle(tmp_path, name):
+    """The Default and Stratified draws of the GPU (per pixel, sample and dimension) are the
+    oracle's restatement of them: per-sample radiance equal to the oracle's (same paths) except
+    where CUDA and libm transcendentals round differently.  The oracle's per-draw samplers are in
+    turn checked against the reference's tile streams in distribution, on the CPU
+    (test_oracle_golden.py), and the image mean agrees with the reference's frame here."""
     cp, sp = sampler_scene(str(tmp_path), name)
-    ctx = _ctx(cp, sp)
+    ctx = _ctx(cp, sp, N.TREE_REF_EQUAL_COUNT)
     p = ctx.render_params()
-    ctx.render(p)
-    s, w = ctx.film()
-    m2 = ctx.film_m2()
+    G = _per_sample(ctx, p.spp)
+    o = B.oracle_open(cp, sp)
+    o.set_counter_sampler(True)
+    ys, xs = np.mgrid[0:p.height, 0:p.width]
+    O = o.render_samples(xs.ravel(), ys.ravel()).reshape(p.height, p.width, p.spp, 3).transpose(2, 0, 1, 3)
+    O = np.where(np.isfinite(O), O, 0)
+    d = np.abs(G - O).max(-1)
+    assert (d <= 1e-6 * (1 + np.abs(O).max(-1))).mean() >= 0.9
+    assert (d / (np.abs(O).max(-1) + 1e-3) < 1e-3).mean() >= 0.99
     z = np.load(os.path.join(GOLDEN, f"render_{name}.npz"))
-    gm = s / w[..., None]
     rm = z["sum"] / z["weight"][..., None]
-    var = 2 * np.maximum(m2 / w[..., None] - gm ** 2, 0) / p.spp
-    zt = (gm - rm) / np.sqrt(var + 1e-12)
-    assert (np.abs(zt) > 3).mean() <= 0.01
-    assert abs(gm.mean() - rm.mean()) <= 3 * np.sqrt(var.sum()) / gm.size + 1e-6
+    gm = G.mean(0)
+    se = np.sqrt(G.var(0).sum() / p.spp * 2) / gm.size
+    assert abs(gm.mean() - rm.mean()) <= 4 * se + 1e-6
 
 
 def test_stratified_sampler_covers_every_stratum(tmp_path):
