@@ -311,6 +311,40 @@ def test_full_size_frame_properties(tmp_path):
     assert abs(diff) <= 4 * se + 1e-5
 
 
+def test_edge_configs_match_oracle(tmp_path):
+    """Ragged and degenerate configurations against the oracle: a 13 x 7 frame (no multiple of any
+    tile or warp size), depth 0 (PathTracingIntegrator's loop never runs: black), depth 1 (only
+    emission seen directly), a scene without lights (black), and a ray query of zero rays."""
+    import json
+    cp, sp = scenes.cornell(str(tmp_path / "c"), width=13, height=7, spp=3)
+    for depth, integ in ((0, "PathTracer"), (1, "PathTracer"), (1, "DirectLight"), (3, "PathTracer")):
+        cfg = json.load(open(cp))
+        cfg["Integrator"]["Depth"] = depth
+        cfg["Integrator"]["Type"] = integ
+        json.dump(cfg, open(cp, "w"))
+        ctx = _ctx(cp, sp, N.TREE_REF_EQUAL_COUNT)
+        p = ctx.render_params()
+        ctx.render(p)
+        s, w = ctx.film()
+        assert np.all(w == 3)
+        o = B.oracle_open(cp, sp)
+        os_, _, _ = o.render_region(0, 0, 13, 7)
+        if depth == 0:
+            assert not s.any() and not os_.any()
+        else:
+            np.testing.assert_allclose(s, os_, rtol=1e-5, atol=1e-6)
+    d0 = str(tmp_path / "dark")
+    cfg = scenes.config_json(13, 7, 2, 4)
+    cp, sp = scenes.write_scene(d0, cfg, scenes.camera((0, 0, -4), (0, 0, 0), 40),
+                                [scenes.sphere((0, 0, 0), 1.0, scenes.diffuse((0.5, 0.5, 0.5)))], "dark")
+    ctx = _ctx(cp, sp)
+    ctx.render(ctx.render_params())
+    s, w = ctx.film()
+    assert np.all(w == 2) and not s.any()
+    obj, t = ctx.trace_rays(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32))
+    assert obj.shape == (0,) and t.shape == (0,)
+
+
 def test_error_paths(tmp_path):
     ctx = Context(0)
     with pytest.raises(N.C2GError) as e:

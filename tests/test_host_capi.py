@@ -190,3 +190,12 @@ def test_sampler_types_follow_reference_factory(tmp_path):
     ctx.load_text(json.dumps(cfg), scn)
     cfg["Integrator"]["Sampler"]["Type"] = "Sobol"
     _expect(N.C2G_ERR_INVALID, lambda: ctx.load_text(json.dumps(cfg), scn))
+
+
+def test_scene_without_objects_is_rejected(tmp_path):
+    """A scene with no geometry (none at all, or only a point light) is C2G_ERR_INVALID: the
+    reference's BVH build dereferences the missing objects and crashes on it."""
+    cfg = scenes.config_json(13, 7, 2, 4)
+    for name, objs in (("empty", []), ("point_only", [scenes.point_light((0, 2, 0), (10, 10, 10))])):
+        cp, sp = scenes.write_scene(str(tmp_path), cfg, scenes.camera((0, 0, -4), (0, 0, 0), 40), objs, name)
+        _expect(N.C2G_ERR_INVALID, lambda: Context(device=-1).load(cp, sp))
