@@ -136,17 +136,92 @@ __device__ __forceinline__ void mma_rows(const __nv_bfloat16* in, int ldi, const
     }
 }
 
-// Forward pass of one warp's 32 samples (two row tiles): A holds the encoded inputs (ld kLdA0);
-// the FP32 outputs land in F (ld kLdF), which aliases A.  `wts` = padded forward weights.
-__device__ __forceinline__ void warp_forward32(const GuideNet& net, const __nv_bfloat16* wts, __nv_bfloat16* A,
-                                               __nv_bfloat16* Bb, float* F) {
-    mma_rows<2, 80, 64>(A, kLdA0, wts + fw_off(0), fw_ld(0), net.params + guide_b_off(0), Bb, kLdH, true, nullptr, 0, nullptr, 0);
-    __syncwarp();
-    mma_rows<2, 64, 64>(Bb, kLdH, wts + fw_off(1), fw_ld(1), net.params + guide_b_off(1), A, kLdH, true, nullptr, 0, nullptr, 0);
-    __syncwarp();
-    mma_rows<2, 64, 64>(A, kLdH, wts + fw_off(2), fw_ld(2), net.params + guide_b_off(2), Bb, kLdH, true, nullptr, 0, nullptr, 0);
-    __syncwarp();
-    mma_rows<2, 64, 48>(Bb, kLdH, wts + fw_off(3), fw_ld(3), net.params + guide_b_off(3), nullptr, 0, false, F, kLdF, nullptr, 0);
+// One hidden layer of a warp's 32 rows with the activations in registers: `a` holds the A
+// fragments of the layer input (two 16-row tiles, K/16 k-tiles), `an` receives the BF16 A
+// fragments of ReLU(a @ W + b) for the next layer.  The accumulator fragment of output columns
+// [16j, 16j + 8) and [16j + 8, 16j + 16) is exactly the next layer's A fragment of k-tile j
+// (rows g and g + 8, columns 2t, 2t + 1 and 2t + 8, 2t + 9), so no shared-memory round trip.
+template <int K, int N>
+__device__ __forceinline__ void layer_relu_reg(const uint32_t (&a)[2][K / 16][4], const __nv_bfloat16* w, int ldw,
+                                               const float* __restrict__ bias, uint32_t (&an)[2][N / 16][4]) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int j = 0; j < N / 16; j++) {
+        float d[2][2][4];
+#pragma unroll
+        for (int hf = 0; hf < 2; hf++) {
+            const int n0 = 16 * j + 8 * hf;
+            const float b0 = __ldg(bias + n0 + 2 * t), b1 = __ldg(bias + n0 + 2 * t + 1);
+#pragma unroll
+            for (int m = 0; m < 2; m++) { d[hf][m][0] = b0; d[hf][m][1] = b1; d[hf][m][2] = b0; d[hf][m][3] = b1; }
+#pragma unroll
+            for (int kk = 0; kk < K / 16; kk++) {
+                uint32_t b[2];
+                const __nv_bfloat16* wr = w + (n0 + g) * ldw + kk * 16 + 2 * t;
+                b[0] = ld32(wr);
+                b[1] = ld32(wr + 8);
+#pragma unroll
+                for (int m = 0; m < 2; m++) mma16816(d[hf][m], a[m][kk], b);
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < 2; m++) {
+            an[m][j][0] = pack_bf16(fmaxf(d[0][m][0], 0.f), fmaxf(d[0][m][1], 0.f));
+            an[m][j][1] = pack_bf16(fmaxf(d[0][m][2], 0.f), fmaxf(d[0][m][3], 0.f));
+            an[m][j][2] = pack_bf16(fmaxf(d[1][m][0], 0.f), fmaxf(d[1][m][1], 0.f));
+            an[m][j][3] = pack_bf16(fmaxf(d[1][m][2], 0.f), fmaxf(d[1][m][3], 0.f));
+        }
+    }
+}
+
+// Forward pass of one warp's 32 samples: A holds the encoded inputs (ld kLdA0); the FP32 outputs
+// land in F (ld kLdF), which aliases A.  `wts` = padded forward weights.  The hidden activations
+// stay in registers (BF16 A fragments), rounded exactly as the tiled training pass rounds them.
+__device__ __forceinline__ void warp_forward32(const GuideNet& net, const __nv_bfloat16* wts, const __nv_bfloat16* A,
+                                               float* F) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    uint32_t a0[2][5][4];
+#pragma unroll
+    for (int m = 0; m < 2; m++)
+#pragma unroll
+        for (int kk = 0; kk < 5; kk++) {
+            const __nv_bfloat16* r0 = A + (m * 16 + g) * kLdA0 + kk * 16 + 2 * t;
+            a0[m][kk][0] = ld32(r0);
+            a0[m][kk][1] = ld32(r0 + 8 * kLdA0);
+            a0[m][kk][2] = ld32(r0 + 8);
+            a0[m][kk][3] = ld32(r0 + 8 * kLdA0 + 8);
+        }
+    __syncwarp();  // every lane has its input fragments before F (aliasing A) is written
+    uint32_t a1[2][4][4], a2[2][4][4];
+    layer_relu_reg<80, 64>(a0, wts + fw_off(0), fw_ld(0), net.params + guide_b_off(0), a1);
+    layer_relu_reg<64, 64>(a1, wts + fw_off(1), fw_ld(1), net.params + guide_b_off(1), a2);
+    layer_relu_reg<64, 64>(a2, wts + fw_off(2), fw_ld(2), net.params + guide_b_off(2), a1);
+    const float* bias = net.params + guide_b_off(3);
+    const __nv_bfloat16* w = wts + fw_off(3);
+#pragma unroll
+    for (int n0 = 0; n0 < 48; n0 += 8) {
+        float d[2][4];
+        const float b0 = __ldg(bias + n0 + 2 * t), b1 = __ldg(bias + n0 + 2 * t + 1);
+#pragma unroll
+        for (int m = 0; m < 2; m++) { d[m][0] = b0; d[m][1] = b1; d[m][2] = b0; d[m][3] = b1; }
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++) {
+            uint32_t b[2];
+            const __nv_bfloat16* wr = w + (n0 + g) * fw_ld(3) + kk * 16 + 2 * t;
+            b[0] = ld32(wr);
+            b[1] = ld32(wr + 8);
+#pragma unroll
+            for (int m = 0; m < 2; m++) mma16816(d[m], a1[m][kk], b);
+        }
+#pragma unroll
+        for (int m = 0; m < 2; m++) {
+            const int r0 = m * 16 + g, c = n0 + 2 * t;
+            F[r0 * kLdF + c] = d[m][0];
+            F[r0 * kLdF + c + 1] = d[m][1];
+            F[(r0 + 8) * kLdF + c] = d[m][2];
+            F[(r0 + 8) * kLdF + c + 1] = d[m][3];
+        }
+    }
     __syncwarp();
 }
 
@@ -156,14 +231,15 @@ __device__ __forceinline__ void store_inputs(__nv_bfloat16* row, const float* in
 }
 
 // ---- inference ---------------------------------------------------------------------------------
-// 128 threads, 32 samples per warp; dynamic shared memory: padded forward weights + per warp an
-// input/output tile (the FP32 outputs overwrite the inputs) and a hidden tile.
-constexpr int kInferWarps = 4;
+// 256 threads, 32 samples per warp; dynamic shared memory: padded forward weights + per warp an
+// input/output tile (the FP32 outputs overwrite the inputs; hidden activations live in registers).
+constexpr int kInferWarps = 8;
+constexpr int kInferThreads = 32 * kInferWarps;
 constexpr int kTileA = 32 * kLdF * 4;      // 6144 B: 32 x 88 BF16 inputs or 32 x 48 FP32 outputs
-constexpr int kTileB = 32 * kLdH * 2;      // 4608 B
-constexpr size_t kInferSmem = kFwElems * 2 + kInferWarps * (kTileA + kTileB);
+static_assert(32 * kLdA0 * 2 <= kTileA, "input tile fits the output tile");
+constexpr size_t kInferSmem = kFwElems * 2 + kInferWarps * kTileA;
 
-__global__ void __launch_bounds__(128) k_guide_infer(DevScene S, GuideNet net, const float4* __restrict__ ray_o,
+__global__ void __launch_bounds__(kInferThreads, 2) k_guide_infer(DevScene S, GuideNet net, const float4* __restrict__ ray_o,
                                                      const float4* __restrict__ ray_d, const float4* __restrict__ hits,
                                                      const int* bucket_cnt, const int* __restrict__ bucket_list, int cap,
                                                      int mask, float* out) {
@@ -172,27 +248,28 @@ __global__ void __launch_bounds__(128) k_guide_infer(DevScene S, GuideNet net, c
     stage_forward_weights(net, wts);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* wbase = smem + kFwElems * 2 + warp * (kTileA + kTileB);
+    unsigned char* wbase = smem + kFwElems * 2 + warp * kTileA;
     __nv_bfloat16* A = reinterpret_cast<__nv_bfloat16*>(wbase);
-    __nv_bfloat16* Bb = reinterpret_cast<__nv_bfloat16*>(wbase + kTileA);
     float* F = reinterpret_cast<float*>(wbase);
-    // work list = the guided buckets back to back
-    int total = 0;
-    int bstart[kBuckets], bcnt[kBuckets];
-#pragma unroll
-    for (int b = 0; b < kBuckets; b++) {
-        bstart[b] = total;
-        bcnt[b] = ((mask >> b) & 1) ? bucket_cnt[b] : 0;
-        total += bcnt[b];
+    // work list = the guided buckets back to back; their prefix offsets live in shared memory
+    __shared__ int bend[kBuckets];
+    if (threadIdx.x == 0) {
+        int total = 0;
+        for (int b = 0; b < kBuckets; b++) {
+            total += ((mask >> b) & 1) ? bucket_cnt[b] : 0;
+            bend[b] = total;
+        }
     }
+    __syncthreads();
+    const int total = bend[kBuckets - 1];
     const int gwarp = blockIdx.x * kInferWarps + warp, nwarps = gridDim.x * kInferWarps;
     for (int base = gwarp * 32; base < total; base += nwarps * 32) {
         int item = base + lane;
         int slot = -1;
         if (item < total) {
             int b = 0;
-            while (b < kBuckets - 1 && item >= bstart[b] + bcnt[b]) b++;
-            slot = bucket_list[(size_t)b * cap + (item - bstart[b])];
+            while (b < kBuckets - 1 && item >= bend[b]) b++;
+            slot = bucket_list[(size_t)b * cap + (item - (b ? bend[b - 1] : 0))];
         }
         float in[kGuideIn];
         if (slot >= 0) {
@@ -207,7 +284,7 @@ __global__ void __launch_bounds__(128) k_guide_infer(DevScene S, GuideNet net, c
         }
         store_inputs(A + lane * kLdA0, in);
         __syncwarp();
-        warp_forward32(net, wts, A, Bb, F);
+        warp_forward32(net, wts, A, F);
         if (slot >= 0) {
             float o[kGuideOut];
 #pragma unroll
@@ -220,15 +297,14 @@ __global__ void __launch_bounds__(128) k_guide_infer(DevScene S, GuideNet net, c
 
 // Forward pass over explicit inputs (x, n, wo as 9 floats per sample): the same tiles as
 // k_guide_infer, used to check the network against the oracle.
-__global__ void __launch_bounds__(128) k_guide_eval(GuideNet net, const float* __restrict__ xnw, int n, float* out) {
+__global__ void __launch_bounds__(kInferThreads, 2) k_guide_eval(GuideNet net, const float* __restrict__ xnw, int n, float* out) {
     extern __shared__ __align__(16) unsigned char smem[];
     __nv_bfloat16* wts = reinterpret_cast<__nv_bfloat16*>(smem);
     stage_forward_weights(net, wts);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* wbase = smem + kFwElems * 2 + warp * (kTileA + kTileB);
+    unsigned char* wbase = smem + kFwElems * 2 + warp * kTileA;
     __nv_bfloat16* A = reinterpret_cast<__nv_bfloat16*>(wbase);
-    __nv_bfloat16* Bb = reinterpret_cast<__nv_bfloat16*>(wbase + kTileA);
     float* F = reinterpret_cast<float*>(wbase);
     const int gwarp = blockIdx.x * kInferWarps + warp, nwarps = gridDim.x * kInferWarps;
     for (int base = gwarp * 32; base < n; base += nwarps * 32) {
@@ -243,7 +319,7 @@ __global__ void __launch_bounds__(128) k_guide_eval(GuideNet net, const float* _
         }
         store_inputs(A + lane * kLdA0, in);
         __syncwarp();
-        warp_forward32(net, wts, A, Bb, F);
+        warp_forward32(net, wts, A, F);
         if (j < n) {
 #pragma unroll
             for (int k = 0; k < kGuideOut; k++) out[(size_t)j * kGuideOut + k] = F[lane * kLdF + k];
@@ -678,7 +754,7 @@ void GuideTrainer::prepare_launch() {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_infer, 128, kInferSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_infer, kInferThreads, kInferSmem);
     g_infer_grid = std::max(1, sms * std::max(1, per));
     g_train_grid = std::max(1, sms);
 }
@@ -691,7 +767,7 @@ void GuideTrainer::infer(cudaStream_t st, const void* Sv, const float4* ray_o, c
     for (int b = 0; b < kBuckets; b++)
         if (((bucket_mask >> b) & 1) && bucket_guided(b)) mask |= 1 << b;
     if (!mask) return;
-    k_guide_infer<<<grid, 128, kInferSmem, st>>>(*static_cast<const DevScene*>(Sv), view(false, false).net, ray_o, ray_d, hits,
+    k_guide_infer<<<grid, kInferThreads, kInferSmem, st>>>(*static_cast<const DevScene*>(Sv), view(false, false).net, ray_o, ray_d, hits,
                                                 bucket_cnt, bucket_list, cap, mask, out_);
 }
 
@@ -755,8 +831,8 @@ int GuideTrainer::eval(DeviceArena& arena, const float* host_xnw, int n, float* 
     if (!din || !dout) rc = C2G_ERR_OOM;
     if (!rc) {
         cudaMemcpy(din, host_xnw, (size_t)n * 9 * 4, cudaMemcpyHostToDevice);
-        int blocks = std::min(1024, (n + 127) / 128);
-        k_guide_eval<<<blocks, 128, kInferSmem>>>(view(false, false).net, din, n, dout);
+        int blocks = std::min(1024, (n + kInferThreads - 1) / kInferThreads);
+        k_guide_eval<<<blocks, kInferThreads, kInferSmem>>>(view(false, false).net, din, n, dout);
         if (cudaDeviceSynchronize() != cudaSuccess) { err = cudaGetErrorString(cudaGetLastError()); rc = C2G_ERR_CUDA; }
         else cudaMemcpy(host_out, dout, (size_t)n * kGuideOut * 4, cudaMemcpyDeviceToHost);
     }
