@@ -130,8 +130,9 @@ __device__ __forceinline__ float packed_select(const float4* p) { return __ldg(p
 
 __device__ __forceinline__ bool packed_valid(const float4* p) { return isfinite(__ldg(p + 8).x); }
 
-// Mixture density at the unit direction w.
-__device__ __forceinline__ float packed_pdf(const float4* p, float3 w) {
+// Mixture density at the unit direction w.  Kept out of line: the shading kernel calls it per
+// light and per continuation, and one copy keeps its instruction footprint small.
+static __device__ __noinline__ float packed_pdf(const float4* p, float3 w) {
     const float* wc = reinterpret_cast<const float*>(p + 10);
     float s = 0.f;
 #pragma unroll
@@ -143,7 +144,7 @@ __device__ __forceinline__ float packed_pdf(const float4* p, float3 w) {
 }
 
 // Sample: lobe by weight with u0, then the vMF around its mean (w = cos theta by inversion).
-__device__ __forceinline__ float3 packed_sample(const float4* p, float u0, float u1, float u2) {
+static __device__ __noinline__ float3 packed_sample(const float4* p, float u0, float u1, float u2) {
     const float* wt = reinterpret_cast<const float*>(p + 8);
     int k = kGuideLobes - 1;
     float acc = 0.f;

@@ -293,7 +293,7 @@ struct ShadeOut {
 };
 
 template <int MT, bool G>
-__global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs cur, const float4* __restrict__ hits,
+__global__ void __launch_bounds__(128, 4) k_shade(DevScene S, WaveArgs a, PathRefs cur, const float4* __restrict__ hits,
                                                 const int* bucket_cnt, const int* __restrict__ bucket_list, int cap, ShadeOut out,
                                                 GuideView gv) {
     const int n = bucket_cnt[MT];
@@ -497,10 +497,14 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
             float3 wi = f3(0.f, 0.f, 0.f);
             float pdf = 0.f;
             int stype = 0;
-            bool ok;
-            float3 f = bsdf_sample(bx, fr, u1, u2, wo, wi, pdf, BXDF_ALL, stype, ok);
+            bool ok = false;
+            // a guided vertex picks its technique first: the mixture's draws need no BSDF sample
+            const bool mix = gvert && alpha < 1.f;
+            const bool use_guide = mix && hash_uniform(pixel, sample, 0x4000u + 4u * bounce, S.seed) >= alpha;
+            float3 f = f3(0.f, 0.f, 0.f);
+            if (!use_guide) f = bsdf_sample(bx, fr, u1, u2, wo, wi, pdf, BXDF_ALL, stype, ok);
             float pb_rec = pdf;  // BSDF density of the continuation (local measure), for training
-            if (gvert && alpha < 1.f) {
+            if (mix) {
                 // One-sample MIS over {BSDF, learned mixture}: q = alpha p_bsdf + (1 - alpha) p_guide,
                 // both exactly evaluated, so the estimator stays unbiased.  The BSDF technique draws
                 // a local direction l and traces M l (M = [dpdu N dpdv], not orthonormal under
@@ -509,8 +513,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveArgs a, PathRefs 
                 // numbers come from hashed dimensions far above the plain path's.
                 const float3 c0 = cross(fr.N, fr.B), c1 = cross(fr.B, fr.T), c2 = cross(fr.T, fr.N);
                 const float3 wol = to_local(fr, wo);
-                float us = hash_uniform(pixel, sample, 0x4000u + 4u * bounce, S.seed);
-                if (us >= alpha) {
+                if (use_guide) {
                     float3 wg = packed_sample(lobes, hash_uniform(pixel, sample, 0x4001u + 4u * bounce, S.seed),
                                              hash_uniform(pixel, sample, 0x4002u + 4u * bounce, S.seed),
                                              hash_uniform(pixel, sample, 0x4003u + 4u * bounce, S.seed));
