@@ -101,8 +101,29 @@ struct WaveBuffers {
 
 GpuScene::GpuScene() : sb_(new DeviceSceneBuffers()), wb_(new WaveBuffers()) {}
 GpuScene::~GpuScene() {
+    if (side_) cudaStreamDestroy(side_);
+    for (int k = 0; k < 2; k++) {
+        if (fork_ev_[k]) cudaEventDestroy(fork_ev_[k]);
+        if (join_ev_[k]) cudaEventDestroy(join_ev_[k]);
+    }
     delete sb_;
     delete wb_;
+}
+
+int GpuScene::side_stream(std::string& err) {
+    if (side_) return C2G_OK;
+    if (cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking) != cudaSuccess) {
+        err = "cannot create the side stream";
+        side_ = nullptr;
+        return C2G_ERR_CUDA;
+    }
+    for (int k = 0; k < 2; k++)
+        if (cudaEventCreateWithFlags(&fork_ev_[k], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&join_ev_[k], cudaEventDisableTiming) != cudaSuccess) {
+            err = "cannot create stream events";
+            return C2G_ERR_CUDA;
+        }
+    return C2G_OK;
 }
 
 // ---- small device helpers ------------------------------------------------------------------------
@@ -1175,6 +1196,16 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
     WaveBuffers& w = *wb_;
     unsigned long long* cnt = sb_->counts;
     launches = 0;
+    const bool overlap = overlap_ && side_stream(err) == C2G_OK;
+    // fork: the side stream waits for everything enqueued on st so far; join: st waits for the side
+    auto fork = [&](int k) {
+        cudaEventRecord(fork_ev_[k], st);
+        cudaStreamWaitEvent(side_, fork_ev_[k], 0);
+    };
+    auto join = [&](int k) {
+        cudaEventRecord(join_ev_[k], side_);
+        cudaStreamWaitEvent(st, join_ev_[k], 0);
+    };
     int* C = w.counters;
     C2G_CUDA(cudaMemsetAsync(C, 0, 256, st));
     PathRefs buf[2] = {{w.o[0], w.d[0], w.beta[0], w.L[0]}, {w.o[1], w.d[1], w.beta[1], w.L[1]}};
@@ -1218,12 +1249,28 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
             launches++;
         }
         ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc, w.mis_hit};
+        // the material buckets are independent (they append to the shared queues with atomics):
+        // with overlap every second present bucket shades on the side stream
+        if (overlap) fork(0);
+        int nb = 0;
         for (int bk = 0; bk < kBuckets; bk++) {
             if (!(present_buckets_ & (1 << bk))) continue;
             begin(C2G_K_SHADE);
-            launch_shade(bk, g_shade, st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so, gv, glevel);
+            launch_shade(bk, g_shade, (overlap && (nb & 1)) ? side_ : st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list,
+                         (int)w.P, so, gv, glevel);
             end();
             launches++;
+            nb++;
+        }
+        if (overlap) join(0);
+        // MIS rays (closest hit + emitter test) beside the shadow rays (any hit): disjoint inputs
+        // and outputs; both must finish before k_accumulate
+        if (overlap) {
+            fork(1);
+            begin(C2G_K_MIS);  // counts the launch (no timing events while overlapping)
+            if (count) k_mis<true><<<g_mis_c, 128, 0, side_>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
+            else k_mis<false><<<g_mis, 128, 0, side_>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
+            end();
         }
         begin(C2G_K_SHADOW);
         if (S.tree == C2G_TREE_SAH && S.sah_width == 4) {
@@ -1236,10 +1283,14 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
             k_shadow<false><<<g_sh, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
         }
         end();
-        begin(C2G_K_MIS);
-        if (count) k_mis<true><<<g_mis_c, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
-        else k_mis<false><<<g_mis, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
-        end();
+        if (overlap) {
+            join(1);
+        } else {
+            begin(C2G_K_MIS);
+            if (count) k_mis<true><<<g_mis_c, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
+            else k_mis<false><<<g_mis, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
+            end();
+        }
         begin(C2G_K_ACCUM);
         k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.mis_hit, w.out_L, C + cur, gv);
         end();
@@ -1299,6 +1350,9 @@ int GpuScene::capture_wave(const c2g_render_params& p, bool guide_sample, cudaSt
     const GuideView gv = plan.guided ? guide_.view(true, guide_sample) : GuideView{};
     auto no_begin = [](int) {};
     auto no_end = []() {};
+    overlap_ = true;
+    rc = side_stream(err);  // created before the capture starts
+    if (rc) return rc;
     C2G_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
     int launches = 0;
     rc = enqueue_wave(plan, a, gv, false, st, no_begin, no_end, launches, err);
@@ -1324,6 +1378,7 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
     const bool guided = plan.guided;
     const bool count = (counting_ & C2G_COUNT_TRAVERSAL) != 0;
     const bool timing = (counting_ & C2G_COUNT_TIMING) != 0;
+    overlap_ = !timing;  // per-kernel timing events need one stream
     unsigned long long* cnt = sb_->counts;
     if (count) C2G_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 3 * C2G_K_KINDS, st));
     // per-launch events (timing mode): a pool reused across calls

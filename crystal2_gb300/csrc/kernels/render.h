@@ -127,6 +127,13 @@ private:
     int guide_warmup_ = 2;     // guided waves that only record (BSDF sampling) before the mixture is used
     int guide_train_steps_ = 1;  // Adam steps per guided wave
     int guide_levels_ = 2;       // bounce levels served by the guide (0: all)
+    // Second stream of a wave: independent kernels of a bounce level (shading buckets, the MIS
+    // rays beside the shadow rays) run on it between fork and join events, in eager launches and
+    // in captured graphs alike.  Off while per-kernel timing events are recorded.
+    bool overlap_ = true;
+    cudaStream_t side_ = nullptr;
+    cudaEvent_t fork_ev_[2] = {nullptr, nullptr}, join_ev_[2] = {nullptr, nullptr};
+    int side_stream(std::string& err);
     float box_lo_[3] = {0, 0, 0}, box_hi_[3] = {1, 1, 1};  // scene bounds (network input range)
     c2g_stats stats_{};
     int film_w_ = 0, film_h_ = 0;
