@@ -255,7 +255,7 @@ __global__ void k_extend(DevScene S, const float4* __restrict__ qo, const float4
 // is finished writes its hit, appends the slot to its material bucket (all lanes join the keyed
 // append of every round; idle lanes with no key) and takes the next ray.
 template <bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads) k_extend_fetch(DevScene S, const float4* __restrict__ qo, const float4* __restrict__ qd,
+__global__ void __launch_bounds__(128) k_extend_fetch(DevScene S, const float4* __restrict__ qo, const float4* __restrict__ qd,
                                                       float4* hit, const int* qcount, int* zero_a, int* zero_b, int* zero_c,
                                                       int* bucket_cnt, int* bucket_list, int cap, int* fetch,
                                                       unsigned long long* cnt) {
@@ -267,11 +267,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_extend_fetch(DevScene S, cons
     bool exhausted = false;
     RayQ r;
     Hit h{INFINITY, 0.f, 0.f, -1};
-    __shared__ int sh_ref[kShStack * kTraceThreads];
-    __shared__ float sh_t[kShStack * kTraceThreads];
     Bvh4State st;
-    st.stack.sh = sh_ref + threadIdx.x;
-    st.stack_t.sh = sh_t + threadIdx.x;
     while (true) {
         const bool need = ray < 0 && !exhausted;
         const int idx = warp_fetch(fetch, need, n);
@@ -632,7 +628,7 @@ __global__ void k_shadow(DevScene S, const int* __restrict__ list, const int* co
 // slowest ray of its warp ends (persistent threads with ray replacement).  Same per-ray traversal
 // as trace_any_bvh4, so the same rays are occluded.
 template <bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads) k_shadow_fetch(DevScene S, const int* __restrict__ list, const int* count,
+__global__ void __launch_bounds__(128) k_shadow_fetch(DevScene S, const int* __restrict__ list, const int* count,
                                                       const float4* __restrict__ so, const float4* __restrict__ sd,
                                                       float4* sc, int* fetch, unsigned long long* cnt) {
     const int n = *count;
@@ -643,9 +639,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_shadow_fetch(DevScene S, cons
     RayQ r;
     float tmax = 0.f;
     int ign = -1;
-    __shared__ int sh_ref[kShStack * kTraceThreads];
     Bvh4AnyState st;
-    st.stack.sh = sh_ref + threadIdx.x;
     while (true) {
         const bool need = ray < 0 && !exhausted;
         const int idx = warp_fetch(fetch, need, n);
@@ -784,7 +778,7 @@ __global__ void k_trace_rays(DevScene S, int n, const float* o, const float* d, 
 }
 
 // Ray queries on four-wide nodes with dynamic fetch (same results as k_trace_rays).
-__global__ void __launch_bounds__(kTraceThreads) k_trace_rays_fetch(DevScene S, int n, const float* o, const float* d, const float* tmin,
+__global__ void __launch_bounds__(128) k_trace_rays_fetch(DevScene S, int n, const float* o, const float* d, const float* tmin,
                                                           const float* tmax, const int* ignore, int any_hit, int* obj,
                                                           float* t, int* fetch) {
     int ray = -1;
@@ -793,14 +787,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_rays_fetch(DevScene S, 
     float a = 0.f, b = INFINITY;
     int ig = -1;
     Hit h{INFINITY, 0.f, 0.f, -1};
-    // one shared column per lane serves both traversals (a lane runs one query at a time)
-    __shared__ int sh_ref[kShStack * kTraceThreads];
-    __shared__ float sh_t[kShStack * kTraceThreads];
     Bvh4State st;
     Bvh4AnyState sa;
-    st.stack.sh = sh_ref + threadIdx.x;
-    st.stack_t.sh = sh_t + threadIdx.x;
-    sa.stack.sh = sh_ref + threadIdx.x;
     while (true) {
         const bool need = ray < 0 && !exhausted;
         const int idx = warp_fetch(fetch, need, n);

@@ -570,30 +570,13 @@ __device__ __forceinline__ bool trace_any_bvh4(const DevScene& S, const RayQ& r,
 // One while-while round of the traversal above: inner nodes until every active lane of the warp
 // holds a leaf, then the leaves.  The state survives between rounds, so a kernel can hand a lane a
 // new ray as soon as its previous one is done (see k_shadow_fetch / k_extend_fetch).
-//
-// The lower kShStack entries of a lane's stack live in shared memory, one column per lane (entry k
-// of lane j at k * kTraceThreads + j: the 32 lanes of a warp always touch 32 distinct banks, however
-// deep each lane is); deeper entries spill to a local array.  The fetch kernels run 128-thread
-// blocks and hand each lane its column.
-constexpr int kTraceThreads = 128;
-constexpr int kShStack = 16;
-template <class T>
-struct HybridStack {
-    T* sh;                           // this lane's column of the block's shared stack
-    T loc[kStack4 - kShStack];
-    __device__ __forceinline__ T get(int k) const { return k < kShStack ? sh[k * kTraceThreads] : loc[k - kShStack]; }
-    __device__ __forceinline__ void set(int k, T v) {
-        if (k < kShStack) sh[k * kTraceThreads] = v;
-        else loc[k - kShStack] = v;
-    }
-};
 struct Bvh4AnyState {       // any hit: no entry distances
-    HybridStack<int> stack;
+    int stack[kStack4];
     int top, ref, leaf;
 };
 struct Bvh4State {          // closest hit: entry distance per stacked subtree
-    HybridStack<int> stack;
-    HybridStack<float> stack_t;
+    int stack[kStack4];
+    float stack_t[kStack4];
     int top, ref, leaf;
 };
 
@@ -624,13 +607,13 @@ __device__ __forceinline__ bool bvh4_any_round(const DevScene& S, const RayQ& r,
         if (top + 3 > kStack4) { dev_flag_error(S.err, DEVERR_STACK); top = 0; ref = kNoRef; leaf = kNoRef; break; }
         int next = kNoRef;
         if (h3) next = ch.w;
-        if (h2) { if (next != kNoRef) st.stack.set(top++, next); next = ch.z; }
-        if (h1) { if (next != kNoRef) st.stack.set(top++, next); next = ch.y; }
-        if (h0) { if (next != kNoRef) st.stack.set(top++, next); next = ch.x; }
-        ref = next != kNoRef ? next : (top ? st.stack.get(--top) : kNoRef);
+        if (h2) { if (next != kNoRef) st.stack[top++] = next; next = ch.z; }
+        if (h1) { if (next != kNoRef) st.stack[top++] = next; next = ch.y; }
+        if (h0) { if (next != kNoRef) st.stack[top++] = next; next = ch.x; }
+        ref = next != kNoRef ? next : (top ? st.stack[--top] : kNoRef);
         if (is_leaf(ref) && leaf == kNoRef) {
             leaf = ref;
-            ref = top ? st.stack.get(--top) : kNoRef;
+            ref = top ? st.stack[--top] : kNoRef;
         }
         if (!__any_sync(__activemask(), leaf == kNoRef)) break;
     }
@@ -644,7 +627,7 @@ __device__ __forceinline__ bool bvh4_any_round(const DevScene& S, const RayQ& r,
         leaf = kNoRef;
         if (!occluded && is_leaf(ref)) {
             leaf = ref;
-            ref = top ? st.stack.get(--top) : kNoRef;
+            ref = top ? st.stack[--top] : kNoRef;
         }
     }
     st.top = top;
@@ -661,7 +644,7 @@ __device__ __forceinline__ bool bvh4_closest_round(const DevScene& S, const RayQ
     auto pop = [&]() -> int {
         while (top > 0) {
             --top;
-            if (st.stack_t.get(top) <= h.t) return st.stack.get(top);
+            if (st.stack_t[top] <= h.t) return st.stack[top];
         }
         return kNoRef;
     };
@@ -686,7 +669,7 @@ __device__ __forceinline__ bool bvh4_closest_round(const DevScene& S, const RayQ
         if (top + 3 > kStack4) { dev_flag_error(S.err, DEVERR_STACK); top = 0; ref = kNoRef; leaf = kNoRef; break; }
 #pragma unroll
         for (int k = 3; k >= 1; k--)
-            if (c[k] != kNoRef) { st.stack.set(top, c[k]); st.stack_t.set(top, t[k]); top++; }
+            if (c[k] != kNoRef) { st.stack[top] = c[k]; st.stack_t[top] = t[k]; top++; }
         ref = c[0] != kNoRef ? c[0] : pop();
         if (is_leaf(ref) && leaf == kNoRef) {
             leaf = ref;
