@@ -128,8 +128,8 @@ private:
     int guide_train_steps_ = 1;  // Adam steps per guided wave
     int guide_levels_ = 2;       // bounce levels served by the guide (0: all)
     // Second stream of a wave: independent kernels of a bounce level (shading buckets, the MIS
-    // rays beside the shadow rays) run on it between fork and join events, in eager launches and
-    // in captured graphs alike.  Off while per-kernel timing events are recorded.
+    // rays beside the shadow rays) run on it between fork and join events.  Eager renders only:
+    // off while per-kernel timing events are recorded and in the graphs batched jobs replay.
     bool overlap_ = true;
     cudaStream_t side_ = nullptr;
     cudaEvent_t fork_ev_[2] = {nullptr, nullptr}, join_ev_[2] = {nullptr, nullptr};
