@@ -461,7 +461,8 @@ __device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, floa
 }
 
 __global__ void __launch_bounds__(256, 1) k_guide_train(GuideNet net, const float4* __restrict__ batch, const int* batch_count,
-                                                        int batch_cap, float* grad, float* stats) {
+                                                        int batch_cap, float* grad, float* stats, int splits,
+                                                        const int* __restrict__ step) {
     extern __shared__ __align__(16) unsigned char smem[];
     __nv_bfloat16* wts = reinterpret_cast<__nv_bfloat16*>(smem);
     __nv_bfloat16* wns = wts + kFwElems;
@@ -474,6 +475,10 @@ __global__ void __launch_bounds__(256, 1) k_guide_train(GuideNet net, const floa
     float* OF = reinterpret_cast<float*>(T + kTD1);
     const int n = min(*batch_count, batch_cap);
     const float mean_w = stats[2] / fmaxf(1.f, (float)n);
+    // minibatch of this Adam step: the batch split into `splits` windows, taken in turn, so the
+    // steps of one wave pass over the batch once
+    const int per = (n + splits - 1) / splits;
+    const int lo = min(n, (*step % splits) * per), hi = min(n, lo + per);
 
     float acc[kDwPerWarp][4];
 #pragma unroll
@@ -486,10 +491,10 @@ __global__ void __launch_bounds__(256, 1) k_guide_train(GuideNet net, const floa
     float loss = 0.f, wsum = 0.f;
 
     const int chunk = kTrainWarps * kTrainRows;
-    for (int base = blockIdx.x * chunk; base < n; base += gridDim.x * chunk) {
+    for (int base = lo + blockIdx.x * chunk; base < hi; base += gridDim.x * chunk) {
         const int s = lane & 15;
         const int j = base + warp * kTrainRows + s;
-        const bool valid = j < n;
+        const bool valid = j < hi;
         float3 wi = f3(0.f, 0.f, 1.f);
         float w = 0.f, pb = 0.f;
         if (lane < 16) {
@@ -780,7 +785,8 @@ void GuideTrainer::train(cudaStream_t st, const float4* out_L, int wave_paths, i
     const int grid = g_train_grid;
     GuideNet net = view(false, false).net;
     for (int s = 0; s < steps; s++) {
-        k_guide_train<<<grid, 256, kTrainSmem, st>>>(net, batch_, batch_count_, (int)rec_cap_, grad_, loss_acc_);
+        cudaMemsetAsync(loss_acc_, 0, 8, st);  // this step's loss and weight sum (Adam normalises by it)
+        k_guide_train<<<grid, 256, kTrainSmem, st>>>(net, batch_, batch_count_, (int)rec_cap_, grad_, loss_acc_, steps, step_dev_);
         steps_++;
         k_guide_adam<<<64, 256, 0, st>>>(params_, grad_, adam_m_, adam_v_, bf_, loss_acc_, lr_, 0.9f, 0.99f, 1e-8f, step_dev_);
         k_guide_tick<<<1, 1, 0, st>>>(step_dev_);
@@ -863,7 +869,7 @@ int GuideTrainer::gradient(DeviceArena& arena, const float* host_samples, int n,
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    k_guide_train<<<sms, 256, kTrainSmem>>>(view(false, false).net, db, batch_count_, n, grad_, loss_acc_);
+    k_guide_train<<<sms, 256, kTrainSmem>>>(view(false, false).net, db, batch_count_, n, grad_, loss_acc_, 1, step_dev_);
     int rc = C2G_OK;
     if (cudaDeviceSynchronize() != cudaSuccess) { err = cudaGetErrorString(cudaGetLastError()); rc = C2G_ERR_CUDA; }
     else {
