@@ -52,6 +52,7 @@ constexpr int kBucketMiss = 11;
 enum : int {
     DEVERR_STACK = 1,             // traversal stack overflow
     DEVERR_QUEUE = 2,             // queue capacity exceeded
+    DEVERR_WAIT = 4,              // a bounded wait on a tensor-core completion barrier ran out
 };
 
 }  // namespace c2g

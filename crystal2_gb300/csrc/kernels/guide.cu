@@ -16,6 +16,7 @@
 #include "guide.cuh"
 #include "render.h"
 #include "shade.cuh"
+#include "umma.cuh"
 
 namespace c2g {
 
@@ -26,7 +27,6 @@ namespace {
 constexpr int kLdA0 = 88;    // encoded inputs (80)
 constexpr int kLdH = 72;     // hidden activations / deltas (64)
 constexpr int kLdO = 56;     // output-layer gradient (48)
-constexpr int kLdF = 48;     // FP32 outputs (inference)
 constexpr int kLdOF = 52;    // FP32 outputs (training)
 
 // Padded weight copies in shared memory.  Forward: wt_l (N_l rows of K_l + 8).  Backward: wn_l
@@ -136,195 +136,175 @@ __device__ __forceinline__ void mma_rows(const __nv_bfloat16* in, int ldi, const
     }
 }
 
-// One hidden layer of a warp's 32 rows with the activations in registers: `a` holds the A
-// fragments of the layer input (two 16-row tiles, K/16 k-tiles), `an` receives the BF16 A
-// fragments of ReLU(a @ W + b) for the next layer.  The accumulator fragment of output columns
-// [16j, 16j + 8) and [16j + 8, 16j + 16) is exactly the next layer's A fragment of k-tile j
-// (rows g and g + 8, columns 2t, 2t + 1 and 2t + 8, 2t + 9), so no shared-memory round trip.
-template <int K, int N>
-__device__ __forceinline__ void layer_relu_reg(const uint32_t (&a)[2][K / 16][4], const __nv_bfloat16* w, int ldw,
-                                               const float* __restrict__ bias, uint32_t (&an)[2][N / 16][4]) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int j = 0; j < N / 16; j++) {
-        float d[2][2][4];
-#pragma unroll
-        for (int hf = 0; hf < 2; hf++) {
-            const int n0 = 16 * j + 8 * hf;
-            const float b0 = __ldg(bias + n0 + 2 * t), b1 = __ldg(bias + n0 + 2 * t + 1);
-#pragma unroll
-            for (int m = 0; m < 2; m++) { d[hf][m][0] = b0; d[hf][m][1] = b1; d[hf][m][2] = b0; d[hf][m][3] = b1; }
-#pragma unroll
-            for (int kk = 0; kk < K / 16; kk++) {
-                uint32_t b[2];
-                const __nv_bfloat16* wr = w + (n0 + g) * ldw + kk * 16 + 2 * t;
-                b[0] = ld32(wr);
-                b[1] = ld32(wr + 8);
-#pragma unroll
-                for (int m = 0; m < 2; m++) mma16816(d[hf][m], a[m][kk], b);
-            }
-        }
-#pragma unroll
-        for (int m = 0; m < 2; m++) {
-            an[m][j][0] = pack_bf16(fmaxf(d[0][m][0], 0.f), fmaxf(d[0][m][1], 0.f));
-            an[m][j][1] = pack_bf16(fmaxf(d[0][m][2], 0.f), fmaxf(d[0][m][3], 0.f));
-            an[m][j][2] = pack_bf16(fmaxf(d[1][m][0], 0.f), fmaxf(d[1][m][1], 0.f));
-            an[m][j][3] = pack_bf16(fmaxf(d[1][m][2], 0.f), fmaxf(d[1][m][3], 0.f));
-        }
-    }
-}
-
-// Forward pass of one warp's 32 samples: A holds the encoded inputs (ld kLdA0); the FP32 outputs
-// land in F (ld kLdF), which aliases A.  `wts` = padded forward weights.  The hidden activations
-// stay in registers (BF16 A fragments), rounded exactly as the tiled training pass rounds them.
-__device__ __forceinline__ void warp_forward32(const GuideNet& net, const __nv_bfloat16* wts, const __nv_bfloat16* A,
-                                               float* F) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    uint32_t a0[2][5][4];
-#pragma unroll
-    for (int m = 0; m < 2; m++)
-#pragma unroll
-        for (int kk = 0; kk < 5; kk++) {
-            const __nv_bfloat16* r0 = A + (m * 16 + g) * kLdA0 + kk * 16 + 2 * t;
-            a0[m][kk][0] = ld32(r0);
-            a0[m][kk][1] = ld32(r0 + 8 * kLdA0);
-            a0[m][kk][2] = ld32(r0 + 8);
-            a0[m][kk][3] = ld32(r0 + 8 * kLdA0 + 8);
-        }
-    __syncwarp();  // every lane has its input fragments before F (aliasing A) is written
-    uint32_t a1[2][4][4], a2[2][4][4];
-    layer_relu_reg<80, 64>(a0, wts + fw_off(0), fw_ld(0), net.params + guide_b_off(0), a1);
-    layer_relu_reg<64, 64>(a1, wts + fw_off(1), fw_ld(1), net.params + guide_b_off(1), a2);
-    layer_relu_reg<64, 64>(a2, wts + fw_off(2), fw_ld(2), net.params + guide_b_off(2), a1);
-    const float* bias = net.params + guide_b_off(3);
-    const __nv_bfloat16* w = wts + fw_off(3);
-#pragma unroll
-    for (int n0 = 0; n0 < 48; n0 += 8) {
-        float d[2][4];
-        const float b0 = __ldg(bias + n0 + 2 * t), b1 = __ldg(bias + n0 + 2 * t + 1);
-#pragma unroll
-        for (int m = 0; m < 2; m++) { d[m][0] = b0; d[m][1] = b1; d[m][2] = b0; d[m][3] = b1; }
-#pragma unroll
-        for (int kk = 0; kk < 4; kk++) {
-            uint32_t b[2];
-            const __nv_bfloat16* wr = w + (n0 + g) * fw_ld(3) + kk * 16 + 2 * t;
-            b[0] = ld32(wr);
-            b[1] = ld32(wr + 8);
-#pragma unroll
-            for (int m = 0; m < 2; m++) mma16816(d[m], a1[m][kk], b);
-        }
-#pragma unroll
-        for (int m = 0; m < 2; m++) {
-            const int r0 = m * 16 + g, c = n0 + 2 * t;
-            F[r0 * kLdF + c] = d[m][0];
-            F[r0 * kLdF + c + 1] = d[m][1];
-            F[(r0 + 8) * kLdF + c] = d[m][2];
-            F[(r0 + 8) * kLdF + c + 1] = d[m][3];
-        }
-    }
-    __syncwarp();
-}
-
 __device__ __forceinline__ void store_inputs(__nv_bfloat16* row, const float* in) {
 #pragma unroll
     for (int k = 0; k < kGuideIn; k += 2) *reinterpret_cast<uint32_t*>(row + k) = pack_bf16(in[k], in[k + 1]);
 }
 
-// ---- inference ---------------------------------------------------------------------------------
-// 256 threads, 32 samples per warp; dynamic shared memory: padded forward weights + per warp an
-// input/output tile (the FP32 outputs overwrite the inputs; hidden activations live in registers).
-constexpr int kInferWarps = 8;
-constexpr int kInferThreads = 32 * kInferWarps;
-constexpr int kTileA = 32 * kLdF * 4;      // 6144 B: 32 x 88 BF16 inputs or 32 x 48 FP32 outputs
-static_assert(32 * kLdA0 * 2 <= kTileA, "input tile fits the output tile");
-constexpr size_t kInferSmem = kFwElems * 2 + kInferWarps * kTileA;
+// ---- inference on the fifth-generation tensor cores (tcgen05) -----------------------------------
+// One warpgroup (128 threads) per CTA and 128 vertices per tile, one per thread and per
+// tensor-memory lane.  Per layer a single thread issues K/16 tcgen05.mma (M = 128, N = 64 or 48,
+// BF16 operands from shared memory, FP32 accumulator in tensor memory) and commits them to an
+// mbarrier; every thread then reads its row of the accumulator (tcgen05.ld), adds the bias,
+// applies ReLU, rounds to BF16 and writes the next layer's operand row.  Operands are K-major
+// 8-row x 16-byte core matrices without swizzle: element (r, k) of a K-column operand sits at
+// (r / 8) * 16K + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2 bytes, so one K=16 step spans two
+// core matrices 128 B apart (descriptor LBO) and 8-row groups are 16K bytes apart (SBO).
+constexpr int kTcRows = 128;
+__host__ __device__ constexpr int tc_w_off(int l) { return l == 0 ? 0 : tc_w_off(l - 1) + guide_n(l - 1) * guide_k(l - 1) * 2; }
+constexpr int kTcA0 = tc_w_off(4);                      // 32768: inputs (K = 80) / layer-2 activations
+constexpr int kTcA1 = kTcA0 + kTcRows * kGuideIn * 2;   // hidden activations (K = 64)
+constexpr int kTcBias = kTcA1 + kTcRows * kGuideHidden * 2;
+constexpr int kTcBiasN = 3 * kGuideHidden + kGuideOutPad;
+constexpr int kTcBar = kTcBias + kTcBiasN * 4;
+constexpr int kTcTmemSlot = kTcBar + 8;
+constexpr size_t kTcSmem = (size_t)kTcTmemSlot + 8;
+constexpr uint32_t kTcCols = 64;                        // tensor-memory columns per CTA
+constexpr uint32_t kTcWaitPolls = 1u << 22;
+static_assert(kTcA0 % 128 == 0 && kTcA1 % 128 == 0 && kTcBar % 8 == 0, "operand and barrier alignment");
 
-__global__ void __launch_bounds__(kInferThreads, 2) k_guide_infer(DevScene S, GuideNet net, const float4* __restrict__ ray_o,
-                                                     const float4* __restrict__ ray_d, const float4* __restrict__ hits,
-                                                     const int* bucket_cnt, const int* __restrict__ bucket_list, int cap,
-                                                     int mask, float* out) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __nv_bfloat16* wts = reinterpret_cast<__nv_bfloat16*>(smem);
-    stage_forward_weights(net, wts);
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* wbase = smem + kFwElems * 2 + warp * kTileA;
-    __nv_bfloat16* A = reinterpret_cast<__nv_bfloat16*>(wbase);
-    float* F = reinterpret_cast<float*>(wbase);
-    // work list = the guided buckets back to back; their prefix offsets live in shared memory
-    __shared__ int bend[kBuckets];
-    if (threadIdx.x == 0) {
-        int total = 0;
-        for (int b = 0; b < kBuckets; b++) {
-            total += ((mask >> b) & 1) ? bucket_cnt[b] : 0;
-            bend[b] = total;
-        }
-    }
-    __syncthreads();
-    const int total = bend[kBuckets - 1];
-    const int gwarp = blockIdx.x * kInferWarps + warp, nwarps = gridDim.x * kInferWarps;
-    for (int base = gwarp * 32; base < total; base += nwarps * 32) {
-        int item = base + lane;
-        int slot = -1;
-        if (item < total) {
-            int b = 0;
-            while (b < kBuckets - 1 && item >= bend[b]) b++;
-            slot = bucket_list[(size_t)b * cap + (item - (b ? bend[b - 1] : 0))];
-        }
-        float in[kGuideIn];
-        if (slot >= 0) {
-            float4 o4 = ray_o[slot], d4 = ray_d[slot], h4 = hits[slot];
-            Hit h{h4.x, h4.y, h4.z, __float_as_int(h4.w)};
-            Surface s;
-            make_surface(S, f3(o4), f3(d4), h, s);
-            guide_encode(net, s.pos, s.N, -f3(d4), in);
-        } else {
+__device__ __forceinline__ int tc_cm(int r, int k, int K) { return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2; }
+
+// One row (this thread's vertex) of a K-column operand from K floats, rounded to BF16.
+template <int K>
+__device__ __forceinline__ void tc_store_row(unsigned char* base, int r, const float* v) {
 #pragma unroll
-            for (int k = 0; k < kGuideIn; k++) in[k] = 0.f;
-        }
-        store_inputs(A + lane * kLdA0, in);
-        __syncwarp();
-        warp_forward32(net, wts, A, F);
-        if (slot >= 0) {
-            float o[kGuideOut];
-#pragma unroll
-            for (int k = 0; k < kGuideOut; k++) o[k] = F[lane * kLdF + k];
-            pack_lobes(o, out + (size_t)slot * kGuidePacked);
-        }
-        __syncwarp();
+    for (int c = 0; c < K / 8; c++) {
+        uint4 q;
+        q.x = pack_bf16(v[8 * c + 0], v[8 * c + 1]);
+        q.y = pack_bf16(v[8 * c + 2], v[8 * c + 3]);
+        q.z = pack_bf16(v[8 * c + 4], v[8 * c + 5]);
+        q.w = pack_bf16(v[8 * c + 6], v[8 * c + 7]);
+        *reinterpret_cast<uint4*>(base + tc_cm(r, 8 * c, K)) = q;
     }
 }
 
-// Forward pass over explicit inputs (x, n, wo as 9 floats per sample): the same tiles as
-// k_guide_infer, used to check the network against the oracle.
-__global__ void __launch_bounds__(kInferThreads, 2) k_guide_eval(GuideNet net, const float* __restrict__ xnw, int n, float* out) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __nv_bfloat16* wts = reinterpret_cast<__nv_bfloat16*>(smem);
-    stage_forward_weights(net, wts);
+// MODE 0: vertices of the guided buckets (surface + encoding), packed mixtures per queue slot.
+// MODE 1: explicit inputs xnw (9 floats each), raw outputs (kGuideOut floats each).
+template <int MODE>
+__global__ void __launch_bounds__(kTcRows) k_guide_infer_tc(DevScene S, GuideNet net, const float4* __restrict__ ray_o,
+                                                           const float4* __restrict__ ray_d, const float4* __restrict__ hits,
+                                                           const int* bucket_cnt, const int* __restrict__ bucket_list,
+                                                           int cap, int mask, const float* __restrict__ xnw, int n_in,
+                                                           float* out, int* err) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    float* bias = reinterpret_cast<float*>(smem + kTcBias);
+    const uint32_t bar = smem_u32(smem + kTcBar);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kTcTmemSlot);
+    // weights -> core-matrix layout; biases
+#pragma unroll
+    for (int l = 0; l < kGuideLayers; l++) {
+        const int K = guide_k(l), N = guide_n(l), vpr = K / 8;
+        const uint4* src = reinterpret_cast<const uint4*>(net.bf + guide_bf_off(l));  // wt: N x K, K contiguous
+        for (int i = tid; i < N * vpr; i += kTcRows) {
+            const int nn = i / vpr, c = i - nn * vpr;
+            *reinterpret_cast<uint4*>(smem + tc_w_off(l) + tc_cm(nn, 8 * c, K)) = src[i];
+        }
+    }
+    for (int i = tid; i < kTcBiasN; i += kTcRows) {
+        const int l = i < 3 * kGuideHidden ? i / kGuideHidden : 3;
+        const int j = i - l * kGuideHidden;
+        bias[i] = net.params[guide_b_off(l) + j];
+    }
+    __shared__ int bend[kBuckets];
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        if (MODE == 0) {
+            int total = 0;
+            for (int b = 0; b < kBuckets; b++) {
+                total += ((mask >> b) & 1) ? bucket_cnt[b] : 0;
+                bend[b] = total;
+            }
+        }
+    }
+    if (warp == 0) tmem_alloc(smem_u32(tslot), kTcCols);
+    fence_async_smem();
+    tc_fence_before();
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* wbase = smem + kFwElems * 2 + warp * kTileA;
-    __nv_bfloat16* A = reinterpret_cast<__nv_bfloat16*>(wbase);
-    float* F = reinterpret_cast<float*>(wbase);
-    const int gwarp = blockIdx.x * kInferWarps + warp, nwarps = gridDim.x * kInferWarps;
-    for (int base = gwarp * 32; base < n; base += nwarps * 32) {
-        const int j = base + lane;
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 lanes
+    const int total = MODE == 0 ? bend[kBuckets - 1] : n_in;
+    uint32_t phase = 0;
+    bool failed = false;
+    for (int base = blockIdx.x * kTcRows; base < total && !failed; base += gridDim.x * kTcRows) {
+        const int item = base + tid;
+        int slot = -1;
         float in[kGuideIn];
-        if (j < n) {
-            const float* v = xnw + (size_t)9 * j;
-            guide_encode(net, f3(v[0], v[1], v[2]), f3(v[3], v[4], v[5]), f3(v[6], v[7], v[8]), in);
-        } else {
 #pragma unroll
-            for (int k = 0; k < kGuideIn; k++) in[k] = 0.f;
+        for (int k = 0; k < kGuideIn; k++) in[k] = 0.f;
+        if (item < total) {
+            if (MODE == 0) {
+                int b = 0;
+                while (b < kBuckets - 1 && item >= bend[b]) b++;
+                slot = bucket_list[(size_t)b * cap + (item - (b ? bend[b - 1] : 0))];
+                const float4 o4 = ray_o[slot], d4 = ray_d[slot], h4 = hits[slot];
+                Hit h{h4.x, h4.y, h4.z, __float_as_int(h4.w)};
+                Surface sf;
+                make_surface(S, f3(o4), f3(d4), h, sf);
+                guide_encode(net, sf.pos, sf.N, -f3(d4), in);
+            } else {
+                slot = item;
+                const float* v = xnw + (size_t)9 * item;
+                guide_encode(net, f3(v[0], v[1], v[2]), f3(v[3], v[4], v[5]), f3(v[6], v[7], v[8]), in);
+            }
         }
-        store_inputs(A + lane * kLdA0, in);
-        __syncwarp();
-        warp_forward32(net, wts, A, F);
-        if (j < n) {
+        tc_store_row<kGuideIn>(smem + kTcA0, tid, in);
+        float o[kGuideOutPad];
 #pragma unroll
-            for (int k = 0; k < kGuideOut; k++) out[(size_t)j * kGuideOut + k] = F[lane * kLdF + k];
+        for (int l = 0; l < kGuideLayers; l++) {
+            const int K = guide_k(l), N = guide_n(l);
+            const int a_off = (l == 0 || l == 2) ? kTcA0 : kTcA1;
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(smem + a_off), b0 = smem_u32(smem + tc_w_off(l));
+                const uint32_t idesc = umma_idesc_bf16(kTcRows, N);
+                for (int kk = 0; kk < K / 16; kk++)
+                    umma_bf16(tmem, umma_desc(a0 + kk * 256, 128, K * 16), umma_desc(b0 + kk * 256, 128, K * 16), idesc, kk > 0);
+                umma_commit(bar);
+            }
+            const bool ok = mbar_wait(bar, phase, kTcWaitPolls);
+            phase ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) dev_flag_error(err, DEVERR_WAIT);
+                // let anything still in flight finish (bounded) before the tensor memory is freed
+                mbar_wait(bar, phase ^ 1u, kTcWaitPolls);
+                failed = true;
+                break;
+            }
+            tc_fence_after();
+            float v[64];
+#pragma unroll
+            for (int c = 0; c < 64; c += 16)
+                if (c < N) tmem_ld16(trow + c, v + c);
+            if (l < kGuideLayers - 1) {
+#pragma unroll
+                for (int j = 0; j < 64; j++) v[j] = fmaxf(v[j] + bias[l * kGuideHidden + j], 0.f);
+                tc_store_row<kGuideHidden>(smem + ((l == 0 || l == 2) ? kTcA1 : kTcA0), tid, v);
+            } else {
+#pragma unroll
+                for (int j = 0; j < kGuideOutPad; j++) o[j] = v[j] + bias[3 * kGuideHidden + j];
+            }
         }
-        __syncwarp();
+        if (failed) break;
+        if (item < total) {
+            if (MODE == 0) pack_lobes(o, out + (size_t)slot * kGuidePacked);
+            else {
+#pragma unroll
+                for (int k = 0; k < kGuideOut; k++) out[(size_t)slot * kGuideOut + k] = o[k];
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_free(tmem, kTcCols);
     }
 }
 
@@ -463,7 +443,7 @@ __device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, floa
 __global__ void __launch_bounds__(256, 1) k_guide_train(GuideNet net, const float4* __restrict__ batch, const int* batch_count,
                                                         int batch_cap, float* grad, float* stats, int splits,
                                                         const int* __restrict__ step) {
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     __nv_bfloat16* wts = reinterpret_cast<__nv_bfloat16*>(smem);
     __nv_bfloat16* wns = wts + kFwElems;
     __nv_bfloat16* tiles = wns + kBwElems;
@@ -722,9 +702,9 @@ int GuideTrainer::init(DeviceArena& arena, size_t paths, int max_depth, const fl
         cudaMemset(adam_m_, 0, kGuideParams * 4);
         cudaMemset(adam_v_, 0, kGuideParams * 4);
         k_guide_bf16_from_params<<<64, 256>>>(params_, bf_);
-        cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
+        cudaFuncSetAttribute(k_guide_infer_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+        cudaFuncSetAttribute(k_guide_infer_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
         cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem);
-        cudaFuncSetAttribute(k_guide_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
         steps_ = 0;
     }
     for (int a = 0; a < 3; a++) {
@@ -759,7 +739,8 @@ void GuideTrainer::prepare_launch() {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_infer, kInferThreads, kInferSmem);
+    cudaFuncSetAttribute(k_guide_infer_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_infer_tc<0>, kTcRows, kTcSmem);
     g_infer_grid = std::max(1, sms * std::max(1, per));
     g_train_grid = std::max(1, sms);
 }
@@ -772,8 +753,9 @@ void GuideTrainer::infer(cudaStream_t st, const void* Sv, const float4* ray_o, c
     for (int b = 0; b < kBuckets; b++)
         if (((bucket_mask >> b) & 1) && bucket_guided(b)) mask |= 1 << b;
     if (!mask) return;
-    k_guide_infer<<<grid, kInferThreads, kInferSmem, st>>>(*static_cast<const DevScene*>(Sv), view(false, false).net, ray_o, ray_d, hits,
-                                                bucket_cnt, bucket_list, cap, mask, out_);
+    const DevScene& S = *static_cast<const DevScene*>(Sv);
+    k_guide_infer_tc<0><<<grid, kTcRows, kTcSmem, st>>>(S, view(false, false).net, ray_o, ray_d, hits, bucket_cnt, bucket_list,
+                                                        cap, mask, nullptr, 0, out_, S.err);
 }
 
 void GuideTrainer::train(cudaStream_t st, const float4* out_L, int wave_paths, int steps) {
@@ -833,17 +815,26 @@ int GuideTrainer::eval(DeviceArena& arena, const float* host_xnw, int n, float* 
     if (n <= 0) return C2G_OK;
     float* din = (float*)arena.alloc((size_t)n * 9 * 4, err);
     float* dout = (float*)arena.alloc((size_t)n * kGuideOut * 4, err);
+    int* derr = (int*)arena.alloc(16, err);
     int rc = C2G_OK;
-    if (!din || !dout) rc = C2G_ERR_OOM;
+    if (!din || !dout || !derr) rc = C2G_ERR_OOM;
     if (!rc) {
         cudaMemcpy(din, host_xnw, (size_t)n * 9 * 4, cudaMemcpyHostToDevice);
-        int blocks = std::min(1024, (n + kInferThreads - 1) / kInferThreads);
-        k_guide_eval<<<blocks, kInferThreads, kInferSmem>>>(view(false, false).net, din, n, dout);
+        cudaMemset(derr, 0, 16);
+        prepare_launch();
+        const int blocks = std::min(g_infer_grid, (n + kTcRows - 1) / kTcRows);
+        k_guide_infer_tc<1><<<blocks, kTcRows, kTcSmem>>>(DevScene{}, view(false, false).net, nullptr, nullptr, nullptr, nullptr,
+                                                          nullptr, 0, 0, din, n, dout, derr);
+        int h = 0;
         if (cudaDeviceSynchronize() != cudaSuccess) { err = cudaGetErrorString(cudaGetLastError()); rc = C2G_ERR_CUDA; }
-        else cudaMemcpy(host_out, dout, (size_t)n * kGuideOut * 4, cudaMemcpyDeviceToHost);
+        else if (cudaMemcpy(&h, derr, 4, cudaMemcpyDeviceToHost) == cudaSuccess && h) {
+            err = "guide inference: tensor-core completion wait timed out";
+            rc = C2G_ERR_DEVICE;
+        } else cudaMemcpy(host_out, dout, (size_t)n * kGuideOut * 4, cudaMemcpyDeviceToHost);
     }
     if (din) arena.free(din);
     if (dout) arena.free(dout);
+    if (derr) arena.free(derr);
     return rc;
 }
 

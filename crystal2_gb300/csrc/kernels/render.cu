@@ -1055,7 +1055,8 @@ int GpuScene::check_device_error(std::string& err) {
     C2G_CUDA(cudaMemcpy(h, sb_->err, sizeof(h), cudaMemcpyDeviceToHost));
     if (h[0]) {
         err = "device error word " + std::to_string(h[0]) + ((h[0] & DEVERR_STACK) ? " (traversal stack overflow)" : "") +
-              ((h[0] & DEVERR_QUEUE) ? " (queue overflow)" : "");
+              ((h[0] & DEVERR_QUEUE) ? " (queue overflow)" : "") +
+              ((h[0] & DEVERR_WAIT) ? " (tensor-core completion wait timed out)" : "");
         cudaMemset(sb_->err, 0, sizeof(int));
         return C2G_ERR_DEVICE;
     }
