@@ -142,26 +142,33 @@ __device__ __forceinline__ void store_inputs(__nv_bfloat16* row, const float* in
 }
 
 // ---- inference on the fifth-generation tensor cores (tcgen05) -----------------------------------
-// One warpgroup (128 threads) per CTA and 128 vertices per tile, one per thread and per
-// tensor-memory lane.  Per layer a single thread issues K/16 tcgen05.mma (M = 128, N = 64 or 48,
-// BF16 operands from shared memory, FP32 accumulator in tensor memory) and commits them to an
-// mbarrier; every thread then reads its row of the accumulator (tcgen05.ld), adds the bias,
-// applies ReLU, rounds to BF16 and writes the next layer's operand row.  Operands are K-major
-// 8-row x 16-byte core matrices without swizzle: element (r, k) of a K-column operand sits at
-// (r / 8) * 16K + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2 bytes, so one K=16 step spans two
-// core matrices 128 B apart (descriptor LBO) and 8-row groups are 16K bytes apart (SBO).
+// Two warpgroups per CTA share the staged weights; each warpgroup runs its own 128-vertex tiles,
+// one vertex per thread and per tensor-memory lane, with its own operand buffers, 64 tensor-memory
+// columns, mbarrier and named barrier.  Per layer one thread of the warpgroup issues K/16
+// tcgen05.mma (M = 128, N = 64 or 48, BF16 operands from shared memory, FP32 accumulator in
+// tensor memory) and commits them to the mbarrier; every thread then reads its accumulator row
+// (tcgen05.ld), adds the bias, applies ReLU, rounds to BF16 and writes the next layer's operand
+// row.  Operands are K-major 8-row x 16-byte core matrices without swizzle: element (r, k) of a
+// K-column operand sits at (r / 8) * 16K + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2 bytes, so one
+// K=16 step spans two core matrices 128 B apart (descriptor LBO) and 8-row groups are 16K bytes
+// apart (SBO).
 constexpr int kTcRows = 128;
+constexpr int kTcGroups = 2;                            // warpgroups per CTA
+constexpr int kTcThreads = kTcRows * kTcGroups;
 __host__ __device__ constexpr int tc_w_off(int l) { return l == 0 ? 0 : tc_w_off(l - 1) + guide_n(l - 1) * guide_k(l - 1) * 2; }
-constexpr int kTcA0 = tc_w_off(4);                      // 32768: inputs (K = 80) / layer-2 activations
-constexpr int kTcA1 = kTcA0 + kTcRows * kGuideIn * 2;   // hidden activations (K = 64)
-constexpr int kTcBias = kTcA1 + kTcRows * kGuideHidden * 2;
+constexpr int kTcGroupBytes = kTcRows * kGuideIn * 2 + kTcRows * kGuideHidden * 2;  // A0 + A1
+__host__ __device__ constexpr int tc_a0(int g) { return tc_w_off(4) + g * kTcGroupBytes; }
+__host__ __device__ constexpr int tc_a1(int g) { return tc_a0(g) + kTcRows * kGuideIn * 2; }
+constexpr int kTcBias = tc_w_off(4) + kTcGroups * kTcGroupBytes;
 constexpr int kTcBiasN = 3 * kGuideHidden + kGuideOutPad;
-constexpr int kTcBar = kTcBias + kTcBiasN * 4;
-constexpr int kTcTmemSlot = kTcBar + 8;
+constexpr int kTcBar = kTcBias + kTcBiasN * 4;          // one mbarrier per warpgroup
+constexpr int kTcTmemSlot = kTcBar + 8 * kTcGroups;
 constexpr size_t kTcSmem = (size_t)kTcTmemSlot + 8;
-constexpr uint32_t kTcCols = 64;                        // tensor-memory columns per CTA
+constexpr uint32_t kTcColsPerGroup = 64;
+constexpr uint32_t kTcCols = kTcColsPerGroup * kTcGroups;  // tensor-memory columns per CTA (power of 2)
 constexpr uint32_t kTcWaitPolls = 1u << 22;
-static_assert(kTcA0 % 128 == 0 && kTcA1 % 128 == 0 && kTcBar % 8 == 0, "operand and barrier alignment");
+static_assert(tc_a0(0) % 128 == 0 && tc_a1(0) % 128 == 0 && kTcGroupBytes % 128 == 0 && kTcBar % 8 == 0,
+              "operand and barrier alignment");
 
 __device__ __forceinline__ int tc_cm(int r, int k, int K) { return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2; }
 
@@ -182,34 +189,34 @@ __device__ __forceinline__ void tc_store_row(unsigned char* base, int r, const f
 // MODE 0: vertices of the guided buckets (surface + encoding), packed mixtures per queue slot.
 // MODE 1: explicit inputs xnw (9 floats each), raw outputs (kGuideOut floats each).
 template <int MODE>
-__global__ void __launch_bounds__(kTcRows) k_guide_infer_tc(DevScene S, GuideNet net, const float4* __restrict__ ray_o,
-                                                           const float4* __restrict__ ray_d, const float4* __restrict__ hits,
-                                                           const int* bucket_cnt, const int* __restrict__ bucket_list,
-                                                           int cap, int mask, const float* __restrict__ xnw, int n_in,
-                                                           float* out, int* err) {
+__global__ void __launch_bounds__(kTcThreads) k_guide_infer_tc(DevScene S, GuideNet net, const float4* __restrict__ ray_o,
+                                                              const float4* __restrict__ ray_d, const float4* __restrict__ hits,
+                                                              const int* bucket_cnt, const int* __restrict__ bucket_list,
+                                                              int cap, int mask, const float* __restrict__ xnw, int n_in,
+                                                              float* out, int* err) {
     extern __shared__ __align__(128) unsigned char smem[];
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int grp = threadIdx.x / kTcRows, row = threadIdx.x - grp * kTcRows, warp = threadIdx.x >> 5;
     float* bias = reinterpret_cast<float*>(smem + kTcBias);
-    const uint32_t bar = smem_u32(smem + kTcBar);
+    const uint32_t bar = smem_u32(smem + kTcBar + 8 * grp);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kTcTmemSlot);
     // weights -> core-matrix layout; biases
 #pragma unroll
     for (int l = 0; l < kGuideLayers; l++) {
         const int K = guide_k(l), N = guide_n(l), vpr = K / 8;
         const uint4* src = reinterpret_cast<const uint4*>(net.bf + guide_bf_off(l));  // wt: N x K, K contiguous
-        for (int i = tid; i < N * vpr; i += kTcRows) {
+        for (int i = threadIdx.x; i < N * vpr; i += kTcThreads) {
             const int nn = i / vpr, c = i - nn * vpr;
             *reinterpret_cast<uint4*>(smem + tc_w_off(l) + tc_cm(nn, 8 * c, K)) = src[i];
         }
     }
-    for (int i = tid; i < kTcBiasN; i += kTcRows) {
+    for (int i = threadIdx.x; i < kTcBiasN; i += kTcThreads) {
         const int l = i < 3 * kGuideHidden ? i / kGuideHidden : 3;
         const int j = i - l * kGuideHidden;
         bias[i] = net.params[guide_b_off(l) + j];
     }
     __shared__ int bend[kBuckets];
-    if (tid == 0) {
-        mbar_init(bar, 1);
+    if (threadIdx.x == 0) {
+        for (int g = 0; g < kTcGroups; g++) mbar_init(smem_u32(smem + kTcBar + 8 * g), 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         if (MODE == 0) {
             int total = 0;
@@ -224,13 +231,16 @@ __global__ void __launch_bounds__(kTcRows) k_guide_infer_tc(DevScene S, GuideNet
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *tslot;
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 lanes
+    const uint32_t tmem = *tslot + grp * kTcColsPerGroup;             // this warpgroup's columns
+    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's 32 lanes
+    unsigned char* A0 = smem + tc_a0(grp);
+    unsigned char* A1 = smem + tc_a1(grp);
+    const int bar_id = 1 + grp;
     const int total = MODE == 0 ? bend[kBuckets - 1] : n_in;
     uint32_t phase = 0;
     bool failed = false;
-    for (int base = blockIdx.x * kTcRows; base < total && !failed; base += gridDim.x * kTcRows) {
-        const int item = base + tid;
+    for (int base = (blockIdx.x * kTcGroups + grp) * kTcRows; base < total && !failed; base += gridDim.x * kTcThreads) {
+        const int item = base + row;
         int slot = -1;
         float in[kGuideIn];
 #pragma unroll
@@ -251,18 +261,18 @@ __global__ void __launch_bounds__(kTcRows) k_guide_infer_tc(DevScene S, GuideNet
                 guide_encode(net, f3(v[0], v[1], v[2]), f3(v[3], v[4], v[5]), f3(v[6], v[7], v[8]), in);
             }
         }
-        tc_store_row<kGuideIn>(smem + kTcA0, tid, in);
+        tc_store_row<kGuideIn>(A0, row, in);
         float o[kGuideOutPad];
 #pragma unroll
         for (int l = 0; l < kGuideLayers; l++) {
             const int K = guide_k(l), N = guide_n(l);
-            const int a_off = (l == 0 || l == 2) ? kTcA0 : kTcA1;
+            unsigned char* Ain = (l == 0 || l == 2) ? A0 : A1;
             fence_async_smem();
             tc_fence_before();
-            __syncthreads();
-            if (tid == 0) {
+            wg_sync(bar_id);
+            if (row == 0) {
                 tc_fence_after();
-                const uint32_t a0 = smem_u32(smem + a_off), b0 = smem_u32(smem + tc_w_off(l));
+                const uint32_t a0 = smem_u32(Ain), b0 = smem_u32(smem + tc_w_off(l));
                 const uint32_t idesc = umma_idesc_bf16(kTcRows, N);
                 for (int kk = 0; kk < K / 16; kk++)
                     umma_bf16(tmem, umma_desc(a0 + kk * 256, 128, K * 16), umma_desc(b0 + kk * 256, 128, K * 16), idesc, kk > 0);
@@ -270,25 +280,27 @@ __global__ void __launch_bounds__(kTcRows) k_guide_infer_tc(DevScene S, GuideNet
             }
             const bool ok = mbar_wait(bar, phase, kTcWaitPolls);
             phase ^= 1u;
-            if (__syncthreads_or(!ok)) {
-                if (tid == 0) dev_flag_error(err, DEVERR_WAIT);
+            if (wg_sync_or(bar_id, !ok)) {
+                if (row == 0) dev_flag_error(err, DEVERR_WAIT);
                 // let anything still in flight finish (bounded) before the tensor memory is freed
                 mbar_wait(bar, phase ^ 1u, kTcWaitPolls);
                 failed = true;
                 break;
             }
             tc_fence_after();
-            float v[64];
+            uint32_t r[64];
 #pragma unroll
             for (int c = 0; c < 64; c += 16)
-                if (c < N) tmem_ld16(trow + c, v + c);
+                if (c < N) tmem_ld16(trow + c, r + c);
+            tmem_wait();
             if (l < kGuideLayers - 1) {
+                float v[64];
 #pragma unroll
-                for (int j = 0; j < 64; j++) v[j] = fmaxf(v[j] + bias[l * kGuideHidden + j], 0.f);
-                tc_store_row<kGuideHidden>(smem + ((l == 0 || l == 2) ? kTcA1 : kTcA0), tid, v);
+                for (int j = 0; j < 64; j++) v[j] = fmaxf(__uint_as_float(r[j]) + bias[l * kGuideHidden + j], 0.f);
+                tc_store_row<kGuideHidden>((l == 0 || l == 2) ? A1 : A0, row, v);
             } else {
 #pragma unroll
-                for (int j = 0; j < kGuideOutPad; j++) o[j] = v[j] + bias[3 * kGuideHidden + j];
+                for (int j = 0; j < kGuideOutPad; j++) o[j] = __uint_as_float(r[j]) + bias[3 * kGuideHidden + j];
             }
         }
         if (failed) break;
@@ -304,7 +316,7 @@ __global__ void __launch_bounds__(kTcRows) k_guide_infer_tc(DevScene S, GuideNet
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
-        tmem_free(tmem, kTcCols);
+        tmem_free(*tslot, kTcCols);
     }
 }
 
@@ -740,7 +752,13 @@ void GuideTrainer::prepare_launch() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaFuncSetAttribute(k_guide_infer_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_infer_tc<0>, kTcRows, kTcSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_infer_tc<0>, kTcThreads, kTcSmem);
+    // resident CTAs per SM as shared memory allows (1 KB reserved per CTA), in case the query
+    // under-reports; extra CTAs of a persistent grid only wait for a slot
+    int smem_sm = 0;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    const int per_smem = smem_sm / (int)(kTcSmem + 1024);
+    per = std::max(per, std::min(4, per_smem));
     g_infer_grid = std::max(1, sms * std::max(1, per));
     g_train_grid = std::max(1, sms);
 }
@@ -754,7 +772,7 @@ void GuideTrainer::infer(cudaStream_t st, const void* Sv, const float4* ray_o, c
         if (((bucket_mask >> b) & 1) && bucket_guided(b)) mask |= 1 << b;
     if (!mask) return;
     const DevScene& S = *static_cast<const DevScene*>(Sv);
-    k_guide_infer_tc<0><<<grid, kTcRows, kTcSmem, st>>>(S, view(false, false).net, ray_o, ray_d, hits, bucket_cnt, bucket_list,
+    k_guide_infer_tc<0><<<grid, kTcThreads, kTcSmem, st>>>(S, view(false, false).net, ray_o, ray_d, hits, bucket_cnt, bucket_list,
                                                         cap, mask, nullptr, 0, out_, S.err);
 }
 
@@ -822,8 +840,8 @@ int GuideTrainer::eval(DeviceArena& arena, const float* host_xnw, int n, float* 
         cudaMemcpy(din, host_xnw, (size_t)n * 9 * 4, cudaMemcpyHostToDevice);
         cudaMemset(derr, 0, 16);
         prepare_launch();
-        const int blocks = std::min(g_infer_grid, (n + kTcRows - 1) / kTcRows);
-        k_guide_infer_tc<1><<<blocks, kTcRows, kTcSmem>>>(DevScene{}, view(false, false).net, nullptr, nullptr, nullptr, nullptr,
+        const int blocks = std::min(g_infer_grid, (n + kTcThreads - 1) / kTcThreads);
+        k_guide_infer_tc<1><<<blocks, kTcThreads, kTcSmem>>>(DevScene{}, view(false, false).net, nullptr, nullptr, nullptr, nullptr,
                                                           nullptr, 0, 0, din, n, dout, derr);
         int h = 0;
         if (cudaDeviceSynchronize() != cudaSuccess) { err = cudaGetErrorString(cudaGetLastError()); rc = C2G_ERR_CUDA; }
