@@ -156,9 +156,10 @@ constexpr int kTcRows = 128;
 constexpr int kTcGroups = 2;                            // warpgroups per CTA
 constexpr int kTcThreads = kTcRows * kTcGroups;
 __host__ __device__ constexpr int tc_w_off(int l) { return l == 0 ? 0 : tc_w_off(l - 1) + guide_n(l - 1) * guide_k(l - 1) * 2; }
-constexpr int kTcGroupBytes = kTcRows * kGuideIn * 2 + kTcRows * kGuideHidden * 2;  // A0 + A1
+// One operand buffer per warpgroup: a layer's MMAs have completed (mbarrier) before its output
+// overwrites the buffer as the next layer's operand.
+constexpr int kTcGroupBytes = kTcRows * kGuideIn * 2;
 __host__ __device__ constexpr int tc_a0(int g) { return tc_w_off(4) + g * kTcGroupBytes; }
-__host__ __device__ constexpr int tc_a1(int g) { return tc_a0(g) + kTcRows * kGuideIn * 2; }
 constexpr int kTcBias = tc_w_off(4) + kTcGroups * kTcGroupBytes;
 constexpr int kTcBiasN = 3 * kGuideHidden + kGuideOutPad;
 constexpr int kTcBar = kTcBias + kTcBiasN * 4;          // one mbarrier per warpgroup
@@ -167,29 +168,53 @@ constexpr size_t kTcSmem = (size_t)kTcTmemSlot + 8;
 constexpr uint32_t kTcColsPerGroup = 64;
 constexpr uint32_t kTcCols = kTcColsPerGroup * kTcGroups;  // tensor-memory columns per CTA (power of 2)
 constexpr uint32_t kTcWaitPolls = 1u << 22;
-static_assert(tc_a0(0) % 128 == 0 && tc_a1(0) % 128 == 0 && kTcGroupBytes % 128 == 0 && kTcBar % 8 == 0,
-              "operand and barrier alignment");
+static_assert(tc_a0(0) % 128 == 0 && kTcGroupBytes % 128 == 0 && kTcBar % 8 == 0, "operand and barrier alignment");
 
 __device__ __forceinline__ int tc_cm(int r, int k, int K) { return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2; }
 
-// One row (this thread's vertex) of a K-column operand from K floats, rounded to BF16.
-template <int K>
-__device__ __forceinline__ void tc_store_row(unsigned char* base, int r, const float* v) {
+// Eight consecutive columns [k0, k0 + 8) of this thread's operand row, rounded to BF16.
+__device__ __forceinline__ void tc_store8(unsigned char* base, int r, int k0, int K, const float* v) {
+    uint4 q;
+    q.x = pack_bf16(v[0], v[1]);
+    q.y = pack_bf16(v[2], v[3]);
+    q.z = pack_bf16(v[4], v[5]);
+    q.w = pack_bf16(v[6], v[7]);
+    *reinterpret_cast<uint4*>(base + tc_cm(r, k0, K)) = q;
+}
+
+// guide_encode written straight into the K = 80 operand row, eight values at a time (the same
+// arithmetic in the same order, with eight values live instead of eighty).
+__device__ __forceinline__ void tc_encode_row(const GuideNet& g, float3 x, float3 n, float3 wo, unsigned char* base, int r) {
+    const float p[3] = {(x.x - g.box_lo[0]) * g.box_inv[0], (x.y - g.box_lo[1]) * g.box_inv[1], (x.z - g.box_lo[2]) * g.box_inv[2]};
+    float chunk[8];
+    int fill = 0, col = 0;
 #pragma unroll
-    for (int c = 0; c < K / 8; c++) {
-        uint4 q;
-        q.x = pack_bf16(v[8 * c + 0], v[8 * c + 1]);
-        q.y = pack_bf16(v[8 * c + 2], v[8 * c + 3]);
-        q.z = pack_bf16(v[8 * c + 4], v[8 * c + 5]);
-        q.w = pack_bf16(v[8 * c + 6], v[8 * c + 7]);
-        *reinterpret_cast<uint4*>(base + tc_cm(r, 8 * c, K)) = q;
+    for (int a = 0; a < 3; a++) {
+        float v = fminf(fmaxf(p[a], 0.f), 1.f);
+        float s, c;
+        sincospif(v, &s, &c);
+#pragma unroll
+        for (int f = 0; f < kGuideFreqs; f++) {
+            chunk[fill++] = s;
+            chunk[fill++] = c;
+            if (fill == 8) {
+                tc_store8(base, r, col, kGuideIn, chunk);
+                col += 8;
+                fill = 0;
+            }
+            const float s2 = 2.f * s * c, c2 = (c - s) * (c + s);
+            s = s2;
+            c = c2;
+        }
     }
+    const float tail[8] = {n.x, n.y, n.z, wo.x, wo.y, wo.z, 0.f, 0.f};
+    tc_store8(base, r, 72, kGuideIn, tail);
 }
 
 // MODE 0: vertices of the guided buckets (surface + encoding), packed mixtures per queue slot.
 // MODE 1: explicit inputs xnw (9 floats each), raw outputs (kGuideOut floats each).
 template <int MODE>
-__global__ void __launch_bounds__(kTcThreads) k_guide_infer_tc(DevScene S, GuideNet net, const float4* __restrict__ ray_o,
+__global__ void __launch_bounds__(kTcThreads, 3) k_guide_infer_tc(DevScene S, GuideNet net, const float4* __restrict__ ray_o,
                                                               const float4* __restrict__ ray_d, const float4* __restrict__ hits,
                                                               const int* bucket_cnt, const int* __restrict__ bucket_list,
                                                               int cap, int mask, const float* __restrict__ xnw, int n_in,
@@ -233,8 +258,7 @@ __global__ void __launch_bounds__(kTcThreads) k_guide_infer_tc(DevScene S, Guide
     tc_fence_after();
     const uint32_t tmem = *tslot + grp * kTcColsPerGroup;             // this warpgroup's columns
     const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's 32 lanes
-    unsigned char* A0 = smem + tc_a0(grp);
-    unsigned char* A1 = smem + tc_a1(grp);
+    unsigned char* A = smem + tc_a0(grp);
     const int bar_id = 1 + grp;
     const int total = MODE == 0 ? bend[kBuckets - 1] : n_in;
     uint32_t phase = 0;
@@ -242,9 +266,6 @@ __global__ void __launch_bounds__(kTcThreads) k_guide_infer_tc(DevScene S, Guide
     for (int base = (blockIdx.x * kTcGroups + grp) * kTcRows; base < total && !failed; base += gridDim.x * kTcThreads) {
         const int item = base + row;
         int slot = -1;
-        float in[kGuideIn];
-#pragma unroll
-        for (int k = 0; k < kGuideIn; k++) in[k] = 0.f;
         if (item < total) {
             if (MODE == 0) {
                 int b = 0;
@@ -254,19 +275,22 @@ __global__ void __launch_bounds__(kTcThreads) k_guide_infer_tc(DevScene S, Guide
                 Hit h{h4.x, h4.y, h4.z, __float_as_int(h4.w)};
                 Surface sf;
                 make_surface(S, f3(o4), f3(d4), h, sf);
-                guide_encode(net, sf.pos, sf.N, -f3(d4), in);
+                tc_encode_row(net, sf.pos, sf.N, -f3(d4), A, row);
             } else {
                 slot = item;
                 const float* v = xnw + (size_t)9 * item;
-                guide_encode(net, f3(v[0], v[1], v[2]), f3(v[3], v[4], v[5]), f3(v[6], v[7], v[8]), in);
+                tc_encode_row(net, f3(v[0], v[1], v[2]), f3(v[3], v[4], v[5]), f3(v[6], v[7], v[8]), A, row);
             }
+        } else {
+            const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int k = 0; k < kGuideIn; k += 8) tc_store8(A, row, k, kGuideIn, z);
         }
-        tc_store_row<kGuideIn>(A0, row, in);
         float o[kGuideOutPad];
 #pragma unroll
         for (int l = 0; l < kGuideLayers; l++) {
             const int K = guide_k(l), N = guide_n(l);
-            unsigned char* Ain = (l == 0 || l == 2) ? A0 : A1;
+            unsigned char* Ain = A;
             fence_async_smem();
             tc_fence_before();
             wg_sync(bar_id);
@@ -288,17 +312,27 @@ __global__ void __launch_bounds__(kTcThreads) k_guide_infer_tc(DevScene S, Guide
                 break;
             }
             tc_fence_after();
-            uint32_t r[64];
-#pragma unroll
-            for (int c = 0; c < 64; c += 16)
-                if (c < N) tmem_ld16(trow + c, r + c);
-            tmem_wait();
             if (l < kGuideLayers - 1) {
-                float v[64];
+                // 32 columns at a time: bias, ReLU, BF16, written over the operand just consumed
 #pragma unroll
-                for (int j = 0; j < 64; j++) v[j] = fmaxf(__uint_as_float(r[j]) + bias[l * kGuideHidden + j], 0.f);
-                tc_store_row<kGuideHidden>((l == 0 || l == 2) ? A1 : A0, row, v);
+                for (int c = 0; c < kGuideHidden; c += 32) {
+                    uint32_t r[32];
+                    tmem_ld16(trow + c, r);
+                    tmem_ld16(trow + c + 16, r + 16);
+                    tmem_wait();
+#pragma unroll
+                    for (int q = 0; q < 32; q += 8) {
+                        float v[8];
+#pragma unroll
+                        for (int j = 0; j < 8; j++) v[j] = fmaxf(__uint_as_float(r[q + j]) + bias[l * kGuideHidden + c + q + j], 0.f);
+                        tc_store8(A, row, c + q, kGuideHidden, v);
+                    }
+                }
             } else {
+                uint32_t r[kGuideOutPad];
+#pragma unroll
+                for (int c = 0; c < kGuideOutPad; c += 16) tmem_ld16(trow + c, r + c);
+                tmem_wait();
 #pragma unroll
                 for (int j = 0; j < kGuideOutPad; j++) o[j] = __uint_as_float(r[j]) + bias[3 * kGuideHidden + j];
             }
