@@ -1569,7 +1569,7 @@ int GpuScene::render_noalloc(const c2g_render_params& p, float4* film_dev, cudaS
     if (!film_dev) { err = "film buffer is null"; return C2G_ERR_INVALID; }
     if (p.width != film_w_ || p.height != film_h_) { err = "render size differs from the loaded film size"; return C2G_ERR_INVALID; }
     if (p.max_depth < 0 || p.sample_count < 0 || p.sample_begin < 0) { err = "invalid render parameters"; return C2G_ERR_INVALID; }
-    if (p.integrator != C2G_INTEGRATOR_PATH && p.integrator != C2G_INTEGRATOR_DIRECT) { err = "integrator not available in this build"; return C2G_ERR_UNSUPPORTED; }
+    if (p.integrator != C2G_INTEGRATOR_PATH && p.integrator != C2G_INTEGRATOR_DIRECT) { err = "the allocation-free entry point runs the path tracer and direct lighting only"; return C2G_ERR_UNSUPPORTED; }
     if (p.max_depth > 255) { err = "max_depth above 255"; return C2G_ERR_INVALID; }
     WaveArgs a{};
     a.W = p.width;
