@@ -142,37 +142,43 @@ __device__ __forceinline__ void store_inputs(__nv_bfloat16* row, const float* in
 }
 
 // ---- inference on the fifth-generation tensor cores (tcgen05) -----------------------------------
-// Two warpgroups per CTA share the staged weights; each warpgroup runs its own 128-vertex tiles,
-// one vertex per thread and per tensor-memory lane, with its own operand buffers, 64 tensor-memory
-// columns, mbarrier and named barrier.  Per layer one thread of the warpgroup issues K/16
-// tcgen05.mma (M = 128, N = 64 or 48, BF16 operands from shared memory, FP32 accumulator in
-// tensor memory) and commits them to the mbarrier; every thread then reads its accumulator row
-// (tcgen05.ld), adds the bias, applies ReLU, rounds to BF16 and writes the next layer's operand
-// row.  Operands are K-major 8-row x 16-byte core matrices without swizzle: element (r, k) of a
+// Two kernels.  k_guide_encode (one thread per guided vertex, full occupancy) reconstructs the
+// surface, encodes (x, n, wo) and writes the row as BF16 into 128-row operand tiles in global
+// memory, already in the tensor core's shared-memory layout.  k_guide_mlp_tc streams those tiles
+// into shared memory with the bulk-copy engine and runs the four layers: two warpgroups per CTA
+// share the staged weights; per warpgroup and tile one thread issues K/16 tcgen05.mma (M = 128,
+// N = 64 or 48, BF16 operands from shared-memory descriptors, FP32 accumulator in 64 tensor-memory
+// columns) and commits them to an mbarrier; every thread then reads its row (tcgen05.ld), adds the
+// bias, applies ReLU and writes BF16 for the next layer, or packs the mixture after the last.  The
+// next tile's copy starts as soon as layer 0 has consumed the input buffer.
+// Operand layout: K-major 8-row x 16-byte core matrices without swizzle; element (r, k) of a
 // K-column operand sits at (r / 8) * 16K + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2 bytes, so one
-// K=16 step spans two core matrices 128 B apart (descriptor LBO) and 8-row groups are 16K bytes
-// apart (SBO).
+// K=16 step spans two core matrices 128 B apart (descriptor LBO), 8-row groups 16K bytes apart (SBO).
 constexpr int kTcRows = 128;
 constexpr int kTcGroups = 2;                            // warpgroups per CTA
 constexpr int kTcThreads = kTcRows * kTcGroups;
+constexpr int kTcTileBytes = kTcRows * kGuideIn * 2;    // one staged input tile: 20480 B
+// staging bytes for n vertices: whole 128-row tiles
+constexpr size_t stage_bytes(size_t n) { return (n + kTcRows - 1) / kTcRows * (size_t)kTcTileBytes; }
 __host__ __device__ constexpr int tc_w_off(int l) { return l == 0 ? 0 : tc_w_off(l - 1) + guide_n(l - 1) * guide_k(l - 1) * 2; }
-// One operand buffer per warpgroup: a layer's MMAs have completed (mbarrier) before its output
-// overwrites the buffer as the next layer's operand.
-constexpr int kTcGroupBytes = kTcRows * kGuideIn * 2;
-__host__ __device__ constexpr int tc_a0(int g) { return tc_w_off(4) + g * kTcGroupBytes; }
+constexpr int kTcActBytes = kTcRows * kGuideHidden * 2;
+constexpr int kTcGroupBytes = kTcTileBytes + kTcActBytes;  // input tile + hidden activations
+__host__ __device__ constexpr int tc_in(int g) { return tc_w_off(4) + g * kTcGroupBytes; }
+__host__ __device__ constexpr int tc_act(int g) { return tc_in(g) + kTcTileBytes; }
 constexpr int kTcBias = tc_w_off(4) + kTcGroups * kTcGroupBytes;
 constexpr int kTcBiasN = 3 * kGuideHidden + kGuideOutPad;
-constexpr int kTcBar = kTcBias + kTcBiasN * 4;          // one mbarrier per warpgroup
-constexpr int kTcTmemSlot = kTcBar + 8 * kTcGroups;
+constexpr int kTcBar = kTcBias + kTcBiasN * 4;          // per warpgroup: MMA-done and input-full mbarriers
+constexpr int kTcTmemSlot = kTcBar + 16 * kTcGroups;
 constexpr size_t kTcSmem = (size_t)kTcTmemSlot + 8;
 constexpr uint32_t kTcColsPerGroup = 64;
 constexpr uint32_t kTcCols = kTcColsPerGroup * kTcGroups;  // tensor-memory columns per CTA (power of 2)
 constexpr uint32_t kTcWaitPolls = 1u << 22;
-static_assert(tc_a0(0) % 128 == 0 && kTcGroupBytes % 128 == 0 && kTcBar % 8 == 0, "operand and barrier alignment");
+static_assert(tc_in(0) % 128 == 0 && tc_act(0) % 128 == 0 && kTcGroupBytes % 128 == 0 && kTcBar % 8 == 0,
+              "operand and barrier alignment");
 
 __device__ __forceinline__ int tc_cm(int r, int k, int K) { return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2; }
 
-// Eight consecutive columns [k0, k0 + 8) of this thread's operand row, rounded to BF16.
+// Eight consecutive columns [k0, k0 + 8) of operand row r, rounded to BF16.
 __device__ __forceinline__ void tc_store8(unsigned char* base, int r, int k0, int K, const float* v) {
     uint4 q;
     q.x = pack_bf16(v[0], v[1]);
@@ -182,8 +188,8 @@ __device__ __forceinline__ void tc_store8(unsigned char* base, int r, int k0, in
     *reinterpret_cast<uint4*>(base + tc_cm(r, k0, K)) = q;
 }
 
-// guide_encode written straight into the K = 80 operand row, eight values at a time (the same
-// arithmetic in the same order, with eight values live instead of eighty).
+// guide_encode written straight into row r of a K = 80 operand tile, eight values at a time (the
+// same arithmetic in the same order, with eight values live instead of eighty).
 __device__ __forceinline__ void tc_encode_row(const GuideNet& g, float3 x, float3 n, float3 wo, unsigned char* base, int r) {
     const float p[3] = {(x.x - g.box_lo[0]) * g.box_inv[0], (x.y - g.box_lo[1]) * g.box_inv[1], (x.z - g.box_lo[2]) * g.box_inv[2]};
     float chunk[8];
@@ -211,18 +217,65 @@ __device__ __forceinline__ void tc_encode_row(const GuideNet& g, float3 x, float
     tc_store8(base, r, 72, kGuideIn, tail);
 }
 
-// MODE 0: vertices of the guided buckets (surface + encoding), packed mixtures per queue slot.
-// MODE 1: explicit inputs xnw (9 floats each), raw outputs (kGuideOut floats each).
+// Work list of the guided buckets back to back: item -> queue slot.
+__device__ __forceinline__ int guided_slot(const int* bend, const int* bucket_list, int cap, int item) {
+    int b = 0;
+    while (b < kBuckets - 1 && item >= bend[b]) b++;
+    return bucket_list[(size_t)b * cap + (item - (b ? bend[b - 1] : 0))];
+}
+__device__ __forceinline__ void guided_bucket_ends(const int* bucket_cnt, int mask, int* bend) {
+    int total = 0;
+    for (int b = 0; b < kBuckets; b++) {
+        total += ((mask >> b) & 1) ? bucket_cnt[b] : 0;
+        bend[b] = total;
+    }
+}
+
+// MODE 0: the guided buckets' vertices; MODE 1: explicit inputs xnw (9 floats each).  Rows past the
+// last item of the last tile are zero.
 template <int MODE>
-__global__ void __launch_bounds__(kTcThreads, 3) k_guide_infer_tc(DevScene S, GuideNet net, const float4* __restrict__ ray_o,
-                                                              const float4* __restrict__ ray_d, const float4* __restrict__ hits,
-                                                              const int* bucket_cnt, const int* __restrict__ bucket_list,
-                                                              int cap, int mask, const float* __restrict__ xnw, int n_in,
-                                                              float* out, int* err) {
+__global__ void __launch_bounds__(256) k_guide_encode(DevScene S, GuideNet net, const float4* __restrict__ ray_o,
+                                                     const float4* __restrict__ ray_d, const float4* __restrict__ hits,
+                                                     const int* bucket_cnt, const int* __restrict__ bucket_list, int cap,
+                                                     int mask, const float* __restrict__ xnw, int n_in,
+                                                     unsigned char* stage) {
+    __shared__ int bend[kBuckets];
+    if (MODE == 0 && threadIdx.x == 0) guided_bucket_ends(bucket_cnt, mask, bend);
+    __syncthreads();
+    const int total = MODE == 0 ? bend[kBuckets - 1] : n_in;
+    const int padded = (total + kTcRows - 1) / kTcRows * kTcRows;
+    for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < padded; item += gridDim.x * blockDim.x) {
+        unsigned char* tile = stage + (size_t)(item / kTcRows) * kTcTileBytes;
+        const int r = item % kTcRows;
+        if (item < total) {
+            if (MODE == 0) {
+                const int slot = guided_slot(bend, bucket_list, cap, item);
+                const float4 o4 = ray_o[slot], d4 = ray_d[slot], h4 = hits[slot];
+                Hit h{h4.x, h4.y, h4.z, __float_as_int(h4.w)};
+                Surface sf;
+                make_surface(S, f3(o4), f3(d4), h, sf);
+                tc_encode_row(net, sf.pos, sf.N, -f3(d4), tile, r);
+            } else {
+                const float* v = xnw + (size_t)9 * item;
+                tc_encode_row(net, f3(v[0], v[1], v[2]), f3(v[3], v[4], v[5]), f3(v[6], v[7], v[8]), tile, r);
+            }
+        } else {
+            const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int k = 0; k < kGuideIn; k += 8) tc_store8(tile, r, k, kGuideIn, z);
+        }
+    }
+}
+
+// MODE 0: packed mixtures per queue slot; MODE 1: raw outputs (kGuideOut floats per input).
+template <int MODE>
+__global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, const unsigned char* __restrict__ stage,
+                                                               const int* bucket_cnt, const int* __restrict__ bucket_list,
+                                                               int cap, int mask, int n_in, float* out, int* err) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int grp = threadIdx.x / kTcRows, row = threadIdx.x - grp * kTcRows, warp = threadIdx.x >> 5;
     float* bias = reinterpret_cast<float*>(smem + kTcBias);
-    const uint32_t bar = smem_u32(smem + kTcBar + 8 * grp);
+    const uint32_t bar_mma = smem_u32(smem + kTcBar + 16 * grp), bar_in = bar_mma + 8;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kTcTmemSlot);
     // weights -> core-matrix layout; biases
 #pragma unroll
@@ -241,15 +294,12 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_guide_infer_tc(DevScene S, Gu
     }
     __shared__ int bend[kBuckets];
     if (threadIdx.x == 0) {
-        for (int g = 0; g < kTcGroups; g++) mbar_init(smem_u32(smem + kTcBar + 8 * g), 1);
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-        if (MODE == 0) {
-            int total = 0;
-            for (int b = 0; b < kBuckets; b++) {
-                total += ((mask >> b) & 1) ? bucket_cnt[b] : 0;
-                bend[b] = total;
-            }
+        for (int g = 0; g < kTcGroups; g++) {
+            mbar_init(smem_u32(smem + kTcBar + 16 * g), 1);
+            mbar_init(smem_u32(smem + kTcBar + 16 * g + 8), 1);
         }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        if (MODE == 0) guided_bucket_ends(bucket_cnt, mask, bend);
     }
     if (warp == 0) tmem_alloc(smem_u32(tslot), kTcCols);
     fence_async_smem();
@@ -258,62 +308,56 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_guide_infer_tc(DevScene S, Gu
     tc_fence_after();
     const uint32_t tmem = *tslot + grp * kTcColsPerGroup;             // this warpgroup's columns
     const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's 32 lanes
-    unsigned char* A = smem + tc_a0(grp);
+    unsigned char* IN = smem + tc_in(grp);
+    unsigned char* ACT = smem + tc_act(grp);
     const int bar_id = 1 + grp;
     const int total = MODE == 0 ? bend[kBuckets - 1] : n_in;
-    uint32_t phase = 0;
-    bool failed = false;
-    for (int base = (blockIdx.x * kTcGroups + grp) * kTcRows; base < total && !failed; base += gridDim.x * kTcThreads) {
-        const int item = base + row;
-        int slot = -1;
-        if (item < total) {
-            if (MODE == 0) {
-                int b = 0;
-                while (b < kBuckets - 1 && item >= bend[b]) b++;
-                slot = bucket_list[(size_t)b * cap + (item - (b ? bend[b - 1] : 0))];
-                const float4 o4 = ray_o[slot], d4 = ray_d[slot], h4 = hits[slot];
-                Hit h{h4.x, h4.y, h4.z, __float_as_int(h4.w)};
-                Surface sf;
-                make_surface(S, f3(o4), f3(d4), h, sf);
-                tc_encode_row(net, sf.pos, sf.N, -f3(d4), A, row);
-            } else {
-                slot = item;
-                const float* v = xnw + (size_t)9 * item;
-                tc_encode_row(net, f3(v[0], v[1], v[2]), f3(v[3], v[4], v[5]), f3(v[6], v[7], v[8]), A, row);
-            }
-        } else {
-            const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int k = 0; k < kGuideIn; k += 8) tc_store8(A, row, k, kGuideIn, z);
+    const int tiles = (total + kTcRows - 1) / kTcRows;
+    const int tstride = gridDim.x * kTcGroups;
+    int tile = blockIdx.x * kTcGroups + grp;
+    // phases of the two barriers, and whether a tile copy / an MMA group is outstanding (the same
+    // in every thread of the warpgroup: issue decisions are uniform)
+    uint32_t ph_mma = 0, ph_in = 0;
+    bool copy_pending = false, mma_pending = false, failed = false;
+    if (tile < tiles) {
+        if (row == 0) {
+            mbar_arrive_expect_tx(bar_in, kTcTileBytes);
+            bulk_g2s(smem_u32(IN), stage + (size_t)tile * kTcTileBytes, kTcTileBytes, bar_in);
         }
+        copy_pending = true;
+    }
+    for (; tile < tiles && !failed; tile += tstride) {
+        bool ok = mbar_wait(bar_in, ph_in, kTcWaitPolls);
+        if (ok) { ph_in ^= 1u; copy_pending = false; }
         float o[kGuideOutPad];
 #pragma unroll
         for (int l = 0; l < kGuideLayers; l++) {
             const int K = guide_k(l), N = guide_n(l);
-            unsigned char* Ain = A;
             fence_async_smem();
             tc_fence_before();
-            wg_sync(bar_id);
+            if (wg_sync_or(bar_id, !ok)) { failed = true; break; }
             if (row == 0) {
                 tc_fence_after();
-                const uint32_t a0 = smem_u32(Ain), b0 = smem_u32(smem + tc_w_off(l));
+                const uint32_t a0 = smem_u32(l == 0 ? IN : ACT), b0 = smem_u32(smem + tc_w_off(l));
                 const uint32_t idesc = umma_idesc_bf16(kTcRows, N);
                 for (int kk = 0; kk < K / 16; kk++)
                     umma_bf16(tmem, umma_desc(a0 + kk * 256, 128, K * 16), umma_desc(b0 + kk * 256, 128, K * 16), idesc, kk > 0);
-                umma_commit(bar);
+                umma_commit(bar_mma);
             }
-            const bool ok = mbar_wait(bar, phase, kTcWaitPolls);
-            phase ^= 1u;
-            if (wg_sync_or(bar_id, !ok)) {
-                if (row == 0) dev_flag_error(err, DEVERR_WAIT);
-                // let anything still in flight finish (bounded) before the tensor memory is freed
-                mbar_wait(bar, phase ^ 1u, kTcWaitPolls);
-                failed = true;
-                break;
-            }
+            mma_pending = true;
+            ok = mbar_wait(bar_mma, ph_mma, kTcWaitPolls);
+            if (ok) { ph_mma ^= 1u; mma_pending = false; }
+            if (wg_sync_or(bar_id, !ok)) { failed = true; break; }
             tc_fence_after();
+            if (l == 0 && tile + tstride < tiles) {
+                // layer 0 has consumed the input tile: fetch the next one behind layers 1-3
+                if (row == 0) {
+                    mbar_arrive_expect_tx(bar_in, kTcTileBytes);
+                    bulk_g2s(smem_u32(IN), stage + (size_t)(tile + tstride) * kTcTileBytes, kTcTileBytes, bar_in);
+                }
+                copy_pending = true;
+            }
             if (l < kGuideLayers - 1) {
-                // 32 columns at a time: bias, ReLU, BF16, written over the operand just consumed
 #pragma unroll
                 for (int c = 0; c < kGuideHidden; c += 32) {
                     uint32_t r[32];
@@ -325,7 +369,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_guide_infer_tc(DevScene S, Gu
                         float v[8];
 #pragma unroll
                         for (int j = 0; j < 8; j++) v[j] = fmaxf(__uint_as_float(r[q + j]) + bias[l * kGuideHidden + c + q + j], 0.f);
-                        tc_store8(A, row, c + q, kGuideHidden, v);
+                        tc_store8(ACT, row, c + q, kGuideHidden, v);
                     }
                 }
             } else {
@@ -338,13 +382,21 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_guide_infer_tc(DevScene S, Gu
             }
         }
         if (failed) break;
+        const int item = tile * kTcRows + row;
         if (item < total) {
-            if (MODE == 0) pack_lobes(o, out + (size_t)slot * kGuidePacked);
+            if (MODE == 0) pack_lobes(o, out + (size_t)guided_slot(bend, bucket_list, cap, item) * kGuidePacked);
             else {
 #pragma unroll
-                for (int k = 0; k < kGuideOut; k++) out[(size_t)slot * kGuideOut + k] = o[k];
+                for (int k = 0; k < kGuideOut; k++) out[(size_t)item * kGuideOut + k] = o[k];
             }
         }
+    }
+    if (failed) {
+        if (row == 0) dev_flag_error(err, DEVERR_WAIT);
+        // let what is still in flight finish (bounded) before the tensor memory is freed and the
+        // CTA's shared memory is released
+        if (mma_pending) mbar_wait(bar_mma, ph_mma, kTcWaitPolls);
+        if (copy_pending) mbar_wait(bar_in, ph_in, kTcWaitPolls);
     }
     tc_fence_before();
     __syncthreads();
@@ -694,12 +746,13 @@ __global__ void k_guide_bf16_from_params(const float* params, __nv_bfloat16* bfw
 GuideTrainer::~GuideTrainer() = default;
 
 void GuideTrainer::release(DeviceArena& arena) {
-    void* ps[] = {params_, grad_, adam_m_, adam_v_, bf_, out_, rec_, batch_, batch_count_, loss_acc_, step_dev_};
+    void* ps[] = {params_, grad_, adam_m_, adam_v_, bf_, out_, stage_, rec_, batch_, batch_count_, loss_acc_, step_dev_};
     for (void* p : ps)
         if (p) arena.free(p);
     params_ = grad_ = adam_m_ = adam_v_ = nullptr;
     bf_ = nullptr;
     out_ = nullptr;
+    stage_ = nullptr;
     rec_ = batch_ = nullptr;
     batch_count_ = nullptr;
     loss_acc_ = nullptr;
@@ -748,8 +801,8 @@ int GuideTrainer::init(DeviceArena& arena, size_t paths, int max_depth, const fl
         cudaMemset(adam_m_, 0, kGuideParams * 4);
         cudaMemset(adam_v_, 0, kGuideParams * 4);
         k_guide_bf16_from_params<<<64, 256>>>(params_, bf_);
-        cudaFuncSetAttribute(k_guide_infer_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
-        cudaFuncSetAttribute(k_guide_infer_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+        cudaFuncSetAttribute(k_guide_mlp_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+        cudaFuncSetAttribute(k_guide_mlp_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
         cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem);
         steps_ = 0;
     }
@@ -760,6 +813,7 @@ int GuideTrainer::init(DeviceArena& arena, size_t paths, int max_depth, const fl
     }
     if (paths > cap_ || std::max(1, max_depth) != rec_depth_) {
         if (out_) arena.free(out_);
+        if (stage_) arena.free(stage_);
         if (rec_) arena.free(rec_);
         if (batch_) arena.free(batch_);
         cap_ = paths;
@@ -768,16 +822,17 @@ int GuideTrainer::init(DeviceArena& arena, size_t paths, int max_depth, const fl
         rec_stride_ = (int)std::max<size_t>(1, paths * 3 / (1u << 18));
         rec_cap_ = (paths / rec_stride_ + 1) * rec_depth_;
         out_ = (float*)A(paths * kGuidePacked * 4);
+        stage_ = (unsigned char*)A(stage_bytes(paths));
         rec_ = (float4*)A(rec_cap_ * 64);
         batch_ = (float4*)A(rec_cap_ * 64);
-        if (!out_ || !rec_ || !batch_) return C2G_ERR_OOM;
+        if (!out_ || !stage_ || !rec_ || !batch_) return C2G_ERR_OOM;
         cudaMemset(rec_, 0, rec_cap_ * 64);
     }
     return C2G_OK;
 }
 
 namespace {
-int g_infer_grid = 0, g_train_grid = 0;
+int g_infer_grid = 0, g_train_grid = 0, g_encode_grid = 0;
 }  // namespace
 
 void GuideTrainer::prepare_launch() {
@@ -785,16 +840,20 @@ void GuideTrainer::prepare_launch() {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncSetAttribute(k_guide_infer_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_infer_tc<0>, kTcThreads, kTcSmem);
+    cudaFuncSetAttribute(k_guide_mlp_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+    cudaFuncSetAttribute(k_guide_mlp_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_mlp_tc<0>, kTcThreads, kTcSmem);
     // resident CTAs per SM as shared memory allows (1 KB reserved per CTA), in case the query
     // under-reports; extra CTAs of a persistent grid only wait for a slot
     int smem_sm = 0;
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     const int per_smem = smem_sm / (int)(kTcSmem + 1024);
-    per = std::max(per, std::min(4, per_smem));
+    per = std::max(per, std::min(2, per_smem));
     g_infer_grid = std::max(1, sms * std::max(1, per));
     g_train_grid = std::max(1, sms);
+    int per_enc = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_enc, k_guide_encode<0>, 256, 0);
+    g_encode_grid = std::max(1, sms * std::max(1, per_enc));
 }
 
 void GuideTrainer::infer(cudaStream_t st, const void* Sv, const float4* ray_o, const float4* ray_d, const float4* hits,
@@ -806,8 +865,10 @@ void GuideTrainer::infer(cudaStream_t st, const void* Sv, const float4* ray_o, c
         if (((bucket_mask >> b) & 1) && bucket_guided(b)) mask |= 1 << b;
     if (!mask) return;
     const DevScene& S = *static_cast<const DevScene*>(Sv);
-    k_guide_infer_tc<0><<<grid, kTcThreads, kTcSmem, st>>>(S, view(false, false).net, ray_o, ray_d, hits, bucket_cnt, bucket_list,
-                                                        cap, mask, nullptr, 0, out_, S.err);
+    const GuideNet net = view(false, false).net;
+    k_guide_encode<0><<<g_encode_grid, 256, 0, st>>>(S, net, ray_o, ray_d, hits, bucket_cnt, bucket_list, cap, mask, nullptr, 0,
+                                                     stage_);
+    k_guide_mlp_tc<0><<<grid, kTcThreads, kTcSmem, st>>>(net, stage_, bucket_cnt, bucket_list, cap, mask, 0, out_, S.err);
 }
 
 void GuideTrainer::train(cudaStream_t st, const float4* out_L, int wave_paths, int steps) {
@@ -867,16 +928,19 @@ int GuideTrainer::eval(DeviceArena& arena, const float* host_xnw, int n, float* 
     if (n <= 0) return C2G_OK;
     float* din = (float*)arena.alloc((size_t)n * 9 * 4, err);
     float* dout = (float*)arena.alloc((size_t)n * kGuideOut * 4, err);
+    unsigned char* dstage = (unsigned char*)arena.alloc(stage_bytes((size_t)n), err);
     int* derr = (int*)arena.alloc(16, err);
     int rc = C2G_OK;
-    if (!din || !dout || !derr) rc = C2G_ERR_OOM;
+    if (!din || !dout || !dstage || !derr) rc = C2G_ERR_OOM;
     if (!rc) {
         cudaMemcpy(din, host_xnw, (size_t)n * 9 * 4, cudaMemcpyHostToDevice);
         cudaMemset(derr, 0, 16);
         prepare_launch();
+        const GuideNet net = view(false, false).net;
+        k_guide_encode<1><<<std::min(g_encode_grid, (n + 255) / 256), 256>>>(DevScene{}, net, nullptr, nullptr, nullptr, nullptr,
+                                                                           nullptr, 0, 0, din, n, dstage);
         const int blocks = std::min(g_infer_grid, (n + kTcThreads - 1) / kTcThreads);
-        k_guide_infer_tc<1><<<blocks, kTcThreads, kTcSmem>>>(DevScene{}, view(false, false).net, nullptr, nullptr, nullptr, nullptr,
-                                                          nullptr, 0, 0, din, n, dout, derr);
+        k_guide_mlp_tc<1><<<blocks, kTcThreads, kTcSmem>>>(net, dstage, nullptr, nullptr, 0, 0, n, dout, derr);
         int h = 0;
         if (cudaDeviceSynchronize() != cudaSuccess) { err = cudaGetErrorString(cudaGetLastError()); rc = C2G_ERR_CUDA; }
         else if (cudaMemcpy(&h, derr, 4, cudaMemcpyDeviceToHost) == cudaSuccess && h) {
@@ -886,6 +950,7 @@ int GuideTrainer::eval(DeviceArena& arena, const float* host_xnw, int n, float* 
     }
     if (din) arena.free(din);
     if (dout) arena.free(dout);
+    if (dstage) arena.free(dstage);
     if (derr) arena.free(derr);
     return rc;
 }
