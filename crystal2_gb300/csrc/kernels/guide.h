@@ -65,7 +65,8 @@ public:
     bool ready() const { return params_ != nullptr; }
     // Free every device buffer; the next init() draws a fresh network.
     void release(DeviceArena& arena);
-    // Network outputs for every slot in the given material buckets (one launch).
+    // Network outputs for every slot in the given material buckets (encoding kernel, then the
+    // tensor-core MLP kernel).
     void infer(cudaStream_t st, const void* S, const float4* ray_o, const float4* ray_d, const float4* hits,
                const int* bucket_cnt, const int* bucket_list, int cap, int bucket_mask);
     // Turn this wave's records into weighted samples and take `steps` Adam steps.
