@@ -856,19 +856,20 @@ void GuideTrainer::prepare_launch() {
     g_encode_grid = std::max(1, sms * std::max(1, per_enc));
 }
 
-void GuideTrainer::infer(cudaStream_t st, const void* Sv, const float4* ray_o, const float4* ray_d, const float4* hits,
-                         const int* bucket_cnt, const int* bucket_list, int cap, int bucket_mask) {
+int GuideTrainer::infer(cudaStream_t st, const void* Sv, const float4* ray_o, const float4* ray_d, const float4* hits,
+                        const int* bucket_cnt, const int* bucket_list, int cap, int bucket_mask) {
     prepare_launch();
     const int grid = g_infer_grid;
     int mask = 0;
     for (int b = 0; b < kBuckets; b++)
         if (((bucket_mask >> b) & 1) && bucket_guided(b)) mask |= 1 << b;
-    if (!mask) return;
+    if (!mask) return 0;
     const DevScene& S = *static_cast<const DevScene*>(Sv);
     const GuideNet net = view(false, false).net;
     k_guide_encode<0><<<g_encode_grid, 256, 0, st>>>(S, net, ray_o, ray_d, hits, bucket_cnt, bucket_list, cap, mask, nullptr, 0,
                                                      stage_);
     k_guide_mlp_tc<0><<<grid, kTcThreads, kTcSmem, st>>>(net, stage_, bucket_cnt, bucket_list, cap, mask, 0, out_, S.err);
+    return 2;
 }
 
 void GuideTrainer::train(cudaStream_t st, const float4* out_L, int wave_paths, int steps) {

@@ -67,8 +67,9 @@ public:
     void release(DeviceArena& arena);
     // Network outputs for every slot in the given material buckets (encoding kernel, then the
     // tensor-core MLP kernel).
-    void infer(cudaStream_t st, const void* S, const float4* ray_o, const float4* ray_d, const float4* hits,
-               const int* bucket_cnt, const int* bucket_list, int cap, int bucket_mask);
+    // Returns the kernels launched (0 when no bucket of the mask is guided).
+    int infer(cudaStream_t st, const void* S, const float4* ray_o, const float4* ray_d, const float4* hits,
+              const int* bucket_cnt, const int* bucket_list, int cap, int bucket_mask);
     // Turn this wave's records into weighted samples and take `steps` Adam steps.
     void train(cudaStream_t st, const float4* out_L, int wave_paths, int steps);
     GuideView view(bool record, bool sample) const;

@@ -1245,9 +1245,9 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
         const bool glevel = guided && (guide_levels_ <= 0 || b < guide_levels_);
         if (gv.sample && glevel) {
             begin(C2G_K_GUIDE);
-            guide_.infer(st, &S, buf[cur].o, buf[cur].d, w.hit, C + kCntBucket, w.bucket_list, (int)w.P, present_buckets_);
+            launches += guide_.infer(st, &S, buf[cur].o, buf[cur].d, w.hit, C + kCntBucket, w.bucket_list, (int)w.P,
+                                     present_buckets_);
             end();
-            launches += 2;  // encoding + tensor-core MLP
         }
         ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc, w.mis_hit};
         // the material buckets are independent (they append to the shared queues with atomics):
