@@ -556,9 +556,9 @@ def main() -> int:
     ap.add_argument("--guided-res", default="960x540")
     ap.add_argument("--guided-ref-spp", type=int, default=16384)
     ap.add_argument("--guided-seconds", type=float, default=4.0)
-    ap.add_argument("--guided-lr", type=float, default=5e-3)
+    ap.add_argument("--guided-lr", type=float, default=2e-3)
     ap.add_argument("--guided-bsdf-fraction", type=float, default=0.7)
-    ap.add_argument("--guided-train-steps", type=int, default=32)
+    ap.add_argument("--guided-train-steps", type=int, default=16)
     ap.add_argument("--guided-levels", type=int, default=0, help="bounce levels served by the guide (0 = all)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-job measurement")
     ap.add_argument("--sah-width", type=int, default=4, choices=[2, 4], help="SAH traversal variant")

@@ -458,6 +458,9 @@ __global__ void k_guide_batch(float4* rec, int rec_cap, int rec_depth, int rec_s
 // layers are split over the warps, each accumulating its tiles in FP32 registers for the whole
 // sweep (A^T and D fragments come from ldmatrix.trans); they reach global memory once per block.
 constexpr int kTrainWarps = 8;
+// A wave's batch is split into at most this many minibatch windows, taken in turn by its Adam
+// steps: smaller windows made the mixture collapse onto a few sharp lobes in some runs.
+constexpr int kTrainWindows = 4;
 constexpr int kTrainRows = 16;
 // per-warp tile offsets (elements)
 constexpr int kTA0 = 0;
@@ -582,7 +585,7 @@ __global__ void __launch_bounds__(256, 1) k_guide_train(GuideNet net, const floa
                 guide_encode(net, f3(b0), f3(b1), f3(b2), in);
                 wi = f3(b3);
                 pb = b3.w;
-                w = fminf(b0.w / fmaxf(mean_w, 1e-12f), 100.f);  // normalised, firefly-clamped weight
+                w = fminf(b0.w / fmaxf(mean_w, 1e-12f), 20.f);  // normalised, firefly-clamped weight
             } else {
 #pragma unroll
                 for (int k = 0; k < kGuideIn; k++) in[k] = 0.f;
@@ -882,7 +885,8 @@ void GuideTrainer::train(cudaStream_t st, const float4* out_L, int wave_paths, i
     GuideNet net = view(false, false).net;
     for (int s = 0; s < steps; s++) {
         cudaMemsetAsync(loss_acc_, 0, 8, st);  // this step's loss and weight sum (Adam normalises by it)
-        k_guide_train<<<grid, 256, kTrainSmem, st>>>(net, batch_, batch_count_, (int)rec_cap_, grad_, loss_acc_, steps, step_dev_);
+        k_guide_train<<<grid, 256, kTrainSmem, st>>>(net, batch_, batch_count_, (int)rec_cap_, grad_, loss_acc_,
+                                                     std::min(steps, kTrainWindows), step_dev_);
         steps_++;
         k_guide_adam<<<64, 256, 0, st>>>(params_, grad_, adam_m_, adam_v_, bf_, loss_acc_, lr_, 0.9f, 0.99f, 1e-8f, step_dev_);
         k_guide_tick<<<1, 1, 0, st>>>(step_dev_);
