@@ -518,11 +518,6 @@ uint64_t mod_inverse(uint64_t A, uint64_t M) {
     extgcd(A, M, d, x, y);
     return d == 1 ? (x + M) % M : (uint64_t)-1;
 }
-uint64_t reverse_digits(uint64_t v, int base, int n) {
-    uint64_t r = 0;
-    for (int i = 0; i < n; i++) { r = r * base + (v % base); v /= base; }
-    return r;
-}
 }  // namespace
 
 HaltonParams halton_params(int width, int height) {
@@ -554,18 +549,6 @@ void halton_perm_tables(std::vector<uint16_t>& perm, std::vector<int>& offset) {
         offset.push_back((int)perm.size());
         for (int v : t) perm.push_back((uint16_t)v);
     }
-}
-
-int halton_vector_index(const HaltonParams& hp, int px, int py, int sample) {
-    int64_t off = 0;
-    if (hp.sampleStride > 1) {
-        int pm[2] = {px % kMaxResolution, py % kMaxResolution};
-        for (int i = 0; i < 2; i++) {
-            uint64_t rem = reverse_digits((uint64_t)(int64_t)pm[i], i == 0 ? 2 : 3, hp.baseExponents[i]);
-            off += (int64_t)(rem * (uint64_t)(int64_t)hp.baseScales[!i] * (uint64_t)(int64_t)hp.multInverse[i]);
-        }
-    }
-    return (int)(off + (int64_t)(sample * hp.sampleStride));
 }
 
 }  // namespace c2g

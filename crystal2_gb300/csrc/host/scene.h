@@ -70,7 +70,5 @@ HaltonParams halton_params(int width, int height);
 void halton_perm_tables(std::vector<uint16_t>& perm, std::vector<int>& offset);
 // Radical-inverse primes of dims 0..99.
 const int* halton_primes();
-// GetVectorIndexForSample for a pixel and sample (HaltonSampler.cpp:251-270).
-int halton_vector_index(const HaltonParams& hp, int px, int py, int sample);
 
 }  // namespace c2g
