@@ -54,6 +54,24 @@ def test_forward_matches_oracle():
     assert np.median(np.abs(q_gpu / q_ref - 1)) < 1e-2
 
 
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 257, 2000])
+def test_forward_tiles_match_oracle(n):
+    """The tensor-core forward pass runs 128-row tiles, two per CTA: partial last tiles, a single
+    row and counts around the tile size give the oracle's outputs row for row."""
+    ctx, params = _guide_ctx(seed=6)
+    x, nn, wo, _, _, _ = G.random_samples(n, seed=7)
+    out = ctx.guide_eval(np.concatenate([x, nn, wo], 1))
+    ref, _ = G.forward(params.astype(np.float64), G.encode(x, nn, wo, BOX_LO, BOX_HI), bf16_mode=True)
+    ref = ref[:, :G.N_OUT]
+    assert out.shape == ref.shape
+    scale = np.abs(ref).max()
+    assert np.abs(out - ref).max() < 2e-2 * scale
+    # rows are independent: the first rows of a longer batch are the same numbers
+    if n > 1:
+        head = ctx.guide_eval(np.concatenate([x[:1], nn[:1], wo[:1]], 1))
+        assert np.array_equal(head[0], out[0])
+
+
 @pytest.mark.parametrize("m", [37, 4096])
 def test_gradient_matches_oracle(m):
     ctx, params = _guide_ctx(seed=4)
