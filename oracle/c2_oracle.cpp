@@ -618,6 +618,8 @@ static void bvh_build(Scene& s, int& p, int l, int r) {
 
 static void build_tree(Scene& s) {
     int n = (int)s.objs.size();
+    // the reference's build dereferences the missing objects of an empty scene; refuse it here
+    if (n == 0) throw std::runtime_error("scene has no objects");
     s.order.resize(n);
     for (int i = 0; i < n; i++) s.order[i] = i;
     s.nodes.assign(2 * n + 1, Node{});

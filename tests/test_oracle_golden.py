@@ -208,3 +208,12 @@ def test_per_draw_samplers_match_reference_streams_in_distribution(tmp_path, smp
     zt = (blocks(ma) - blocks(mb)) / np.sqrt((blocks(va) + blocks(vb)) / 16 + 1e-12)
     assert np.abs(zt).max() <= 4.0
     assert abs(ma.mean() - mb.mean()) <= 3 * np.sqrt((va + vb).sum()) / ma.size
+
+
+def test_oracle_refuses_a_scene_without_objects(tmp_path):
+    """An empty scene is an error for the oracle as for the library (the reference's BVH build
+    crashes on it)."""
+    cfg = scenes.config_json(13, 7, 2, 4)
+    cp, sp = scenes.write_scene(str(tmp_path), cfg, scenes.camera((0, 0, -4), (0, 0, 0), 40), [], "empty")
+    with pytest.raises(Exception):
+        B.oracle_open(cp, sp)
