@@ -30,6 +30,11 @@ __host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N) {
            | ((uint32_t)(M >> 4) << 24);  // M / 16
 }
 
+// bit layout: [4,6) D format, [7,10) A format, [10,13) B format, [15] A major, [16] B major,
+// [17,23) N >> 3, [24,29) M >> 4
+static_assert(umma_idesc_bf16(128, 64) == ((1u << 4) | (1u << 7) | (1u << 10) | (8u << 17) | (8u << 24)), "idesc M=128 N=64");
+static_assert(umma_idesc_bf16(128, 48) == ((1u << 4) | (1u << 7) | (1u << 10) | (6u << 17) | (8u << 24)), "idesc M=128 N=48");
+
 // D[tmem] (+)= A[smem] * B[smem]^T for one K=16 step; issued by a single thread.
 __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, int accumulate) {
     asm volatile(
