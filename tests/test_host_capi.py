@@ -199,3 +199,25 @@ def test_scene_without_objects_is_rejected(tmp_path):
     for name, objs in (("empty", []), ("point_only", [scenes.point_light((0, 2, 0), (10, 10, 10))])):
         cp, sp = scenes.write_scene(str(tmp_path), cfg, scenes.camera((0, 0, -4), (0, 0, 0), 40), objs, name)
         _expect(N.C2G_ERR_INVALID, lambda: Context(device=-1).load(cp, sp))
+
+
+def test_new_entry_points_reject_bad_arguments(tmp_path):
+    """Null pointers and a context without a device give status codes, never a crash."""
+    lib = N.load_library()
+    img = np.zeros((2, 3, 3), np.float32)
+    assert lib.c2g_write_hdr(None, 3, 2, N.fptr(img)) == N.C2G_ERR_INVALID
+    assert lib.c2g_write_hdr(str(tmp_path / "x.hdr").encode(), 0, 2, N.fptr(img)) == N.C2G_ERR_INVALID
+    assert lib.c2g_write_hdr(str(tmp_path / "x.hdr").encode(), 3, 2, None) == N.C2G_ERR_INVALID
+    assert lib.c2g_film_write_hdr(None, b"x.hdr") == N.C2G_ERR_INVALID
+    assert lib.c2g_sampler_values(None, 1, None, None, None, 0, 1, None) == N.C2G_ERR_INVALID
+    ctx = Context(device=-1)
+    # no scene loaded
+    assert lib.c2g_film_write_hdr(ctx.handle, str(tmp_path / "y.hdr").encode()) == N.C2G_ERR_STATE
+    px = np.zeros(1, np.int32)
+    out = np.zeros(2, np.float32)
+    assert lib.c2g_sampler_values(ctx.handle, 1, N.iptr(px), N.iptr(px), N.iptr(px), 0, 1, N.fptr(out)) == N.C2G_ERR_STATE
+    cp, sp = scenes.cornell(str(tmp_path / "c"), width=8, height=8, spp=1)
+    ctx.load(cp, sp)
+    # a host-only context has no device to draw samples on
+    assert lib.c2g_sampler_values(ctx.handle, 1, N.iptr(px), N.iptr(px), N.iptr(px), 0, 1, N.fptr(out)) != N.C2G_OK
+    assert lib.c2g_sampler_values(ctx.handle, 1, N.iptr(px), N.iptr(px), N.iptr(px), -1, 1, N.fptr(out)) == N.C2G_ERR_INVALID
