@@ -49,7 +49,7 @@ WORKLOAD = {
     "materials": "GGX U(0.05,0.8), aniso GGX U(0.05,0.6)^2, glass IOR 1.5 a=0.1, mirror, diffuse U(0.2,0.9)",
     "lights": "2 area quads Le=20 (4 triangle lights) + point light flux 50*4pi",
     "resolution": "1920x1080", "spp_full_render": 256, "max_depth": 16, "sampler": "Halton",
-    "tree": "SAH (binned, 16 bins, leaves <= 4)", "accel_semantics": "BVH",
+    "tree": "SAH (binned, 16 bins, leaves <= 2), collapsed to four-wide nodes", "accel_semantics": "BVH",
 }
 
 

@@ -52,7 +52,9 @@ int build_and_upload(c2g_ctx* ctx, int tree) {
     // the reference tree is always built: it defines the primitive order the parity checks use
     build_ref_tree(*ctx->scene, ctx->ref);
     if (tree == C2G_TREE_SAH) {
-        build_sah_tree(*ctx->scene, ctx->sah, 4);
+        // leaves of at most two primitives: on the 2.05M-triangle 1080p scene 10.3 node visits and
+        // 1.9 triangle tests per shadow ray against 9.9 and 3.0 with four, 2.8% faster per step
+        build_sah_tree(*ctx->scene, ctx->sah, 2);
         collapse_bvh4(ctx->sah);
     }
     ctx->tree = tree;
