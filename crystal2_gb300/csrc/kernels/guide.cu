@@ -509,7 +509,7 @@ __device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, floa
     // the mixture with the BSDF: lobe gradients scale by c q / q_mix; the selection logit s gets
     // -w (q - p_bsdf) dc/ds / q_mix
     const float sg = 1.f / (1.f + __expf(-o[40]));
-    const float csel = 0.05f + 0.9f * sg;
+    const float csel = kGuideSelMin + kGuideSelSpan * sg;
     const float qmix = fmaxf((1.f - csel) * pb + csel * q, 1e-20f);
     const float rho = csel * q / qmix;
 #pragma unroll
@@ -522,7 +522,7 @@ __device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, floa
         const float dk = 1.f / kap - 2.f * e2 / fmaxf(-expm1f(-2.f * kap), 1e-20f) + (c - 1.f);
         const float kraw = o[5 * k + 3];
         float sig = 1.f / (1.f + __expf(-kraw));
-        if (kap >= 2000.f) sig = 0.f;
+        if (kap >= kGuideKappaMax) sig = 0.f;
         const float3 m = f3(o[5 * k], o[5 * k + 1], o[5 * k + 2]);
         const float len = fmaxf(sqrtf(dot(m, m)), 1e-12f);
         const float3 dm = (wi - L[k].mu * c) * (kap / len);
@@ -532,7 +532,7 @@ __device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, floa
         g[5 * k + 3] = -w * rho * r * dk * sig;
         g[5 * k + 4] = -w * rho * (r - L[k].w);
     }
-    g[40] = -w * (q - pb) * 0.9f * sg * (1.f - sg) / qmix;
+    g[40] = -w * (q - pb) * kGuideSelSpan * sg * (1.f - sg) / qmix;
 #pragma unroll
     for (int k = 0; k < kGuideOut; k++) {
         const float v = g[k];
@@ -795,9 +795,9 @@ int GuideTrainer::init(DeviceArena& arena, size_t paths, int max_depth, const fl
                 }
         }
         // selection bias: the untrained network draws from the mixture with probability
-        // 1 - alpha (the configured BSDF fraction), c = 0.05 + 0.9 sigmoid(s)
-        const float c0 = std::min(0.94f, std::max(0.06f, 1.f - alpha_));
-        const float sg = (c0 - 0.05f) / 0.9f;
+        // 1 - alpha (the configured BSDF fraction), c = 0.05 + 0.75 sigmoid(s)
+        const float c0 = std::min(kGuideSelMin + 0.99f * kGuideSelSpan, std::max(kGuideSelMin + 0.01f * kGuideSelSpan, 1.f - alpha_));
+        const float sg = (c0 - kGuideSelMin) / kGuideSelSpan;
         h[guide_b_off(3) + 40] = std::log(sg / (1.f - sg));
         cudaMemcpy(params_, h.data(), kGuideParams * 4, cudaMemcpyHostToDevice);
         cudaMemset(grad_, 0, kGuideParams * 4);

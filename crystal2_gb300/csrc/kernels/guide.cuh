@@ -78,7 +78,7 @@ __device__ __forceinline__ void guide_lobes(const float* out, Lobe* L) {
         float3 m = f3(out[5 * k], out[5 * k + 1], out[5 * k + 2]);
         float len = sqrtf(dot(m, m));
         L[k].mu = len > 1e-12f ? m * (1.f / len) : f3(0.f, 1.f, 0.f);
-        L[k].kappa = fminf(softplusf(out[5 * k + 3]) + 0.05f, 2000.f);
+        L[k].kappa = fminf(softplusf(out[5 * k + 3]) + 0.05f, kGuideKappaMax);
         L[k].w = __expf(out[5 * k + 4] - mx);
         sum += L[k].w;
     }
@@ -99,8 +99,10 @@ __device__ __forceinline__ float vmf_pdf(const Lobe& l, float3 w) {
 // the BSDF.  A non-finite network output is flagged by a NaN first weight.
 constexpr int kGuidePacked = 52;
 
-// Technique selection: c = 0.05 + 0.9 sigmoid(s) keeps both techniques in use.
-__host__ __device__ __forceinline__ float guide_select(float s) { return 0.05f + 0.9f / (1.f + expf(-s)); }
+// Technique selection: c = 0.05 + 0.75 sigmoid(s) keeps both techniques in use; at least a fifth
+// of the continuations follow the BSDF (a defensive mixture: a mixture that trained onto a few
+// sharp lobes cannot make the weights larger than 5x the BSDF-only ones).
+__host__ __device__ __forceinline__ float guide_select(float s) { return kGuideSelMin + kGuideSelSpan / (1.f + expf(-s)); }
 
 __device__ __forceinline__ void pack_lobes(const float* out, float* dst) {
     bool finite = true;

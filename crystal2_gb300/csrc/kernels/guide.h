@@ -15,6 +15,9 @@ constexpr int kGuideOutPad = 48;    // output layer padded to a multiple of 16 (
 constexpr int kGuideLobes = 8;
 constexpr int kGuideFreqs = 12;
 constexpr int kGuideLayers = 4;
+constexpr float kGuideKappaMax = 500.f;   // vMF concentration cap (about 2.5 degrees of spread)
+constexpr float kGuideSelMin = 0.05f;     // selection probability c in [0.05, 0.8]
+constexpr float kGuideSelSpan = 0.75f;
 // Layer shapes (inputs, outputs).
 __host__ __device__ constexpr int guide_k(int l) { return l == 0 ? kGuideIn : kGuideHidden; }
 __host__ __device__ constexpr int guide_n(int l) { return l == 3 ? kGuideOutPad : kGuideHidden; }

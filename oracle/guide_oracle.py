@@ -13,8 +13,8 @@ restates the network defined by the library's C ABI (include/c2g.h, "learned gui
 * layers 80->64->64->64->48 with ReLU after the hidden layers; parameters are one flat vector,
   per layer W (K x N row-major) then b (N);
 * outputs 5 per lobe (8 lobes): mean direction (normalised), concentration softplus(k) + 0.05
-  (capped at 2000), weight softmax(logit); density q = sum_k w_k vMF(wi; mu_k, kappa_k); output 40
-  is the selection logit s: the sampler draws from q with probability c = 0.05 + 0.9 sigmoid(s)
+  (capped at 500), weight softmax(logit); density q = sum_k w_k vMF(wi; mu_k, kappa_k); output 40
+  is the selection logit s: the sampler draws from q with probability c = 0.05 + 0.75 sigmoid(s)
   and from the BSDF otherwise, so the training loss is -w log q_mix, q_mix = (1 - c) p_bsdf + c q.
 
 ``bf16=True`` rounds at the points where the kernels store BF16 (encoded inputs, weights, hidden
@@ -27,6 +27,8 @@ import numpy as np
 
 N_IN, HIDDEN, N_OUT, N_OUT_PAD, LOBES, FREQS = 80, 64, 41, 48, 8, 12
 SHAPES = [(N_IN, HIDDEN), (HIDDEN, HIDDEN), (HIDDEN, HIDDEN), (HIDDEN, N_OUT_PAD)]
+KAPPA_MAX = 500.0            # vMF concentration cap
+SEL_MIN, SEL_SPAN = 0.05, 0.75  # selection probability c in [0.05, 0.8]
 N_PARAMS = sum(k * n + n for k, n in SHAPES)
 
 
@@ -104,7 +106,7 @@ def lobes(out):
     m = o[:, :, :3]
     ln = np.linalg.norm(m, axis=2, keepdims=True)
     mu = np.where(ln > 1e-12, m / np.maximum(ln, 1e-300), np.array([0.0, 1.0, 0.0]))
-    kappa = np.minimum(softplus(o[:, :, 3]) + 0.05, 2000.0)
+    kappa = np.minimum(softplus(o[:, :, 3]) + 0.05, KAPPA_MAX)
     lg = o[:, :, 4]
     e = np.exp(lg - lg.max(axis=1, keepdims=True))
     w = e / e.sum(axis=1, keepdims=True)
@@ -122,7 +124,7 @@ def mixture_pdf(out, wi):
 
 
 def select_prob(s):
-    return 0.05 + 0.9 / (1 + np.exp(-s))
+    return SEL_MIN + SEL_SPAN / (1 + np.exp(-s))
 
 
 def nll_gradient(params, enc, wi, weight, pb, bf16_mode=True, clamp=1e3):
@@ -131,7 +133,7 @@ def nll_gradient(params, enc, wi, weight, pb, bf16_mode=True, clamp=1e3):
     Output-gradient formulas, with rho = c q / q_mix: d log q_mix / d logit_k = rho (r_k - w_k)
     (r = posterior lobe share); d log q_mix / d kraw_k = rho r_k (1/kappa - 2 e^-2kappa /
     (1 - e^-2kappa) + mu.wi - 1) sigmoid(kraw) (zero where kappa is capped); d log q_mix / d m_k =
-    rho r_k kappa (wi - mu (mu.wi)) / |m_k|; d log q_mix / d s = (q - p_bsdf) 0.9 sigmoid'(s) / q_mix.
+    rho r_k kappa (wi - mu (mu.wi)) / |m_k|; d log q_mix / d s = (q - p_bsdf) 0.75 sigmoid'(s) / q_mix.
     """
     r = bf16 if bf16_mode else (lambda v: np.asarray(v, np.float64))
     layers = unpack(params)
@@ -145,14 +147,14 @@ def nll_gradient(params, enc, wi, weight, pb, bf16_mode=True, clamp=1e3):
     rr = p / q[:, None]
     pb = np.asarray(pb, np.float64)
     sg = 1 / (1 + np.exp(-out[:, 40]))
-    csel = 0.05 + 0.9 * sg
+    csel = SEL_MIN + SEL_SPAN * sg
     qmix = np.maximum((1 - csel) * pb + csel * q, 1e-20)
     rho = (csel * q / qmix)[:, None]
     c = np.einsum("mkj,mj->mk", mu, wi)
     e2 = np.exp(-2 * kappa)
     dk = 1 / kappa - 2 * e2 / np.maximum(-np.expm1(-2 * kappa), 1e-20) + (c - 1)
     sig = 1 / (1 + np.exp(-o[:, :, 3]))
-    sig = np.where(kappa >= 2000.0, 0.0, sig)
+    sig = np.where(kappa >= KAPPA_MAX, 0.0, sig)
     ln = np.maximum(np.linalg.norm(o[:, :, :3], axis=2), 1e-12)
     dm = (wi[:, None, :] - mu * c[:, :, None]) * (kappa / ln)[:, :, None]
     g = np.zeros((out.shape[0], N_OUT_PAD))
@@ -162,7 +164,7 @@ def nll_gradient(params, enc, wi, weight, pb, bf16_mode=True, clamp=1e3):
     gv[:, :, 3] = -ww * rho * rr * dk * sig
     gv[:, :, 4] = -ww * rho * (rr - w)
     g[:, :LOBES * 5] = gv.reshape(-1, LOBES * 5)
-    g[:, 40] = -wgt * (q - pb) * 0.9 * sg * (1 - sg) / qmix
+    g[:, 40] = -wgt * (q - pb) * SEL_SPAN * sg * (1 - sg) / qmix
     if clamp is not None:
         g = np.clip(np.where(np.isfinite(g), g, 0.0), -clamp, clamp)
     active = wgt > 0
