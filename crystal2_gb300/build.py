@@ -67,7 +67,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def host(src: str) -> str:
         obj = os.path.join(BUILD, src.replace("/", "_") + ".o")
-        cmd = [cxx, "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
+        cmd = [cxx, "-std=c++17", "-O2", "-fPIC", "-pthread", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
                f"-I{cuda_inc}", *inc, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -91,7 +91,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         futs = [ex.submit(host, s) for s in HOST_SOURCES] + [ex.submit(cuda, s) for s in CUDA_SOURCES]
         objs = [f.result() for f in futs]
     tmp = LIB + ".tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    cmd = [nvcc, *ARCH, "-shared", "-Xcompiler", "-pthread", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stderr[-4000:])

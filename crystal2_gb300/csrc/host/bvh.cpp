@@ -6,6 +6,8 @@
 #include <climits>
 #include <cmath>
 #include <limits>
+#include <thread>
+#include <vector>
 
 namespace c2g {
 
@@ -112,12 +114,16 @@ struct ChildRef {
     int count;   // 0 internal, else prim count
 };
 
+// Subtrees of at least this many objects above depth par_depth are built on their own thread.
+constexpr int kParallelMin = 4096;
+
 struct SahBuilder {
     const std::vector<Box>& boxes;
     const std::vector<float>& centers;
     std::vector<int>& objs;
     std::vector<WideNode>& nodes;
     int max_leaf;
+    int par_depth = 0;   // 2^par_depth threads at most
     int max_depth = 0;
     int leaves = 0;
 
@@ -189,8 +195,31 @@ struct SahBuilder {
         }
         int self = (int)nodes.size();
         nodes.emplace_back();
-        ChildRef L = build(begin, mid, depth + 1);
-        ChildRef R = build(mid, end, depth + 1);
+        ChildRef L, R;
+        if (depth < par_depth && n >= kParallelMin) {
+            // The right subtree is built on another thread into its own node array and appended
+            // after the left one, renumbered: the same depth-first node order, so the same tree
+            // as the sequential build.
+            std::vector<WideNode> rnodes;
+            SahBuilder rb{boxes, centers, objs, rnodes, max_leaf, par_depth};
+            ChildRef Rr;
+            std::thread t([&] { Rr = rb.build(mid, end, depth + 1); });
+            L = build(begin, mid, depth + 1);
+            t.join();
+            const int off = (int)nodes.size();
+            for (WideNode& w : rnodes) {
+                if (w.n0 == 0) w.c0 += off;
+                if (w.n1 == 0) w.c1 += off;
+            }
+            nodes.insert(nodes.end(), rnodes.begin(), rnodes.end());
+            R = Rr;
+            if (R.count == 0) R.index += off;
+            leaves += rb.leaves;
+            max_depth = std::max(max_depth, rb.max_depth);
+        } else {
+            L = build(begin, mid, depth + 1);
+            R = build(mid, end, depth + 1);
+        }
         WideNode& w = nodes[self];
         for (int k = 0; k < 3; k++) {
             w.lo0[k] = L.box.mn[k]; w.hi0[k] = L.box.mx[k];
@@ -231,7 +260,9 @@ void build_sah_tree(const HostScene& s, SahTree& out, int max_leaf) {
     for (size_t i = 0; i < n; i++) out.order[i] = (int)i;
     out.nodes.clear();
     out.nodes.reserve(n);
-    SahBuilder b{boxes, centers, out.order, out.nodes, std::max(1, max_leaf)};
+    int par_depth = 0;
+    for (unsigned t = std::max(1u, std::min(64u, std::thread::hardware_concurrency())); t > 1; t >>= 1) par_depth++;
+    SahBuilder b{boxes, centers, out.order, out.nodes, std::max(1, max_leaf), par_depth + 1};
     if ((int)n <= b.max_leaf) {
         // Single leaf: child 1 is an empty box that never intersects.
         Box bb = empty_box();
