@@ -1,6 +1,7 @@
 #include "scene.h"
 #include <cstdlib>
 #include <cmath>
+#include <map>
 #include <cctype>
 
 #include <algorithm>
@@ -171,7 +172,18 @@ Image load_image(const std::string& path, const ImageRegistry* reg) {
 struct Loader {
     HostScene& s;
     const ImageRegistry* images = nullptr;
+    // OBJ files parsed so far in this load, by path: a scene that instances one mesh many times
+    // (the reference reads the file again for every object) parses it once
+    std::map<std::string, std::vector<ObjVertex>> objs_read;
     explicit Loader(HostScene& sc, const ImageRegistry* reg = nullptr) : s(sc), images(reg) {}
+
+    const std::vector<ObjVertex>& obj_vertices(const std::string& path) {
+        auto it = objs_read.find(path);
+        if (it != objs_read.end()) return it->second;
+        std::vector<ObjVertex> v;
+        load_obj(path, v);
+        return objs_read.emplace(path, std::move(v)).first->second;
+    }
 
     // ImageTexels::CreateImageTexels (Texel.cpp:4-38): texel = (byte / 255)^2.2 in float.
     int add_texture(const std::string& path) {
@@ -283,8 +295,7 @@ struct Loader {
             s.quad_box.insert(s.quad_box.end(), box, box + 6);
             out.push_back({type == "Sphere" ? SHAPE_SPHERE : SHAPE_DISK, (int)s.quads.size() - 1});
         } else if (type == "TriangleMesh") {
-            std::vector<ObjVertex> verts;
-            load_obj(n.at("ObjFile").as_string(), verts);
+            std::vector<ObjVertex> verts = obj_vertices(n.at("ObjFile").as_string());
             // TriangleMesh::CreateTriangleMesh (TriangleMesh.cpp:9-27)
             V3 pos = parse_vec3(n.at("Translation"));
             V3 scl = parse_vec3(n.at("Scale"));
