@@ -188,7 +188,10 @@ def run_reference(args) -> None:
     line = {"metric": "Mpaths/s at 1080p (many-material scene, MIS path tracer)", "value": v, "unit": "Mpaths/s",
             "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": 1e3 * cal["rows"] * 1920 / (v * 1e6),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded scene generator)", "config": dict(WORKLOAD, parallelism="cpu threads"),
+            "data": "synthetic (seeded scene generator)",
+            "config": dict(WORKLOAD, parallelism="cpu threads",
+                           tree="the reference's own binary BVH, equal-count splits (BVH::Build)",
+                           traversal="the reference's stack traversal (BVH::Intersect / IntersectTest)"),
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "Mpaths/s", "cores": cal["cores"], "kind": cal["kind"], "sample": cal["sample"]},
             "e2e": {"value": v, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

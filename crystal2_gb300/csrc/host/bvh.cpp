@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <exception>
 #include <limits>
 #include <thread>
 #include <vector>
@@ -203,9 +204,24 @@ struct SahBuilder {
             std::vector<WideNode> rnodes;
             SahBuilder rb{boxes, centers, objs, rnodes, max_leaf, par_depth};
             ChildRef Rr;
-            std::thread t([&] { Rr = rb.build(mid, end, depth + 1); });
-            L = build(begin, mid, depth + 1);
+            std::exception_ptr r_err;
+            std::thread t([&] {
+                try {
+                    Rr = rb.build(mid, end, depth + 1);
+                } catch (...) {
+                    r_err = std::current_exception();
+                }
+            });
+            // the thread is joined on every way out of this block (a failed left build included),
+            // so an exception reaches the caller instead of std::terminate
+            try {
+                L = build(begin, mid, depth + 1);
+            } catch (...) {
+                t.join();
+                throw;
+            }
             t.join();
+            if (r_err) std::rethrow_exception(r_err);
             const int off = (int)nodes.size();
             for (WideNode& w : rnodes) {
                 if (w.n0 == 0) w.c0 += off;
@@ -260,8 +276,9 @@ void build_sah_tree(const HostScene& s, SahTree& out, int max_leaf) {
     for (size_t i = 0; i < n; i++) out.order[i] = (int)i;
     out.nodes.clear();
     out.nodes.reserve(n);
+    // parallel depth: log2 of the hardware threads (at most 8) plus one, so at most 16 threads
     int par_depth = 0;
-    for (unsigned t = std::max(1u, std::min(64u, std::thread::hardware_concurrency())); t > 1; t >>= 1) par_depth++;
+    for (unsigned t = std::max(1u, std::min(8u, std::thread::hardware_concurrency())); t > 1; t >>= 1) par_depth++;
     SahBuilder b{boxes, centers, out.order, out.nodes, std::max(1, max_leaf), par_depth + 1};
     if ((int)n <= b.max_leaf) {
         // Single leaf: child 1 is an empty box that never intersects.

@@ -1639,14 +1639,25 @@ int GpuScene::render_noalloc(const c2g_render_params& p, float4* film_dev, cudaS
     int* C = w.counters;
     PathRefs buf[2] = {{w.o[0], w.d[0], w.beta[0], w.L[0]}, {w.o[1], w.d[1], w.beta[1], w.L[1]}};
     C2G_CUDA(cudaMemsetAsync(m2, 0, P * 16, st));
+    // Bounce levels: as in render(), direct lighting keeps walking through surfaces without a
+    // material past the depth (the reference's DirectLightingIntegrator continues such a path at the
+    // same level), up to 255 hops, and stops once its queue is empty.
+    const int levels = p.integrator == C2G_INTEGRATOR_DIRECT ? 255 : p.max_depth;
     for (int s0 = 0; s0 < p.sample_count; s0++) {
         a.wave_samples = 1;
         a.sample0 = p.sample_begin + s0;
         C2G_CUDA(cudaMemsetAsync(C, 0, 256, st));  // counters start at zero for every wave
         k_raygen<<<g_raygen, 256, 0, st>>>(S, a, buf[0], w.out_L, C + 0);
         int cur = 0;
-        for (int b = 0; b < p.max_depth; b++) {
+        for (int b = 0; b < levels; b++) {
             int nxt = cur ^ 1;
+            if (b >= a.max_depth) {
+                // the queue count goes to a host stack variable: no allocation
+                int qn = 0;
+                C2G_CUDA(cudaMemcpyAsync(&qn, C + cur, sizeof(int), cudaMemcpyDeviceToHost, st));
+                C2G_CUDA(cudaStreamSynchronize(st));
+                if (qn == 0) break;
+            }
             C2G_CUDA(cudaMemsetAsync(C + kCntBucket, 0, sizeof(int) * kBuckets, st));
             k_extend<false><<<g_ext, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
                                                      C + kCntBucket, w.bucket_list, (int)w.P, nullptr);

@@ -46,6 +46,12 @@ OUT = os.path.join(HERE, "_ref")
 SCRATCH = os.path.join(OUT, "src")
 LIB = os.path.join(OUT, "libc2ref.so")
 HARNESS = os.path.join(HERE, "ref_harness.cpp")
+# The reference checkout: $C2_REFERENCE_SRC, else a sibling directory ``reference`` of the repository.
+DEFAULT_REF = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
+def reference_tree() -> str:
+    return os.environ.get("C2_REFERENCE_SRC") or DEFAULT_REF
 
 # Reference translation units on the path (everything in src/ except the GL app shell and demos).
 EXCLUDE = {"src/CrystalEngine.cpp", "src/Demos/BRDFDemo.cpp"}
@@ -124,7 +130,7 @@ def _includes() -> list[str]:
 def build(ref: str | None = None, force: bool = False, jobs: int | None = None) -> str:
     """Build ``oracle/_ref/libc2ref.so``; return its path.  Raises on a failed compile."""
     if ref is None:
-        ref = os.environ.get("C2_REFERENCE_SRC", "/root/reference")
+        ref = reference_tree()
     have_ref = os.path.isdir(os.path.join(ref, "src"))
     if have_ref and (force or not os.path.isdir(SCRATCH)):
         _copy_tree(ref)
