@@ -128,20 +128,38 @@ def load_peaks() -> tuple[dict, str]:
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "of fallback"
 
 
-def load_traffic(kernel: str) -> float | None:
-    """DRAM bytes per launch of `kernel` on this workload from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "traffic_many_material_1080p.txt")
-    if not os.path.exists(p):
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic_many_material_1080p.md")
+
+
+def load_traffic(kernel: str) -> dict | None:
+    """Measured bytes per ray of `kernel` on this workload from the committed ncu summary: a line
+    `per_ray <kernel> dram <bytes> l2 <bytes>` (DRAM read + write, and L2 tag traffic, over the
+    launches of one step divided by the rays they traced)."""
+    if not os.path.exists(TRAFFIC_FILE):
         return None
-    with open(p) as fh:
+    with open(TRAFFIC_FILE) as fh:
         for ln in fh:
-            parts = ln.split()
-            if len(parts) >= 2 and parts[0] == kernel:
+            parts = ln.strip().strip("`").split()
+            if len(parts) >= 6 and parts[0] == "per_ray" and parts[1] == kernel:
                 try:
-                    return float(parts[1])
+                    return {"dram": float(parts[3]), "l2": float(parts[5])}
                 except ValueError:
                     return None
     return None
+
+
+def l2_read_peak(device: int) -> float | None:
+    """L2 read bandwidth (GB/s) measured by the library's probe: 64 MB read 50 times by every SM
+    with L2-only loads (c2g_probe_l2_read); the best of three."""
+    import ctypes as C
+    from crystal2_gb300 import _native as N
+    lib = N.load_library()
+    best = None
+    for _ in range(3):
+        g = C.c_double(0.0)
+        if lib.c2g_probe_l2_read(device, 64 << 20, 50, C.byref(g)) == 0:
+            best = max(best or 0.0, g.value)
+    return best
 
 
 def cpu_baseline(cfg_dir: str, budget_s: float = 12.0, rows: int | None = None) -> dict:
@@ -318,11 +336,26 @@ def run_ours(args) -> None:
     bytes_per_launch = alg_bytes_per_step / max(1, launches_per_step)
     achieved = bytes_per_launch / max(avg_launch_s, 1e-12) / 1e9
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = load_traffic(names[top_trav])
+    rays_per_launch = rays / max(1, launches_per_step)
+    measured = load_traffic(names[top_trav])
+    traffic = None if measured is None else measured["dram"] * rays_per_launch
     roof = {"kernel": names[top_trav], "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
             "alg_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
             "per_ray": {"nodes": nodes / max(1, rays), "prims": prims / max(1, rays)}}
+    # the roof the traversal actually meets: L2 (the scene's nodes and triangles are re-read by
+    # every ray from L2), against an L2 read peak measured on this GPU
+    l2_peak = l2_read_peak(local)
+    if measured is not None and l2_peak:
+        l2_bytes = measured["l2"] * rays_per_launch
+        l2_ach = l2_bytes / max(avg_launch_s, 1e-12) / 1e9
+        roof["l2"] = {"achieved": l2_ach, "peak": l2_peak, "unit": "GB/s", "frac": l2_ach / l2_peak,
+                      "bytes_per_launch": l2_bytes, "dram_frac": traffic / max(avg_launch_s, 1e-12) / 1e9 / peak,
+                      "peak_source": "measured: c2g_probe_l2_read (64 MB, 50 reads, L2-only loads, every SM)",
+                      "traffic_source": os.path.relpath(TRAFFIC_FILE, ROOT)}
+    elif l2_peak:
+        roof["l2"] = {"peak": l2_peak, "unit": "GB/s", "achieved": None, "frac": None,
+                      "peak_source": "measured: c2g_probe_l2_read (64 MB, 50 reads, L2-only loads, every SM)"}
     share = {names[k]: float(kernel_ms[k] / max(1e-9, kernel_ms.sum())) for k in range(N.K_KINDS) if kernel_n[k] > 0}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

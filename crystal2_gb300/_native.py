@@ -106,6 +106,7 @@ SIGNATURES = {
     "c2g_get_stats": (_I, [_P, C.POINTER(Stats)]),
     "c2g_set_counting": (_I, [_P, _I]),
     "c2g_set_traversal": (_I, [_P, _I]),
+    "c2g_probe_l2_read": (_I, [_I, C.c_size_t, _I, C.POINTER(C.c_double)]),
     "c2g_trace_rays": (_I, [_P, _I, _FP, _FP, _FP, _FP, _IP, _I, _IP, _FP]),
     "c2g_trace_rays_dev": (_I, [_P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
     "c2g_halton": (_I, [_P, _I, _I, _I, _IP, _IP, _IP, _I, _FP]),

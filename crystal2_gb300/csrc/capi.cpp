@@ -434,6 +434,15 @@ int c2g_set_traversal(c2g_ctx* ctx, int width) {
     return C2G_OK;
 }
 
+int c2g_probe_l2_read(int device, size_t bytes, int reps, double* gbs) {
+    if (!gbs) return C2G_ERR_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return C2G_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return C2G_ERR_CUDA;
+    std::string err;
+    return c2g::probe_l2_read(bytes, reps, gbs, err);
+}
+
 int c2g_trace_rays_dev(c2g_ctx* ctx, int n, const float* o_dev, const float* d_dev, const float* tmin_dev,
                        const float* tmax_dev, const int* ignore_dev, int any_hit, int* obj_dev, float* t_dev, void* stream) {
     if (!ctx || n < 0 || (n > 0 && (!o_dev || !d_dev || !obj_dev))) return fail(ctx, C2G_ERR_INVALID, "null argument");

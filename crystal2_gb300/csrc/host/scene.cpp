@@ -455,7 +455,10 @@ void load_scene(HostScene& s, const std::string& config_text, const std::string&
     const Json& smp = integ.at("Sampler");
     s.cfg.sampler = smp.at("Type").as_string();
     s.cfg.seed = smp.at("Seed").as_int();
-    if (s.cfg.integrator != "PathTracer" && s.cfg.integrator != "DirectLight" && s.cfg.integrator != "GuidedPathTracer")
+    // "GPUPathTracer" is the key under which a reference build registers this library's path
+    // tracer in its own factory; here it selects the same integrator as "PathTracer".
+    if (s.cfg.integrator != "PathTracer" && s.cfg.integrator != "DirectLight" && s.cfg.integrator != "GuidedPathTracer" &&
+        s.cfg.integrator != "GPUPathTracer")
         throw SceneError(C2G_ERR_INVALID, "Invalid Integrator Type!");
     s.cfg.depth = (int)integ.at("Depth").as_int();
     if (s.cfg.sampler != "Halton" && s.cfg.sampler != "Default" && s.cfg.sampler != "Stratified")

@@ -1678,4 +1678,54 @@ int GpuScene::render_noalloc(const c2g_render_params& p, float4* film_dev, cudaS
     return check_device_error(err);
 }
 
+// ---- L2 read roof ---------------------------------------------------------------------------------
+namespace {
+__global__ void k_l2_read(const float4* __restrict__ p, size_t n, int reps, float* sink) {
+    float acc = 0.f;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (int r = 0; r < reps; r++) {
+#pragma unroll 4
+        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+            const float4 v = __ldcg(p + i);  // L2 only: every rep after the first is an L2 hit
+            acc += (v.x + v.y) + (v.z + v.w);
+        }
+    }
+    if (acc == -1.f) *sink = acc;  // keeps the loads live; the buffer holds no negative values
+}
+}  // namespace
+
+int probe_l2_read(size_t bytes, int reps, double* gbs, std::string& err) {
+    if (bytes < 4096 || reps < 1) { err = "probe size out of range"; return C2G_ERR_INVALID; }
+    const size_t n = bytes / 16;
+    float4* buf = nullptr;
+    float* sink = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = C2G_OK;
+    do {
+        if (cudaMalloc(&buf, n * 16) != cudaSuccess || cudaMalloc(&sink, sizeof(float)) != cudaSuccess) { rc = C2G_ERR_OOM; break; }
+        if (cudaMemset(buf, 0, n * 16) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+            rc = C2G_ERR_CUDA;
+            break;
+        }
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int grid = sms * 8;
+        k_l2_read<<<grid, 256>>>(buf, n, 2, sink);  // brings the buffer into L2
+        cudaEventRecord(e0);
+        k_l2_read<<<grid, 256>>>(buf, n, reps, sink);
+        cudaEventRecord(e1);
+        if (cudaEventSynchronize(e1) != cudaSuccess) { rc = C2G_ERR_CUDA; break; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        *gbs = (double)n * 16.0 * reps / (ms * 1e-3) / 1e9;
+    } while (0);
+    if (rc) err = "L2 probe failed";
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(buf);
+    cudaFree(sink);
+    return rc;
+}
+
 }  // namespace c2g

@@ -139,4 +139,9 @@ private:
     int film_w_ = 0, film_h_ = 0;
 };
 
+// L2 read bandwidth of the current device in GB/s: a buffer of `bytes` (small enough to stay in L2)
+// read `reps` times by every SM with loads cached in L2 only.  The denominator of the traversal
+// kernels' L2 roofline.
+int probe_l2_read(size_t bytes, int reps, double* gbs, std::string& err);
+
 }  // namespace c2g

@@ -178,6 +178,11 @@ int c2g_set_counting(c2g_ctx* ctx, int flags);
  * same leaves; no counterpart in the reference (its BVH is binary). */
 int c2g_set_traversal(c2g_ctx* ctx, int width);
 
+/* L2 read bandwidth of `device` in GB/s: a `bytes` buffer (keep it well below the L2 size) read
+ * `reps` times by every SM with L2-only loads, timed with CUDA events.  No counterpart in the
+ * reference; it is the measured L2 roof beside which the traversal kernels' bandwidth is reported. */
+int c2g_probe_l2_read(int device, size_t bytes, int reps, double* gbs);
+
 /* ---- batched multi-job rendering ---------------------------------------------------------------
  * No counterpart in the reference (one scene per RayTracer).  A batch renders many jobs - each a
  * context with its own loaded scene and its own render parameters (path tracer or guided) - on one

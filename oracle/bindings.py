@@ -114,6 +114,28 @@ class RefScene(_Scene):
         secs = self.lib.ref_render_region(self.h, threads, x0, y0, x1, y1, _d(s), _d(q))
         return s, q, secs
 
+    def render_region_groups(self, x0, y0, x1, y1, group, threads=8):
+        """Per-pixel sums of each run of `group` consecutive samples (planes of independent
+        estimates), the sum of squares over all samples, and the wall seconds."""
+        w, h = x1 - x0, y1 - y0
+        ng = (self.spp + group - 1) // group
+        s = np.zeros((ng, h, w, 3))
+        q = np.zeros((h, w, 3))
+        secs = self.lib.ref_render_region_groups(self.h, threads, x0, y0, x1, y1, group, _d(s), _d(q))
+        return s, q, secs
+
+    def intersect_test_mt(self, o, d, tmin, tmax, ignore=None, threads=8):
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        n = o.shape[0]
+        if ignore is None:
+            ignore = np.full(n, -1, np.int32)
+        occ = np.zeros(n, np.int32)
+        self.lib.ref_intersect_test_mt(self.h, n, _f(o), _f(d), _f(np.ascontiguousarray(tmin, np.float32)),
+                                       _f(np.ascontiguousarray(tmax, np.float32)), _i(np.ascontiguousarray(ignore, np.int32)),
+                                       _i(occ), threads)
+        return occ.astype(bool)
+
     def render(self, threads=8):
         s = np.zeros((self.H, self.W, 3), np.float32)
         w = np.zeros((self.H, self.W), np.float32)
@@ -224,6 +246,9 @@ def ref_library():
         lib.ref_render.restype = C.c_double
         lib.ref_render_region.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _D, _D]
         lib.ref_render_region.restype = C.c_double
+        lib.ref_render_region_groups.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _D, _D]
+        lib.ref_render_region_groups.restype = C.c_double
+        lib.ref_intersect_test_mt.argtypes = [C.c_void_p, C.c_int, _F, _F, _F, _F, _I, _I, C.c_int]
         lib.ref_render_samples.argtypes = [C.c_void_p, C.c_int, _I, _I, _F]
         lib.ref_write_hdr.argtypes = [C.c_char_p, C.c_int, C.c_int, _F]
         lib.ref_write_hdr.restype = C.c_int

@@ -34,6 +34,7 @@ library is rebuilt from the copy, which lets an aarch64 host rebuild it.
 from __future__ import annotations
 
 import argparse
+import hashlib
 import os
 import re
 import shutil
@@ -137,8 +138,13 @@ def build(ref: str | None = None, force: bool = False, jobs: int | None = None) 
         _patch_tree()
     if not os.path.isdir(SCRATCH):
         raise FileNotFoundError("no reference tree and no scratch copy under oracle/_ref/src")
-    if os.path.exists(LIB) and not force:
-        return LIB
+    stamp = os.path.join(OUT, "harness.sha256")
+    with open(HARNESS, "rb") as fh:
+        digest = hashlib.sha256(fh.read()).hexdigest()
+    if os.path.exists(LIB) and not force and os.path.exists(stamp):
+        with open(stamp) as fh:
+            if fh.read().strip() == digest:
+                return LIB
     objdir = os.path.join(OUT, "obj")
     os.makedirs(objdir, exist_ok=True)
     inc = _includes()
@@ -164,6 +170,8 @@ def build(ref: str | None = None, force: bool = False, jobs: int | None = None) 
     if r.returncode != 0:
         raise RuntimeError("link failed\n" + r.stderr[-4000:])
     os.replace(tmp, LIB)
+    with open(stamp, "w") as fh:
+        fh.write(digest)
     return LIB
 
 

@@ -270,21 +270,31 @@ int ref_write_hdr(const char* path, int w, int h, const float* rgb) { return stb
 // SamplerIntegrator::Render (SamplerIntegrator.cpp:42-59) calling the integrator's own Evaluate,
 // accumulating sum and sum of squares per pixel (after the FrameBuffer's NaN/Inf zeroing,
 // FrameBuffer.cpp:21-28).  Rows are split across `threads` workers, each with its own sampler
-// clone.  Returns wall seconds.  sum/sumsq: 3 floats per pixel of the rectangle (row-major).
-double ref_render_region(void* h, int threads, int x0, int y0, int x1, int y1, double* sum, double* sumsq) {
-    auto ctx = static_cast<RefCtx*>(h);
+// clone.  With group > 0 the sums are kept per run of `group` consecutive samples (sample s adds to
+// group s / group): sum holds ceil(spp / group) planes of 3 floats per pixel, each plane an
+// independent estimate from its own samples.  Returns wall seconds.  sum/sumsq: 3 doubles per pixel
+// of the rectangle (row-major) per plane; sumsq covers all samples.
+static double render_region_groups(RefCtx* ctx, int threads, int x0, int y0, int x1, int y1, int group, double* sum,
+                                   double* sumsq) {
     auto* si = dynamic_cast<crystal::SamplerIntegrator*>(ctx->integrator.get());
     if (!si) return -1.0;
     int W = ctx->info.Width, H = ctx->info.Height;
-    int rw = x1 - x0;
+    const int spp = (int)si->_sampler->GetSamplesPerPixel();
+    if (group <= 0) group = spp;
+    const int ngroups = (spp + group - 1) / group;
+    const int rw = x1 - x0, rh = y1 - y0;
+    const size_t plane = (size_t)rw * rh * 3;
     std::atomic<int> nextRow{y0};
     auto worker = [&]() {
         auto sampler = si->_sampler->Clone(0);
+        std::vector<double> s(3 * (size_t)ngroups);
         while (true) {
             int yy = nextRow.fetch_add(1);
             if (yy >= y1) break;
             for (int xx = x0; xx < x1; xx++) {
-                double s[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+                std::fill(s.begin(), s.end(), 0.0);
+                double q[3] = {0, 0, 0};
+                int k = 0;
                 sampler->StartPixel(Point2i(xx, yy));
                 do {
                     auto u = sampler->Get2D();
@@ -294,10 +304,14 @@ double ref_render_region(void* h, int threads, int x0, int y0, int x1, int y1, d
                     auto ray = ctx->camera->GenerateRay(pos);
                     auto c = si->Evaluate(ray, ctx->scene.get(), sampler.get());
                     if (glm::isnan(c) != glm::bvec3(false) || glm::isinf(c) != glm::bvec3(false)) c = glm::vec3(0);
-                    for (int k = 0; k < 3; k++) { s[k] += c[k]; q[k] += (double)c[k] * c[k]; }
+                    const int g = std::min(ngroups - 1, k / group);
+                    for (int j = 0; j < 3; j++) { s[3 * g + j] += c[j]; q[j] += (double)c[j] * c[j]; }
+                    k++;
                 } while (sampler->StartNextSample());
                 size_t idx = (size_t)(yy - y0) * rw + (xx - x0);
-                for (int k = 0; k < 3; k++) { sum[3 * idx + k] = s[k]; sumsq[3 * idx + k] = q[k]; }
+                for (int g = 0; g < ngroups; g++)
+                    for (int j = 0; j < 3; j++) sum[g * plane + 3 * idx + j] = s[3 * g + j];
+                for (int j = 0; j < 3; j++) sumsq[3 * idx + j] = q[j];
             }
         }
     };
@@ -309,6 +323,34 @@ double ref_render_region(void* h, int threads, int x0, int y0, int x1, int y1, d
     auto t1 = std::chrono::steady_clock::now();
     (void)H;
     return std::chrono::duration<double>(t1 - t0).count();
+}
+
+double ref_render_region(void* h, int threads, int x0, int y0, int x1, int y1, double* sum, double* sumsq) {
+    return render_region_groups(static_cast<RefCtx*>(h), threads, x0, y0, x1, y1, 0, sum, sumsq);
+}
+
+double ref_render_region_groups(void* h, int threads, int x0, int y0, int x1, int y1, int group, double* sum,
+                                double* sumsq) {
+    return render_region_groups(static_cast<RefCtx*>(h), threads, x0, y0, x1, y1, group, sum, sumsq);
+}
+
+// Scene::IntersectTest on `threads` workers (the same per-ray call as ref_intersect_test).
+void ref_intersect_test_mt(void* h, int n, const float* o, const float* d, const float* tmin, const float* tmax,
+                           const int* ignore_obj, int* occluded, int threads) {
+    auto ctx = static_cast<RefCtx*>(h);
+    auto work = [&](int lo, int hi) {
+        for (int i = lo; i < hi; i++) {
+            Ray3f ray(glm::vec3(o[3 * i], o[3 * i + 1], o[3 * i + 2]), glm::vec3(d[3 * i], d[3 * i + 1], d[3 * i + 2]));
+            const crystal::IIntersectable* ign = nullptr;
+            if (ignore_obj && ignore_obj[i] >= 0) ign = entity_shape(ctx->objects[ignore_obj[i]]);
+            occluded[i] = ctx->scene->IntersectTest(ray, tmin[i], tmax[i], ign) ? 1 : 0;
+        }
+    };
+    int nt = std::max(1, threads);
+    std::vector<std::thread> th;
+    int chunk = (n + nt - 1) / nt;
+    for (int k = 0; k < nt; k++) th.emplace_back(work, std::min(n, k * chunk), std::min(n, (k + 1) * chunk));
+    for (auto& x : th) x.join();
 }
 
 // Per-sample radiance for a few pixels: out[(p * spp + s) * 3 + c].
