@@ -18,8 +18,9 @@ Multi-GPU: the path does not exchange data; `--gpus N` runs N independent replic
 one process per GPU, rendering the same frame; value = all paths / max time.
 
 The second half of the metric, equal-time relMSE of the guided path tracer against the plain
-one, is measured after the timed region on the slit-lit glossy room (`guided_equal_time`;
-`--guided-res 1920x1080 --guided-ref-spp 16384` for the full-size protocol, several minutes).
+one, is measured after the timed region on the slit-lit glossy room (`guided_equal_time`): at the
+metric's 1920 x 1080 against a 16384-spp plain reference by default (about two minutes; smaller
+`--guided-res` / `--guided-ref-spp` for quick runs).
 
 Batched multi-job rendering (64 seeded jobs through replayed CUDA graphs, autotuned wave size and
 stream count) is measured last (`batch_run`; `--no-batch` skips it).
@@ -589,9 +590,9 @@ def main() -> int:
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-guided", action="store_true", help="skip the guided-vs-plain equal-time measurement")
-    ap.add_argument("--guided-res", default="960x540")
+    ap.add_argument("--guided-res", default="1920x1080")
     ap.add_argument("--guided-ref-spp", type=int, default=16384)
-    ap.add_argument("--guided-seconds", type=float, default=4.0)
+    ap.add_argument("--guided-seconds", type=float, default=6.0)
     ap.add_argument("--guided-lr", type=float, default=2e-3)
     ap.add_argument("--guided-bsdf-fraction", type=float, default=0.7)
     ap.add_argument("--guided-train-steps", type=int, default=16)

@@ -23,6 +23,9 @@ HOST_SOURCES = ["host/json.cpp", "host/scene.cpp", "host/bvh.cpp", "capi.cpp"]
 CUDA_SOURCES = ["kernels/render.cu", "kernels/guide.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Extra nvcc options (e.g. -D C2G_SHADOW_MIN_BLOCKS=12 to try another register budget); part of the
+# sources digest, so a change rebuilds.
+EXTRA_NVCC = os.environ.get("C2G_NVCC_EXTRA", "").split()
 
 
 def _nvcc() -> str:
@@ -48,6 +51,7 @@ def _sources_digest() -> str:
         h.update(fh.read())
     with open(__file__, "rb") as fh:
         h.update(fh.read())
+    h.update(" ".join(EXTRA_NVCC).encode())
     return h.hexdigest()
 
 
@@ -79,7 +83,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     def cuda(src: str) -> str:
         obj = os.path.join(BUILD, src.replace("/", "_") + ".o")
         cmd = [nvcc, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-               "-Xptxas", "-v" if verbose else "-O3", *inc, "-c", os.path.join(CSRC, src), "-o", obj]
+               "-Xptxas", "-v" if verbose else "-O3", *EXTRA_NVCC, *inc, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr[-8000:]}")

@@ -214,6 +214,16 @@ __global__ void k_raygen(DevScene S, WaveArgs a, PathRefs out, float4* out_L, in
     }
 }
 
+// Minimum resident blocks per SM of the dynamic-fetch traversal kernels (a register budget:
+// 65536 / (128 x blocks) registers per thread).  The traversal waits on dependent node loads, so
+// more resident warps hide more of that latency, until spills to local memory cost more.
+#ifndef C2G_EXTEND_MIN_BLOCKS
+#define C2G_EXTEND_MIN_BLOCKS 1
+#endif
+#ifndef C2G_SHADOW_MIN_BLOCKS
+#define C2G_SHADOW_MIN_BLOCKS 1
+#endif
+
 // ---- extend: closest hit of each queued path ray ------------------------------------------------
 // Per-kernel-kind traversal counters: cnt[3 * kind + {0: rays, 1: nodes, 2: prims}].
 __device__ __forceinline__ void flush_counts(unsigned long long* cnt, int kind, unsigned rays, const TraceCounters& tc) {
@@ -255,7 +265,7 @@ __global__ void k_extend(DevScene S, const float4* __restrict__ qo, const float4
 // is finished writes its hit, appends the slot to its material bucket (all lanes join the keyed
 // append of every round; idle lanes with no key) and takes the next ray.
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_extend_fetch(DevScene S, const float4* __restrict__ qo, const float4* __restrict__ qd,
+__global__ void __launch_bounds__(128, C2G_EXTEND_MIN_BLOCKS) k_extend_fetch(DevScene S, const float4* __restrict__ qo, const float4* __restrict__ qd,
                                                       float4* hit, const int* qcount, int* zero_a, int* zero_b, int* zero_c,
                                                       int* bucket_cnt, int* bucket_list, int cap, int* fetch,
                                                       unsigned long long* cnt) {
@@ -628,7 +638,7 @@ __global__ void k_shadow(DevScene S, const int* __restrict__ list, const int* co
 // slowest ray of its warp ends (persistent threads with ray replacement).  Same per-ray traversal
 // as trace_any_bvh4, so the same rays are occluded.
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_shadow_fetch(DevScene S, const int* __restrict__ list, const int* count,
+__global__ void __launch_bounds__(128, C2G_SHADOW_MIN_BLOCKS) k_shadow_fetch(DevScene S, const int* __restrict__ list, const int* count,
                                                       const float4* __restrict__ so, const float4* __restrict__ sd,
                                                       float4* sc, int* fetch, unsigned long long* cnt) {
     const int n = *count;

@@ -131,6 +131,32 @@ def test_trace_random_rays_match_oracle(accel, tmp_path):
         assert np.array_equal(gocc, oocc)
 
 
+@pytest.mark.parametrize("accel", ["BVH", "Brute"])
+def test_traversal_variants_agree(accel, tmp_path):
+    """The SAH tree's two node layouts, binary and four-wide, reach the same leaves' answers: any
+    hit identical, closest hit identical up to exact distance ties, and so the same image."""
+    cp, sp = scenes.material_box(str(tmp_path / accel), width=24, height=24, spp=2, accel=accel)
+    ctx = _ctx(cp, sp, N.TREE_SAH)
+    o, d = ray_set("material_box", 20000, 91)
+    res = {}
+    for w in (2, 4):
+        ctx.set_traversal(w)
+        obj, t = ctx.trace_rays(o, d)
+        tmin, tmax, ign = anyhit_inputs(obj, t, 20000, 91)
+        occ = ctx.trace_rays(o, d, any_hit=True, tmin=tmin, tmax=tmax, ignore=ign)
+        p = ctx.render_params()
+        ctx.film_clear()
+        ctx.render(p)
+        res[w] = (obj, t, occ, ctx.film()[0])
+    for w in (4,):
+        obj, t, occ, film = res[w]
+        assert (obj == res[2][0]).mean() >= 0.999
+        np.testing.assert_allclose(t[obj == res[2][0]], res[2][1][obj == res[2][0]], rtol=0, atol=0)
+        assert np.array_equal(occ, res[2][2])
+        close = np.isclose(film, res[2][3], rtol=1e-5, atol=1e-6)
+        assert close.mean() >= 0.999
+
+
 def test_axis_aligned_shadow_leak_is_reproduced(tmp_path):
     """The BVH shadow test hands the object-box-clipped interval to the triangle test
     (BVH.cpp:132-134): an axis-aligned wall blocks a shadow ray only when the matrix-inverse t
