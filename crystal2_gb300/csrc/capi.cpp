@@ -604,6 +604,14 @@ int c2g_guide_levels(c2g_ctx* ctx, int levels) {
     return C2G_OK;
 }
 
+int c2g_guide_batch(c2g_ctx* ctx, int records_per_wave, int windows) {
+    if (!ctx) return C2G_ERR_INVALID;
+    if (records_per_wave < 1024 || windows < 1 || windows > 64) return fail(ctx, C2G_ERR_INVALID, "invalid training batch");
+    if (ctx->host_only) return fail(ctx, C2G_ERR_STATE, "host-only context");
+    ctx->gpu->guide().set_batch(records_per_wave, windows);
+    return C2G_OK;
+}
+
 int c2g_guide_config(c2g_ctx* ctx, float learning_rate, float bsdf_fraction, int warmup_waves, int train_steps) {
     if (!ctx) return C2G_ERR_INVALID;
     if (!(learning_rate > 0.f) || !(bsdf_fraction > 0.f && bsdf_fraction <= 1.f) || warmup_waves < 0 || train_steps < 0)

@@ -21,23 +21,6 @@
 namespace c2g {
 
 namespace {
-
-// Shared-memory tile strides (elements): rows padded by 8 so that the eight row groups of an MMA
-// fragment load fall in distinct banks.
-constexpr int kLdA0 = 88;    // encoded inputs (80)
-constexpr int kLdH = 72;     // hidden activations / deltas (64)
-constexpr int kLdO = 56;     // output-layer gradient (48)
-constexpr int kLdOF = 52;    // FP32 outputs (training)
-
-// Padded weight copies in shared memory.  Forward: wt_l (N_l rows of K_l + 8).  Backward: wn_l
-// (K_l rows of N_l + 8), layers 1..3 (the input gradient of layer 0 is never needed).
-__host__ __device__ constexpr int fw_ld(int l) { return guide_k(l) + 8; }
-__host__ __device__ constexpr int fw_off(int l) { return l == 0 ? 0 : fw_off(l - 1) + guide_n(l - 1) * fw_ld(l - 1); }
-constexpr int kFwElems = fw_off(4);
-__host__ __device__ constexpr int bw_ld(int l) { return guide_n(l) + 8; }
-__host__ __device__ constexpr int bw_off(int l) { return l <= 1 ? 0 : bw_off(l - 1) + guide_k(l - 1) * bw_ld(l - 1); }
-constexpr int kBwElems = bw_off(4);
-
 __device__ __forceinline__ float luminance(float3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
 
 // Bucket ids whose hits are guided: the non-specular materials whose BSDF sampling routine returns
@@ -45,100 +28,6 @@ __device__ __forceinline__ float luminance(float3 c) { return 0.2126f * c.x + 0.
 __host__ __device__ constexpr bool bucket_guided(int b) {
     return b == MAT_DIFFUSE || b == MAT_MICRO_GGX || b == MAT_MICRO_BECKMANN || b == MAT_PLASTIC_GGX ||
            b == MAT_PLASTIC_BECKMANN || b == MAT_ORENNAYAR;
-}
-
-__device__ __forceinline__ void stage_forward_weights(const GuideNet& net, __nv_bfloat16* wts) {
-#pragma unroll
-    for (int l = 0; l < kGuideLayers; l++) {
-        const int K = guide_k(l), N = guide_n(l), vpr = K / 8;
-        const uint4* src = reinterpret_cast<const uint4*>(net.bf + guide_bf_off(l));
-        for (int i = threadIdx.x; i < N * vpr; i += blockDim.x) {
-            int n = i / vpr, c = i - n * vpr;
-            *reinterpret_cast<uint4*>(wts + fw_off(l) + n * fw_ld(l) + c * 8) = src[i];
-        }
-    }
-}
-
-__device__ __forceinline__ void stage_backward_weights(const GuideNet& net, __nv_bfloat16* wns) {
-#pragma unroll
-    for (int l = 1; l < kGuideLayers; l++) {
-        const int K = guide_k(l), N = guide_n(l), vpr = N / 8;
-        const uint4* src = reinterpret_cast<const uint4*>(net.bf + guide_bf_off(l) + K * N);
-        for (int i = threadIdx.x; i < K * vpr; i += blockDim.x) {
-            int k = i / vpr, c = i - k * vpr;
-            *reinterpret_cast<uint4*>(wns + bw_off(l) + k * bw_ld(l) + c * 8) = src[i];
-        }
-    }
-}
-
-__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
-
-// MT 16-row tiles through one layer: out[16 MT x N] = epilogue(in[16 MT x K] @ W + bias), W given
-// as w = N x K (row stride ldw).  A fragments are loaded once and reused across the N columns;
-// each B fragment serves all MT row tiles.  Epilogue: FP32 store to outf when non-null; else
-// optional ReLU, optional mask (value kept where mask > 0, the ReLU derivative) and a BF16 store.
-template <int MT, int K, int N>
-__device__ __forceinline__ void mma_rows(const __nv_bfloat16* in, int ldi, const __nv_bfloat16* w, int ldw,
-                                         const float* bias, __nv_bfloat16* out, int ldo, bool relu, float* outf, int ldf,
-                                         const __nv_bfloat16* mask, int ldm) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    uint32_t a[MT][K / 16][4];
-#pragma unroll
-    for (int m = 0; m < MT; m++)
-#pragma unroll
-        for (int kk = 0; kk < K / 16; kk++) {
-            const __nv_bfloat16* r0 = in + (m * 16 + g) * ldi + kk * 16 + 2 * t;
-            a[m][kk][0] = ld32(r0);
-            a[m][kk][1] = ld32(r0 + 8 * ldi);
-            a[m][kk][2] = ld32(r0 + 8);
-            a[m][kk][3] = ld32(r0 + 8 * ldi + 8);
-        }
-#pragma unroll
-    for (int n0 = 0; n0 < N; n0 += 8) {
-        float d[MT][4];
-        const float b0 = bias ? bias[n0 + 2 * t] : 0.f, b1 = bias ? bias[n0 + 2 * t + 1] : 0.f;
-#pragma unroll
-        for (int m = 0; m < MT; m++) { d[m][0] = b0; d[m][1] = b1; d[m][2] = b0; d[m][3] = b1; }
-#pragma unroll
-        for (int kk = 0; kk < K / 16; kk++) {
-            uint32_t b[2];
-            const __nv_bfloat16* wr = w + (n0 + g) * ldw + kk * 16 + 2 * t;
-            b[0] = ld32(wr);
-            b[1] = ld32(wr + 8);
-#pragma unroll
-            for (int m = 0; m < MT; m++) mma16816(d[m], a[m][kk], b);
-        }
-#pragma unroll
-        for (int m = 0; m < MT; m++) {
-            const int r0 = m * 16 + g, r1 = r0 + 8, c = n0 + 2 * t;
-            if (outf) {
-                outf[r0 * ldf + c] = d[m][0];
-                outf[r0 * ldf + c + 1] = d[m][1];
-                outf[r1 * ldf + c] = d[m][2];
-                outf[r1 * ldf + c + 1] = d[m][3];
-                continue;
-            }
-            if (relu) {
-#pragma unroll
-                for (int q = 0; q < 4; q++) d[m][q] = fmaxf(d[m][q], 0.f);
-            }
-            if (mask) {
-                __nv_bfloat162 k0 = *reinterpret_cast<const __nv_bfloat162*>(mask + r0 * ldm + c);
-                __nv_bfloat162 k1 = *reinterpret_cast<const __nv_bfloat162*>(mask + r1 * ldm + c);
-                if (!(__low2float(k0) > 0.f)) d[m][0] = 0.f;
-                if (!(__high2float(k0) > 0.f)) d[m][1] = 0.f;
-                if (!(__low2float(k1) > 0.f)) d[m][2] = 0.f;
-                if (!(__high2float(k1) > 0.f)) d[m][3] = 0.f;
-            }
-            *reinterpret_cast<uint32_t*>(out + r0 * ldo + c) = pack_bf16(d[m][0], d[m][1]);
-            *reinterpret_cast<uint32_t*>(out + r1 * ldo + c) = pack_bf16(d[m][2], d[m][3]);
-        }
-    }
-}
-
-__device__ __forceinline__ void store_inputs(__nv_bfloat16* row, const float* in) {
-#pragma unroll
-    for (int k = 0; k < kGuideIn; k += 2) *reinterpret_cast<uint32_t*>(row + k) = pack_bf16(in[k], in[k + 1]);
 }
 
 // ---- inference on the fifth-generation tensor cores (tcgen05) -----------------------------------
@@ -188,8 +77,12 @@ __device__ __forceinline__ void tc_store8(unsigned char* base, int r, int k0, in
     *reinterpret_cast<uint4*>(base + tc_cm(r, k0, K)) = q;
 }
 
-// guide_encode written straight into row r of a K = 80 operand tile, eight values at a time (the
-// same arithmetic in the same order, with eight values live instead of eighty).
+// The encoded inputs of one vertex straight into row r of a W-wide operand tile (columns 0..79),
+// eight values at a time: position p in the scene box as sin/cos(pi 2^f p), f = 0..11 per axis
+// (one exactly reduced sincospif, then the double-angle recurrence sin 2u = 2 sin u cos u,
+// cos 2u = (cos u - sin u)(cos u + sin u), whose absolute error grows about 2x per octave: ~1e-4 at
+// 2^11, far below BF16 resolution), the shading normal, the outgoing direction, two zeros.
+template <int W = kGuideIn>
 __device__ __forceinline__ void tc_encode_row(const GuideNet& g, float3 x, float3 n, float3 wo, unsigned char* base, int r) {
     const float p[3] = {(x.x - g.box_lo[0]) * g.box_inv[0], (x.y - g.box_lo[1]) * g.box_inv[1], (x.z - g.box_lo[2]) * g.box_inv[2]};
     float chunk[8];
@@ -204,7 +97,7 @@ __device__ __forceinline__ void tc_encode_row(const GuideNet& g, float3 x, float
             chunk[fill++] = s;
             chunk[fill++] = c;
             if (fill == 8) {
-                tc_store8(base, r, col, kGuideIn, chunk);
+                tc_store8(base, r, col, W, chunk);
                 col += 8;
                 fill = 0;
             }
@@ -214,7 +107,7 @@ __device__ __forceinline__ void tc_encode_row(const GuideNet& g, float3 x, float
         }
     }
     const float tail[8] = {n.x, n.y, n.z, wo.x, wo.y, wo.z, 0.f, 0.f};
-    tc_store8(base, r, 72, kGuideIn, tail);
+    tc_store8(base, r, 72, W, tail);
 }
 
 // Work list of the guided buckets back to back: item -> queue slot.
@@ -450,55 +343,69 @@ __global__ void k_guide_batch(float4* rec, int rec_cap, int rec_depth, int rec_s
     }
 }
 
-// ---- fused training step ------------------------------------------------------------------------
-// 256 threads = 8 warps; a block takes 128 samples per iteration, 16 per warp.  Each warp runs the
-// forward and backward passes of its samples on tensor-core tiles (weights staged in shared memory,
-// activations and deltas kept as BF16 tiles).  The weight gradients dW_l = A_l^T D_l are then
-// tensor-core products over the block's 128 samples: the 124 (16 x 8) output tiles of the four
-// layers are split over the warps, each accumulating its tiles in FP32 registers for the whole
-// sweep (A^T and D fragments come from ldmatrix.trans); they reach global memory once per block.
-constexpr int kTrainWarps = 8;
-// A wave's batch is split into at most this many minibatch windows, taken in turn by its Adam
-// steps: smaller windows made the mixture collapse onto a few sharp lobes in some runs.
-constexpr int kTrainWindows = 4;
-constexpr int kTrainRows = 16;
-// per-warp tile offsets (elements)
-constexpr int kTA0 = 0;
-constexpr int kTH1 = kTA0 + kTrainRows * kLdA0;
-constexpr int kTH2 = kTH1 + kTrainRows * kLdH;
-constexpr int kTH3 = kTH2 + kTrainRows * kLdH;
-constexpr int kTD1 = kTH3 + kTrainRows * kLdH;
-constexpr int kTD2 = kTD1 + kTrainRows * kLdH;
-constexpr int kTD3 = kTD2 + kTrainRows * kLdH;
-constexpr int kTDO = kTD3 + kTrainRows * kLdH;
-constexpr int kTWarpElems = kTDO + kTrainRows * kLdO;
-static_assert(kTrainRows * kLdOF * 4 <= 2 * kTrainRows * kLdH * 2, "FP32 outputs alias the d1/d2 tiles");
-constexpr size_t kTrainSmem = (size_t)(kFwElems + kBwElems + kTrainWarps * kTWarpElems) * 2;
-// dW tiles: layer 0 5 x 8, layers 1-2 4 x 8, layer 3 4 x 6 (outputs 40..47: selection + padding)
-constexpr int kDwTiles = 40 + 32 + 32 + 24;
-constexpr int kDwPerWarp = (kDwTiles + kTrainWarps - 1) / kTrainWarps;
+// ---- fused training step on the fifth-generation tensor cores (tcgen05) -------------------------
+// One CTA per SM with two warpgroups, each working through its own 128-sample tiles; thread r of a
+// warpgroup owns row r of its tiles.  Per tile:
+//  * the thread encodes its sample into the input tile (BF16, the inference kernel's K-major core
+//    layout);
+//  * four forward layers: one thread issues tcgen05.mma (M = 128, BF16 operands from shared-memory
+//    descriptors) into a 64-column tensor-memory scratch and commits to the warpgroup's mbarrier;
+//    every thread reads its row back (tcgen05.ld), adds the bias, applies ReLU and writes the next
+//    activation tile;
+//  * the loss gradient at the 41 outputs, one row per thread, stored as the output-delta tile;
+//  * per layer j = 3, 2, 1 one commit group with the input gradient G = delta_j W_j^T (A: the delta
+//    tile; B: the forward weight copy read MN-major) and the weight gradient
+//    dW_j += [a_j | 1]^T delta_j over the tile's 128 samples (both operands read MN-major from the
+//    activation and delta tiles, so no transposed copies are written); then delta_{j-1} =
+//    G * relu'(a_j) replaces a_j in place (the MMA that read a_j has completed);
+//  * dW_0 = [a_0 | 1]^T delta_0 into the scratch, added row by row (81 rows) into the warpgroup's
+//    partial gradient in global memory (a region only this warpgroup touches).
+// Every activation tile carries a constant-one column behind its features, so row K_j of dW_j is
+// the bias gradient.  dW_1..dW_3 accumulate in tensor memory over all tiles of the launch.  Each
+// warpgroup finally writes its partial gradient of every parameter; k_guide_adam sums them.
+// MN-major operands (no swizzle) are 8 K-rows x 16-byte (8 element) core matrices; the descriptor's
+// SBO is the byte stride between 8-element groups along M or N, its LBO the stride between 8-row
+// groups along K.  An M = 128 weight-gradient operand covers 128 features of a narrower tile: rows
+// past the tile's features read other rows' values (finite BF16 numbers inside the allocation) and
+// land in tensor-memory rows that are never read.
+constexpr int kTgGroups = 2;                             // warpgroups per CTA
+constexpr int kTgThreads = 128 * kTgGroups;
+constexpr int kTgW0 = kGuideIn + 8;                      // input tile: 80 encoded inputs, the one column
+constexpr int kTgWH = kGuideHidden + 8;                  // hidden tiles: 64 activations, the one column
+constexpr int kTgWO = kGuideOutPad;                      // output-delta tile
+constexpr int kTgA0 = 128 * kTgW0 * 2;
+constexpr int kTgH = 128 * kTgWH * 2;
+constexpr int kTgD = 128 * kTgWO * 2;
+constexpr int kTgGroupBytes = kTgA0 + 3 * kTgH + kTgD;
+// weights sit behind both warpgroups' tiles, so every operand read stays inside the allocation
+constexpr int kTgWts = kTgGroups * kTgGroupBytes;
+constexpr int kTgBias = kTgWts + tc_w_off(4);
+constexpr int kTgBar = kTgBias + kTcBiasN * 4;
+constexpr int kTgSlot = kTgBar + 8 * kTgGroups;
+// Slack behind the last buffer: the MN-major weight operand of G = delta_3 W_3^T would reach up to
+// 5.4 KB past the weights if the descriptor's two strides were read the other way round, and the
+// allocation covers that reach too.
+constexpr int kTgSlack = 8192;
+constexpr size_t kTgSmem = (size_t)kTgSlot + 8 + kTgSlack;
+constexpr uint32_t kTgColsPerGroup = 256;                // scratch 64 | dW_1 64 | dW_2 64 | dW_3 48
+constexpr uint32_t kTgCols = kTgColsPerGroup * kTgGroups;
+static_assert(kTgA0 % 128 == 0 && kTgH % 128 == 0 && kTgD % 128 == 0 && kTgWts % 128 == 0 && kTgBar % 8 == 0,
+              "operand and barrier alignment");
+static_assert(kTgSmem <= 232448, "training tiles fit one CTA's shared memory");
+static_assert(64 + 2 * kGuideHidden + kGuideOutPad <= (int)kTgColsPerGroup, "tensor-memory columns per warpgroup");
 
-__device__ __forceinline__ void ldsm_x4_trans(uint32_t* r, const void* p) {
-    uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+// Instruction descriptor with the A and / or B operand read MN-major.
+__host__ __device__ constexpr uint32_t umma_idesc_mn(int N, bool a_mn, bool b_mn) {
+    return umma_idesc_bf16(128, N) | (a_mn ? 1u << 15 : 0u) | (b_mn ? 1u << 16 : 0u);
 }
-__device__ __forceinline__ void ldsm_x2_trans(uint32_t* r, const void* p) {
-    uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n" : "=r"(r[0]), "=r"(r[1]) : "r"(a));
-}
-
-__device__ __forceinline__ void dw_tile(int idx, int& l, int& mt, int& nt) {
-    if (idx < 40) { l = 0; mt = idx >> 3; nt = idx & 7; }
-    else if (idx < 72) { l = 1; mt = (idx - 40) >> 3; nt = (idx - 40) & 7; }
-    else if (idx < 104) { l = 2; mt = (idx - 72) >> 3; nt = (idx - 72) & 7; }
-    else { l = 3; mt = (idx - 104) / 6; nt = (idx - 104) % 6; }
-}
+static_assert(umma_idesc_mn(64, true, true) == (umma_idesc_bf16(128, 64) | (3u << 15)), "transpose bits");
 
 // Gradient of w * -log q_mix(wi), q_mix = (1 - c) p_bsdf + c q_guide, with respect to the 41 raw
-// outputs o (see the oracle for the formulas); returns -log q_mix.  g[41..47] (padding) are left
-// to the caller.
-__device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, float w, float pb, float* g) {
+// outputs o (see the oracle for the formulas), each handed to put(k, g_k) as soon as it is known
+// (clamped to [-1e3, 1e3], a non-finite value as 0); returns -log q_mix.
+template <class Put>
+__device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, float w, float pb, Put put) {
+    auto clamped = [](float v) { return isfinite(v) ? fminf(fmaxf(v, -1e3f), 1e3f) : 0.f; };
     Lobe L[kGuideLobes];
     guide_lobes(o, L);
     float p[kGuideLobes], q = 0.f;
@@ -526,176 +433,291 @@ __device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, floa
         const float3 m = f3(o[5 * k], o[5 * k + 1], o[5 * k + 2]);
         const float len = fmaxf(sqrtf(dot(m, m)), 1e-12f);
         const float3 dm = (wi - L[k].mu * c) * (kap / len);
-        g[5 * k + 0] = -w * rho * r * dm.x;
-        g[5 * k + 1] = -w * rho * r * dm.y;
-        g[5 * k + 2] = -w * rho * r * dm.z;
-        g[5 * k + 3] = -w * rho * r * dk * sig;
-        g[5 * k + 4] = -w * rho * (r - L[k].w);
+        put(5 * k + 0, clamped(-w * rho * r * dm.x));
+        put(5 * k + 1, clamped(-w * rho * r * dm.y));
+        put(5 * k + 2, clamped(-w * rho * r * dm.z));
+        put(5 * k + 3, clamped(-w * rho * r * dk * sig));
+        put(5 * k + 4, clamped(-w * rho * (r - L[k].w)));
     }
-    g[40] = -w * (q - pb) * kGuideSelSpan * sg * (1.f - sg) / qmix;
-#pragma unroll
-    for (int k = 0; k < kGuideOut; k++) {
-        const float v = g[k];
-        g[k] = isfinite(v) ? fminf(fmaxf(v, -1e3f), 1e3f) : 0.f;
-    }
+    put(40, clamped(-w * (q - pb) * kGuideSelSpan * sg * (1.f - sg) / qmix));
     return -__logf(qmix);
 }
 
-__global__ void __launch_bounds__(256, 1) k_guide_train(GuideNet net, const float4* __restrict__ batch, const int* batch_count,
-                                                        int batch_cap, float* grad, float* stats, int splits,
-                                                        const int* __restrict__ step) {
+__global__ void __launch_bounds__(kTgThreads, 1) k_guide_train_tc(GuideNet net, const float4* __restrict__ batch,
+                                                                 const int* batch_count, int batch_cap, float* part,
+                                                                 float* stats, int splits, const int* __restrict__ step,
+                                                                 int* err) {
     extern __shared__ __align__(128) unsigned char smem[];
-    __nv_bfloat16* wts = reinterpret_cast<__nv_bfloat16*>(smem);
-    __nv_bfloat16* wns = wts + kFwElems;
-    __nv_bfloat16* tiles = wns + kBwElems;
-    stage_forward_weights(net, wts);
-    stage_backward_weights(net, wns);
+    const int grp = threadIdx.x >> 7, row = threadIdx.x & 127, warp = threadIdx.x >> 5;
+    unsigned char* const A0 = smem + grp * kTgGroupBytes;
+    unsigned char* const H1 = A0 + kTgA0;
+    unsigned char* const H2 = H1 + kTgH;
+    unsigned char* const H3 = H2 + kTgH;
+    unsigned char* const DO = H3 + kTgH;
+    unsigned char* const WT = smem + kTgWts;
+    float* bias = reinterpret_cast<float*>(smem + kTgBias);
+    const uint32_t bar = smem_u32(smem + kTgBar + 8 * grp);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kTgSlot);
+    // forward weights in the K-major core layout (as inference), biases
+#pragma unroll
+    for (int l = 0; l < kGuideLayers; l++) {
+        const int K = guide_k(l), N = guide_n(l), vpr = K / 8;
+        const uint4* src = reinterpret_cast<const uint4*>(net.bf + guide_bf_off(l));
+        for (int i = threadIdx.x; i < N * vpr; i += kTgThreads) {
+            const int nn = i / vpr, c = i - nn * vpr;
+            *reinterpret_cast<uint4*>(WT + tc_w_off(l) + tc_cm(nn, 8 * c, K)) = src[i];
+        }
+    }
+    for (int i = threadIdx.x; i < kTcBiasN; i += kTgThreads) {
+        const int l = i < 3 * kGuideHidden ? i / kGuideHidden : 3;
+        bias[i] = net.params[guide_b_off(l) + (i - l * kGuideHidden)];
+    }
+    // the constant-one columns (then seven zeros) of this thread's rows and the padding outputs of
+    // its delta row; the epilogues never write them
+    {
+        const float one[8] = {1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        tc_store8(A0, row, kGuideIn, kTgW0, one);
+        tc_store8(H1, row, kGuideHidden, kTgWH, one);
+        tc_store8(H2, row, kGuideHidden, kTgWH, one);
+        tc_store8(H3, row, kGuideHidden, kTgWH, one);
+        tc_store8(DO, row, kGuideOutPad - 8, kTgWO, z);
+    }
+    if (threadIdx.x == 0) {
+        for (int g = 0; g < kTgGroups; g++) mbar_init(smem_u32(smem + kTgBar + 8 * g), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) tmem_alloc(smem_u32(tslot), kTgCols);
+    fence_async_smem();
+    tc_fence_before();
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __nv_bfloat16* T = tiles + warp * kTWarpElems;
-    float* OF = reinterpret_cast<float*>(T + kTD1);
+    tc_fence_after();
+    const uint32_t tS = *tslot + grp * kTgColsPerGroup;            // scratch (lane 0, column base)
+    const uint32_t tW1 = tS + 64, tW2 = tS + 128, tW3 = tS + 192;   // weight-gradient accumulators
+    const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;    // this warp's 32 lanes
+    const int bar_id = 1 + grp;
+
     const int n = min(*batch_count, batch_cap);
     const float mean_w = stats[2] / fmaxf(1.f, (float)n);
-    // minibatch of this Adam step: the batch split into `splits` windows, taken in turn, so the
-    // steps of one wave pass over the batch once
+    // minibatch of this Adam step: the batch split into `splits` windows, taken in turn
     const int per = (n + splits - 1) / splits;
     const int lo = min(n, (*step % splits) * per), hi = min(n, lo + per);
+    const int tiles = (hi - lo + 127) / 128;
 
-    float acc[kDwPerWarp][4];
-#pragma unroll
-    for (int q = 0; q < kDwPerWarp; q++) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
-    // bias gradients: thread -> one of the 64 + 64 + 64 + 40 bias columns
-    float bacc = 0.f;
-    int bl = -1, bc = 0;
-    if (threadIdx.x < 192) { bl = threadIdx.x >> 6; bc = threadIdx.x & 63; }
-    else if (threadIdx.x < 192 + kGuideOut) { bl = 3; bc = threadIdx.x - 192; }
     float loss = 0.f, wsum = 0.f;
+    float* P = part + (size_t)(blockIdx.x * kTgGroups + grp) * kGuideParams;
+    // row K_0 of dW_0 is the bias gradient b_0
+    float* dw0_row = row < kGuideIn ? P + guide_w_off(0) + row * kGuideHidden : P + guide_b_off(0);
+    uint32_t ph = 0;
+    bool failed = false, pending = false, have = false;
 
-    const int chunk = kTrainWarps * kTrainRows;
-    for (int base = lo + blockIdx.x * chunk; base < hi; base += gridDim.x * chunk) {
-        const int s = lane & 15;
-        const int j = base + warp * kTrainRows + s;
+    // Make this warpgroup's shared-memory writes visible to the tensor core, let one thread issue
+    // `mma` and commit it, and wait (bounded) for completion.  Returns false once a wait timed out.
+    auto run = [&](auto&& mma) -> bool {
+        fence_async_smem();
+        tc_fence_before();
+        if (wg_sync_or(bar_id, failed)) { failed = true; return false; }
+        if (row == 0) {
+            tc_fence_after();
+            mma();
+            umma_commit(bar);
+        }
+        pending = true;
+        const bool ok = mbar_wait(bar, ph, kTcWaitPolls);
+        if (ok) { ph ^= 1u; pending = false; }
+        if (wg_sync_or(bar_id, !ok)) { failed = true; return false; }
+        tc_fence_after();
+        return true;
+    };
+    // forward layer l: scratch = a_l W_l (a_l: W-wide tile, K-major; W_l: K-major)
+    auto fwd = [&](int l, const unsigned char* a, int W) {
+        const int K = guide_k(l), N = guide_n(l);
+        const uint32_t a0 = smem_u32(a), b0 = smem_u32(WT + tc_w_off(l));
+        for (int kk = 0; kk < K / 16; kk++)
+            umma_bf16(tS, umma_desc(a0 + kk * 256, 128, 16 * W), umma_desc(b0 + kk * 256, 128, 16 * K),
+                      umma_idesc_bf16(128, N), kk > 0);
+    };
+    // input gradient of layer j: scratch = delta_j W_j^T (K = layer j's outputs, N = its 64 inputs)
+    auto grad_in = [&](int j, const unsigned char* d, int W) {
+        const int K = guide_n(j), N = guide_k(j);
+        const uint32_t a0 = smem_u32(d), b0 = smem_u32(WT + tc_w_off(j));
+        for (int kk = 0; kk < K / 16; kk++)
+            umma_bf16(tS, umma_desc(a0 + kk * 256, 128, 16 * W), umma_desc(b0 + kk * 32 * N, 16 * N, 128),
+                      umma_idesc_mn(N, false, true), kk > 0);
+    };
+    // weight gradient of layer j: D (+)= [a_j | 1]^T delta_j over the tile's 128 samples
+    auto grad_w = [&](int j, uint32_t dst, const unsigned char* a, int Wa, const unsigned char* d, int Wd, bool acc) {
+        const uint32_t a0 = smem_u32(a), b0 = smem_u32(d);
+        for (int kk = 0; kk < 8; kk++)
+            umma_bf16(dst, umma_desc(a0 + kk * 32 * Wa, 16 * Wa, 128), umma_desc(b0 + kk * 32 * Wd, 16 * Wd, 128),
+                      umma_idesc_mn(guide_n(j), true, true), acc || kk > 0);
+    };
+    // delta_{j-1} = G * relu'(a_j), written over a_j (this thread's row)
+    auto delta = [&](unsigned char* a) {
+#pragma unroll
+        for (int c = 0; c < kGuideHidden; c += 32) {
+            uint32_t r[32];
+            tmem_ld16(tS + lane_off + c, r);
+            tmem_ld16(tS + lane_off + c + 16, r + 16);
+            tmem_wait();
+#pragma unroll
+            for (int q = 0; q < 32; q += 8) {
+                const uint4 hv = *reinterpret_cast<const uint4*>(a + tc_cm(row, c + q, kTgWH));
+                const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&hv);
+                float v[8];
+#pragma unroll
+                for (int e = 0; e < 8; e++) v[e] = __bfloat162float(h[e]) > 0.f ? __uint_as_float(r[q + e]) : 0.f;
+                tc_store8(a, row, c + q, kTgWH, v);
+            }
+        }
+    };
+
+    for (int t = blockIdx.x * kTgGroups + grp; t < tiles && !failed; t += gridDim.x * kTgGroups) {
+        const int j = lo + t * 128 + row;
         const bool valid = j < hi;
         float3 wi = f3(0.f, 0.f, 1.f);
         float w = 0.f, pb = 0.f;
-        if (lane < 16) {
-            float in[kGuideIn];
-            if (valid) {
-                const float4 b0 = batch[4 * j], b1 = batch[4 * j + 1], b2 = batch[4 * j + 2], b3 = batch[4 * j + 3];
-                guide_encode(net, f3(b0), f3(b1), f3(b2), in);
-                wi = f3(b3);
-                pb = b3.w;
-                w = fminf(b0.w / fmaxf(mean_w, 1e-12f), 20.f);  // normalised, firefly-clamped weight
-            } else {
+        if (valid) {
+            const float4 b0 = batch[4 * j], b1 = batch[4 * j + 1], b2 = batch[4 * j + 2], b3 = batch[4 * j + 3];
+            tc_encode_row<kTgW0>(net, f3(b0), f3(b1), f3(b2), A0, row);
+            wi = f3(b3);
+            pb = b3.w;
+            w = fminf(b0.w / fmaxf(mean_w, 1e-12f), 20.f);  // normalised, firefly-clamped weight
+        } else {
+            const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-                for (int k = 0; k < kGuideIn; k++) in[k] = 0.f;
-            }
-            store_inputs(T + kTA0 + s * kLdA0, in);
+            for (int k = 0; k < kGuideIn; k += 8) tc_store8(A0, row, k, kTgW0, z);
         }
-        __syncwarp();
-        mma_rows<1, 80, 64>(T + kTA0, kLdA0, wts + fw_off(0), fw_ld(0), net.params + guide_b_off(0), T + kTH1, kLdH, true, nullptr, 0, nullptr, 0);
-        __syncwarp();
-        mma_rows<1, 64, 64>(T + kTH1, kLdH, wts + fw_off(1), fw_ld(1), net.params + guide_b_off(1), T + kTH2, kLdH, true, nullptr, 0, nullptr, 0);
-        __syncwarp();
-        mma_rows<1, 64, 64>(T + kTH2, kLdH, wts + fw_off(2), fw_ld(2), net.params + guide_b_off(2), T + kTH3, kLdH, true, nullptr, 0, nullptr, 0);
-        __syncwarp();
-        mma_rows<1, 64, 48>(T + kTH3, kLdH, wts + fw_off(3), fw_ld(3), net.params + guide_b_off(3), nullptr, 0, false, OF, kLdOF, nullptr, 0);
-        __syncwarp();
-        // loss gradient at the outputs: one lane per sample
-        float g[kGuideOutPad];
+        // ---- forward
+        float o[kGuideOutPad];
+        unsigned char* act[4] = {A0, H1, H2, H3};
 #pragma unroll
-        for (int k = 0; k < kGuideOutPad; k++) g[k] = 0.f;
-        if (lane < 16 && valid && w > 0.f) {
-            float o[kGuideOut];
+        for (int l = 0; l < kGuideLayers; l++) {
+            if (!run([&] { fwd(l, act[l], l == 0 ? kTgW0 : kTgWH); })) break;
+            if (l < kGuideLayers - 1) {
 #pragma unroll
-            for (int k = 0; k < kGuideOut; k++) o[k] = OF[s * kLdOF + k];
-            loss += w * nll_output_grad(o, wi, w, pb, g);
-            wsum += w;
-        }
-        __syncwarp();  // OF (aliasing d1/d2) fully read before the deltas are written
-        if (lane < 16) {
+                for (int c = 0; c < kGuideHidden; c += 32) {
+                    uint32_t r[32];
+                    tmem_ld16(tS + lane_off + c, r);
+                    tmem_ld16(tS + lane_off + c + 16, r + 16);
+                    tmem_wait();
 #pragma unroll
-            for (int k = 0; k < kGuideOutPad; k += 2) *reinterpret_cast<uint32_t*>(T + kTDO + s * kLdO + k) = pack_bf16(g[k], g[k + 1]);
-        }
-        __syncwarp();
-        // backward: d_l = (d_{l+1} @ W_{l+1}^T) masked by relu'(h)
-        mma_rows<1, 48, 64>(T + kTDO, kLdO, wns + bw_off(3), bw_ld(3), nullptr, T + kTD3, kLdH, false, nullptr, 0, T + kTH3, kLdH);
-        __syncwarp();
-        mma_rows<1, 64, 64>(T + kTD3, kLdH, wns + bw_off(2), bw_ld(2), nullptr, T + kTD2, kLdH, false, nullptr, 0, T + kTH2, kLdH);
-        __syncwarp();
-        mma_rows<1, 64, 64>(T + kTD2, kLdH, wns + bw_off(1), bw_ld(1), nullptr, T + kTD1, kLdH, false, nullptr, 0, T + kTH1, kLdH);
-        __syncthreads();
-        // weight gradients over the block's 128 samples
-        {
-            const int jm = lane >> 3, qr = lane & 7;
+                    for (int q = 0; q < 32; q += 8) {
+                        float v[8];
 #pragma unroll
-            for (int q = 0; q < kDwPerWarp; q++) {
-                const int idx = warp + kTrainWarps * q;
-                if (idx < kDwTiles) {
-                    int l, mt, nt;
-                    dw_tile(idx, l, mt, nt);
-                    const int ain = l == 0 ? kTA0 : (l == 1 ? kTH1 : (l == 2 ? kTH2 : kTH3));
-                    const int lda = l == 0 ? kLdA0 : kLdH;
-                    const int dlt = l == 0 ? kTD1 : (l == 1 ? kTD2 : (l == 2 ? kTD3 : kTDO));
-                    const int ldd = l == 3 ? kLdO : kLdH;
-                    const int arow = qr + (jm >> 1) * 8, acol = mt * 16 + (jm & 1) * 8;
-                    const int brow = qr + (jm & 1) * 8, bcol = nt * 8;
-#pragma unroll
-                    for (int wv = 0; wv < kTrainWarps; wv++) {
-                        const __nv_bfloat16* Tw = tiles + wv * kTWarpElems;
-                        uint32_t a[4], b[2];
-                        ldsm_x4_trans(a, Tw + ain + arow * lda + acol);
-                        ldsm_x2_trans(b, Tw + dlt + brow * ldd + bcol);
-                        mma16816(acc[q], a, b);
+                        for (int e = 0; e < 8; e++) v[e] = fmaxf(__uint_as_float(r[q + e]) + bias[l * kGuideHidden + c + q + e], 0.f);
+                        tc_store8(act[l + 1], row, c + q, kTgWH, v);
                     }
+                }
+            } else {
+                uint32_t r[kGuideOutPad];
+#pragma unroll
+                for (int c = 0; c < kGuideOutPad; c += 16) tmem_ld16(tS + lane_off + c, r + c);
+                tmem_wait();
+#pragma unroll
+                for (int k = 0; k < kGuideOutPad; k++) o[k] = __uint_as_float(r[k]) + bias[3 * kGuideHidden + k];
+            }
+        }
+        if (failed) break;
+        // ---- loss gradient at the outputs (BF16, straight into this row of the delta tile; its
+        // padding columns 41..47 stay zero)
+        if (valid && w > 0.f) {
+            loss += w * nll_output_grad(o, wi, w, pb, [&](int k, float v) {
+                *reinterpret_cast<__nv_bfloat16*>(DO + tc_cm(row, k, kTgWO)) = __float2bfloat16_rn(v);
+            });
+            wsum += w;
+        } else {
+            const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int k = 0; k < kGuideOutPad; k += 8) tc_store8(DO, row, k, kTgWO, z);
+        }
+        // ---- backward
+        if (!run([&] { grad_in(3, DO, kTgWO); grad_w(3, tW3, H3, kTgWH, DO, kTgWO, have); })) break;
+        delta(H3);
+        if (!run([&] { grad_in(2, H3, kTgWH); grad_w(2, tW2, H2, kTgWH, H3, kTgWH, have); })) break;
+        delta(H2);
+        if (!run([&] { grad_in(1, H2, kTgWH); grad_w(1, tW1, H1, kTgWH, H2, kTgWH, have); })) break;
+        delta(H1);
+        if (!run([&] { grad_w(0, tS, A0, kTgW0, H1, kTgWH, false); })) break;
+#pragma unroll
+        for (int c = 0; c < kGuideHidden; c += 32) {
+            uint32_t r[32];
+            tmem_ld16(tS + lane_off + c, r);
+            tmem_ld16(tS + lane_off + c + 16, r + 16);
+            tmem_wait();
+            if (row <= kGuideIn) {
+                float4* d4 = reinterpret_cast<float4*>(dw0_row + c);
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    float4 v = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]), __uint_as_float(r[4 * q + 2]),
+                                           __uint_as_float(r[4 * q + 3]));
+                    if (have) {
+                        const float4 u = d4[q];
+                        v.x += u.x; v.y += u.y; v.z += u.z; v.w += u.w;
+                    }
+                    d4[q] = v;
                 }
             }
         }
-        if (bl >= 0) {
-            const int dlt = bl == 0 ? kTD1 : (bl == 1 ? kTD2 : (bl == 2 ? kTD3 : kTDO));
-            const int ldd = bl == 3 ? kLdO : kLdH;
-            for (int wv = 0; wv < kTrainWarps; wv++) {
-                const __nv_bfloat16* D = tiles + wv * kTWarpElems + dlt;
+        have = true;
+    }
+    if (failed) {
+        if (row == 0) dev_flag_error(err, DEVERR_WAIT);
+        if (pending) mbar_wait(bar, ph, kTcWaitPolls);  // the MMAs still in flight finish (bounded)
+    }
+    // ---- this warpgroup's partial gradient: rows 0..K-1 of dW_l are weights, row K the bias
+    tc_fence_before();
+    wg_sync(bar_id);
+    tc_fence_after();
+    const bool use = have && !failed;
+    if (!use && row <= kGuideIn) {
 #pragma unroll
-                for (int r = 0; r < kTrainRows; r++) bacc += __bfloat162float(D[r * ldd + bc]);
+        for (int k = 0; k < kGuideHidden; k++) dw0_row[k] = 0.f;
+    }
+    const uint32_t tW[4] = {0u, tW1, tW2, tW3};
+    for (int l = 1; l < kGuideLayers; l++) {
+        const int N = guide_n(l);
+        float* dst = row < kGuideHidden ? P + guide_w_off(l) + row * N : P + guide_b_off(l);
+        for (int c = 0; c < N; c += 16) {
+            uint32_t r[16];
+            if (use) {
+                tmem_ld16(tW[l] + lane_off + c, r);
+                tmem_wait();
+            } else {
+#pragma unroll
+                for (int k = 0; k < 16; k++) r[k] = 0u;
+            }
+            if (row <= kGuideHidden) {
+                float4* d4 = reinterpret_cast<float4*>(dst + c);
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    d4[k] = make_float4(__uint_as_float(r[4 * k]), __uint_as_float(r[4 * k + 1]), __uint_as_float(r[4 * k + 2]),
+                                        __uint_as_float(r[4 * k + 3]));
             }
         }
-        __syncthreads();
     }
-    // flush: dW_l[k][n] with k = mt*16 + g (+8), n = nt*8 + 2t (+1)
-    {
-        const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-        for (int q = 0; q < kDwPerWarp; q++) {
-            const int idx = warp + kTrainWarps * q;
-            if (idx < kDwTiles) {
-                int l, mt, nt;
-                dw_tile(idx, l, mt, nt);
-                const int N = guide_n(l);
-                float* G = grad + guide_w_off(l);
-                const int k0 = mt * 16 + g, c = nt * 8 + 2 * t;
-                if (acc[q][0] != 0.f) atomicAdd(G + k0 * N + c, acc[q][0]);
-                if (acc[q][1] != 0.f) atomicAdd(G + k0 * N + c + 1, acc[q][1]);
-                if (acc[q][2] != 0.f) atomicAdd(G + (k0 + 8) * N + c, acc[q][2]);
-                if (acc[q][3] != 0.f) atomicAdd(G + (k0 + 8) * N + c + 1, acc[q][3]);
-            }
-        }
+    for (int s = 16; s > 0; s >>= 1) {
+        loss += __shfl_down_sync(0xffffffffu, loss, s);
+        wsum += __shfl_down_sync(0xffffffffu, wsum, s);
     }
-    if (bl >= 0 && bacc != 0.f) atomicAdd(grad + guide_b_off(bl) + bc, bacc);
-    for (int o = 16; o > 0; o >>= 1) {
-        loss += __shfl_down_sync(0xffffffffu, loss, o);
-        wsum += __shfl_down_sync(0xffffffffu, wsum, o);
-    }
-    if (lane == 0 && wsum != 0.f) {
+    if ((threadIdx.x & 31) == 0 && wsum != 0.f) {
         atomicAdd(stats + 0, loss);
         atomicAdd(stats + 1, wsum);
     }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_free(*tslot, kTgCols);
+    }
 }
 
-// Adam on the FP32 master weights (gradients normalised by the batch weight sum), then the two
-// BF16 layouts the kernels read.  The padded output columns stay zero.
-__global__ void k_guide_adam(float* params, float* grad, float* m, float* v, __nv_bfloat16* bfw, const float* stats,
-                             float lr, float b1, float b2, float eps, const int* step) {
+// Adam on the FP32 master weights: the gradient is the sum of the training kernel's per-warpgroup
+// partials, normalised by the batch weight sum; then the two BF16 layouts the kernels read.  The
+// padded output columns stay zero.
+__global__ void k_guide_adam(float* params, const float* __restrict__ part, int nparts, float* m, float* v,
+                             __nv_bfloat16* bfw, const float* stats, float lr, float b1, float b2, float eps,
+                             const int* step) {
     const float norm = 1.f / fmaxf(stats[1], 1e-12f);
     // bias corrections of Adam step t = *step + 1 (the counter lives on the device so that captured
     // graphs replay correctly; k_guide_tick advances it)
@@ -709,9 +731,10 @@ __global__ void k_guide_adam(float* params, float* grad, float* m, float* v, __n
         bool is_bias = rel >= K * N;
         int kk = is_bias ? 0 : rel / N, nn = is_bias ? rel - K * N : rel % N;
         bool pad = (l == 3) && (nn >= kGuideOut);
-        float g = pad ? 0.f : grad[p] * norm;
+        float sum = 0.f;
+        for (int q = 0; q < nparts; q++) sum += part[(size_t)q * kGuideParams + p];
+        float g = pad ? 0.f : sum * norm;
         if (!isfinite(g)) g = 0.f;  // a non-finite batch leaves the weights unchanged
-        grad[p] = 0.f;
         float mm = b1 * m[p] + (1.f - b1) * g;
         float vv = b2 * v[p] + (1.f - b2) * g * g;
         m[p] = mm;
@@ -727,7 +750,24 @@ __global__ void k_guide_adam(float* params, float* grad, float* m, float* v, __n
     }
 }
 
-__global__ void k_guide_tick(int* step) { *step += 1; }
+// Sum of the per-warpgroup partial gradients (the explicit-batch gradient entry point).
+__global__ void k_guide_reduce(const float* __restrict__ part, int nparts, float* grad) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < kGuideParams; p += gridDim.x * blockDim.x) {
+        float sum = 0.f;
+        for (int q = 0; q < nparts; q++) sum += part[(size_t)q * kGuideParams + p];
+        grad[p] = sum;
+    }
+}
+
+// After an Adam step: advance the step counter, keep the step's loss and weight sum for reporting
+// (stats[4..5]) and clear the accumulators for the next step.
+__global__ void k_guide_tick(int* step, float* stats) {
+    *step += 1;
+    stats[4] = stats[0];
+    stats[5] = stats[1];
+    stats[0] = 0.f;
+    stats[1] = 0.f;
+}
 
 __global__ void k_guide_bf16_from_params(const float* params, __nv_bfloat16* bfw) {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < kGuideParams; p += gridDim.x * blockDim.x) {
@@ -749,10 +789,10 @@ __global__ void k_guide_bf16_from_params(const float* params, __nv_bfloat16* bfw
 GuideTrainer::~GuideTrainer() = default;
 
 void GuideTrainer::release(DeviceArena& arena) {
-    void* ps[] = {params_, grad_, adam_m_, adam_v_, bf_, out_, stage_, rec_, batch_, batch_count_, loss_acc_, step_dev_};
+    void* ps[] = {params_, grad_, part_, adam_m_, adam_v_, bf_, out_, stage_, rec_, batch_, batch_count_, loss_acc_, step_dev_};
     for (void* p : ps)
         if (p) arena.free(p);
-    params_ = grad_ = adam_m_ = adam_v_ = nullptr;
+    params_ = grad_ = part_ = adam_m_ = adam_v_ = nullptr;
     bf_ = nullptr;
     out_ = nullptr;
     stage_ = nullptr;
@@ -770,16 +810,21 @@ int GuideTrainer::init(DeviceArena& arena, size_t paths, int max_depth, const fl
                        unsigned long long seed, std::string& err) {
     auto A = [&](size_t bytes) { return arena.alloc(bytes, err); };
     if (!params_) {
+        prepare_launch();
+        nparts_ = train_parts();
         params_ = (float*)A(kGuideParams * 4);
         grad_ = (float*)A(kGuideParams * 4);
+        part_ = (float*)A((size_t)nparts_ * kGuideParams * 4);
         adam_m_ = (float*)A(kGuideParams * 4);
         adam_v_ = (float*)A(kGuideParams * 4);
         bf_ = (__nv_bfloat16*)A(kGuideBf16 * 2);
-        loss_acc_ = (float*)A(16);
+        loss_acc_ = (float*)A(32);
         batch_count_ = (int*)A(16);
         step_dev_ = (int*)A(16);
-        if (!params_ || !grad_ || !adam_m_ || !adam_v_ || !bf_ || !loss_acc_ || !batch_count_ || !step_dev_) return C2G_ERR_OOM;
+        if (!params_ || !grad_ || !part_ || !adam_m_ || !adam_v_ || !bf_ || !loss_acc_ || !batch_count_ || !step_dev_)
+            return C2G_ERR_OOM;
         cudaMemset(step_dev_, 0, 16);
+        cudaMemset(loss_acc_, 0, 32);
         // He-uniform initialisation (seeded); the output layer starts small so the first mixture is broad
         std::vector<float> h(kGuideParams, 0.f);
         std::mt19937_64 rng(seed ^ 0x9e3779b97f4a7c15ULL);
@@ -806,7 +851,7 @@ int GuideTrainer::init(DeviceArena& arena, size_t paths, int max_depth, const fl
         k_guide_bf16_from_params<<<64, 256>>>(params_, bf_);
         cudaFuncSetAttribute(k_guide_mlp_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
         cudaFuncSetAttribute(k_guide_mlp_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
-        cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem);
+        cudaFuncSetAttribute(k_guide_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTgSmem);
         steps_ = 0;
     }
     for (int a = 0; a < 3; a++) {
@@ -821,8 +866,8 @@ int GuideTrainer::init(DeviceArena& arena, size_t paths, int max_depth, const fl
         if (batch_) arena.free(batch_);
         cap_ = paths;
         rec_depth_ = std::max(1, max_depth);
-        // about 2^18 recorded vertices per wave: every rec_stride-th path records its bounces
-        rec_stride_ = (int)std::max<size_t>(1, paths * 3 / (1u << 18));
+        // about rec_target_ recorded vertices per wave: every rec_stride-th path records its bounces
+        rec_stride_ = (int)std::max<size_t>(1, paths * 3 / (size_t)rec_target_);
         rec_cap_ = (paths / rec_stride_ + 1) * rec_depth_;
         out_ = (float*)A(paths * kGuidePacked * 4);
         stage_ = (unsigned char*)A(stage_bytes(paths));
@@ -845,6 +890,7 @@ void GuideTrainer::prepare_launch() {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaFuncSetAttribute(k_guide_mlp_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
     cudaFuncSetAttribute(k_guide_mlp_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+    cudaFuncSetAttribute(k_guide_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTgSmem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_guide_mlp_tc<0>, kTcThreads, kTcSmem);
     // resident CTAs per SM as shared memory allows (1 KB reserved per CTA), in case the query
     // under-reports; extra CTAs of a persistent grid only wait for a slot
@@ -875,21 +921,28 @@ int GuideTrainer::infer(cudaStream_t st, const void* Sv, const float4* ray_o, co
     return 2;
 }
 
-void GuideTrainer::train(cudaStream_t st, const float4* out_L, int wave_paths, int steps) {
+int GuideTrainer::train_parts() {
+    prepare_launch();
+    return g_train_grid * kTgGroups;
+}
+
+void GuideTrainer::train(cudaStream_t st, const float4* out_L, int wave_paths, int steps, int* err) {
     cudaMemsetAsync(batch_count_, 0, 16, st);
-    cudaMemsetAsync(loss_acc_, 0, 16, st);
+    cudaMemsetAsync(loss_acc_, 0, 32, st);
     k_guide_batch<<<(int)std::min<size_t>(4096, (rec_cap_ + 255) / 256), 256, 0, st>>>(
         rec_, (int)rec_cap_, rec_depth_, rec_stride_, out_L, wave_paths, batch_, batch_count_, loss_acc_, (int)rec_cap_);
     prepare_launch();
-    const int grid = g_train_grid;
     GuideNet net = view(false, false).net;
+    // per Adam step: the fused tensor-core forward/backward over one minibatch window (partial
+    // gradients per warpgroup), Adam over their sum, and the step counter; k_guide_tick clears the
+    // loss accumulators for the next step
     for (int s = 0; s < steps; s++) {
-        cudaMemsetAsync(loss_acc_, 0, 8, st);  // this step's loss and weight sum (Adam normalises by it)
-        k_guide_train<<<grid, 256, kTrainSmem, st>>>(net, batch_, batch_count_, (int)rec_cap_, grad_, loss_acc_,
-                                                     std::min(steps, kTrainWindows), step_dev_);
+        k_guide_train_tc<<<g_train_grid, kTgThreads, kTgSmem, st>>>(net, batch_, batch_count_, (int)rec_cap_, part_, loss_acc_,
+                                                                   std::min(steps, windows_), step_dev_, err);
         steps_++;
-        k_guide_adam<<<64, 256, 0, st>>>(params_, grad_, adam_m_, adam_v_, bf_, loss_acc_, lr_, 0.9f, 0.99f, 1e-8f, step_dev_);
-        k_guide_tick<<<1, 1, 0, st>>>(step_dev_);
+        k_guide_adam<<<64, 256, 0, st>>>(params_, part_, nparts_, adam_m_, adam_v_, bf_, loss_acc_, lr_, 0.9f, 0.99f, 1e-8f,
+                                         step_dev_);
+        k_guide_tick<<<1, 1, 0, st>>>(step_dev_, loss_acc_);
     }
 }
 
@@ -972,37 +1025,46 @@ int GuideTrainer::gradient(DeviceArena& arena, const float* host_samples, int n,
         b[4 * j + 3] = make_float4(v[9], v[10], v[11], v[13]);
     }
     float4* db = (float4*)arena.alloc(b.size() * 16, err);
-    if (!db) return C2G_ERR_OOM;
+    int* derr = (int*)arena.alloc(16, err);
+    if (!db || !derr) {
+        if (db) arena.free(db);
+        if (derr) arena.free(derr);
+        return C2G_ERR_OOM;
+    }
     // stats[2] = n makes the kernel's weight normaliser (mean weight) exactly 1
-    float st[4] = {0.f, 0.f, (float)n, 0.f};
+    float st[8] = {0.f, 0.f, (float)n, 0.f, 0.f, 0.f, 0.f, 0.f};
     cudaMemcpy(db, b.data(), b.size() * 16, cudaMemcpyHostToDevice);
     cudaMemcpy(batch_count_, &n, 4, cudaMemcpyHostToDevice);
-    cudaMemcpy(loss_acc_, st, 16, cudaMemcpyHostToDevice);
-    cudaMemset(grad_, 0, kGuideParams * 4);
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    k_guide_train<<<sms, 256, kTrainSmem>>>(view(false, false).net, db, batch_count_, n, grad_, loss_acc_, 1, step_dev_);
-    int rc = C2G_OK;
+    cudaMemcpy(loss_acc_, st, 32, cudaMemcpyHostToDevice);
+    cudaMemset(derr, 0, 16);
+    prepare_launch();
+    k_guide_train_tc<<<g_train_grid, kTgThreads, kTgSmem>>>(view(false, false).net, db, batch_count_, n, part_, loss_acc_, 1,
+                                                           step_dev_, derr);
+    k_guide_reduce<<<64, 256>>>(part_, nparts_, grad_);
+    int rc = C2G_OK, h = 0;
     if (cudaDeviceSynchronize() != cudaSuccess) { err = cudaGetErrorString(cudaGetLastError()); rc = C2G_ERR_CUDA; }
-    else {
+    else if (cudaMemcpy(&h, derr, 4, cudaMemcpyDeviceToHost) == cudaSuccess && h) {
+        err = "guide training: tensor-core completion wait timed out";
+        rc = C2G_ERR_DEVICE;
+    } else {
         cudaMemcpy(host_grad, grad_, kGuideParams * 4, cudaMemcpyDeviceToHost);
-        cudaMemcpy(st, loss_acc_, 16, cudaMemcpyDeviceToHost);
+        cudaMemcpy(st, loss_acc_, 32, cudaMemcpyDeviceToHost);
         if (loss) *loss = st[1] > 0 ? (double)st[0] / st[1] : 0.0;
     }
-    cudaMemset(grad_, 0, kGuideParams * 4);
+    cudaMemset(loss_acc_, 0, 32);
     arena.free(db);
+    arena.free(derr);
     return rc;
 }
 
 GuideStats GuideTrainer::stats() {
-    float h[4] = {0, 0, 0, 0};
+    float h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int n = 0;
-    if (loss_acc_) cudaMemcpy(h, loss_acc_, 16, cudaMemcpyDeviceToHost);
+    if (loss_acc_) cudaMemcpy(h, loss_acc_, 32, cudaMemcpyDeviceToHost);
     if (batch_count_) cudaMemcpy(&n, batch_count_, 4, cudaMemcpyDeviceToHost);
     int t = steps_;
     if (step_dev_) cudaMemcpy(&t, step_dev_, 4, cudaMemcpyDeviceToHost);
-    last_.loss = h[1] > 0 ? h[0] / h[1] : 0.0;
+    last_.loss = h[5] > 0 ? h[4] / h[5] : 0.0;  // the last Adam step's batch
     last_.records = n;
     last_.steps = t;
     return last_;

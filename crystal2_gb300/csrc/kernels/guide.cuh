@@ -1,17 +1,17 @@
-// Learned path-guiding proposal: input encoding, the BF16 tensor-core MLP, and the directional
-// mixture it parameterises.
+// Learned path-guiding proposal: the network's shapes and the directional mixture it
+// parameterises.
 //
 // Network: 80 inputs (position p in the scene box, normalised to [0, 1]^3 and encoded as
 // sin/cos(pi 2^f p) for f = 0..11 per axis = 72; shading normal 3; outgoing direction 3; 2 zeros),
 // three hidden ReLU layers of 64, 40 outputs = 8 lobes x (mean direction 3, concentration 1,
-// weight logit 1).  The mixture is a sum of
-// von Mises-Fisher lobes on the sphere, which has a closed-form pdf and an exact sampling routine,
-// so the guided estimator can use exactly evaluated pdfs.
+// weight logit 1) and the technique-selection logit.  The mixture is a sum of von Mises-Fisher
+// lobes on the sphere, which has a closed-form pdf and an exact sampling routine, so the guided
+// estimator can use exactly evaluated pdfs.
 //
-// Matrix products use the warp-level tensor-core instruction mma.sync.m16n8k16 (BF16 inputs, FP32
-// accumulators) on 16-row tiles held in shared memory (guide.cu).  Weight layout per layer l (K_l inputs,
-// N_l outputs): `wt` = N_l x K_l row-major BF16 (the B operand of x @ W), `wn` = K_l x N_l row-major
-// BF16 (the B operand of delta @ W^T), bias FP32.
+// Matrix products run on the fifth-generation tensor cores (tcgen05.mma, BF16 operands in shared
+// memory, FP32 accumulators in tensor memory; guide.cu).  Weight layout per layer l (K_l inputs,
+// N_l outputs): `wt` = N_l x K_l row-major BF16 (staged K-major for x @ W, and read MN-major for
+// delta @ W^T), `wn` = K_l x N_l row-major BF16, bias FP32.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -20,39 +20,7 @@
 
 namespace c2g {
 
-// ---- input encoding ------------------------------------------------------------------------
-__device__ __forceinline__ void guide_encode(const GuideNet& g, float3 x, float3 n, float3 wo, float* in) {
-    float p[3] = {(x.x - g.box_lo[0]) * g.box_inv[0], (x.y - g.box_lo[1]) * g.box_inv[1], (x.z - g.box_lo[2]) * g.box_inv[2]};
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        float v = fminf(fmaxf(p[a], 0.f), 1.f);
-        // sin/cos(pi v) with exact argument reduction, then the double-angle recurrence
-        // sin 2u = 2 sin u cos u, cos 2u = (cos u - sin u)(cos u + sin u) for the higher frequencies
-        // (the absolute error grows about 2x per octave: ~1e-4 at 2^11, far below BF16 resolution)
-        float s, c;
-        sincospif(v, &s, &c);
-#pragma unroll
-        for (int f = 0; f < kGuideFreqs; f++) {
-            in[a * 2 * kGuideFreqs + 2 * f] = s;
-            in[a * 2 * kGuideFreqs + 2 * f + 1] = c;
-            const float s2 = 2.f * s * c, c2 = (c - s) * (c + s);
-            s = s2;
-            c = c2;
-        }
-    }
-    in[72] = n.x; in[73] = n.y; in[74] = n.z;
-    in[75] = wo.x; in[76] = wo.y; in[77] = wo.z;
-    in[78] = 0.f; in[79] = 0.f;
-}
-
-// ---- tensor-core tile helpers ----------------------------------------------------------------
-__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, const uint32_t* b) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
+// ---- BF16 packing --------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);

@@ -73,14 +73,24 @@ public:
     // Returns the kernels launched (0 when no bucket of the mask is guided).
     int infer(cudaStream_t st, const void* S, const float4* ray_o, const float4* ray_d, const float4* hits,
               const int* bucket_cnt, const int* bucket_list, int cap, int bucket_mask);
-    // Turn this wave's records into weighted samples and take `steps` Adam steps.
-    void train(cudaStream_t st, const float4* out_L, int wave_paths, int steps);
+    // Turn this wave's records into weighted samples and take `steps` Adam steps (a tensor-memory
+    // wait that times out sets DEVERR_WAIT in *err).
+    void train(cudaStream_t st, const float4* out_L, int wave_paths, int steps, int* err);
     GuideView view(bool record, bool sample) const;
     // Launch configuration (occupancy queries), done once before any stream capture.
     static void prepare_launch();
+    // Partial gradients the training kernel writes per launch (one per warpgroup of its grid).
+    static int train_parts();
     GuideStats stats();
     void set_learning_rate(float lr) { lr_ = lr; }
     void set_alpha(float a) { alpha_ = a; }
+    // Recorded vertices per wave and minibatch windows (the record buffers are re-sized by the next
+    // init()).
+    void set_batch(int records, int windows) {
+        if (records != rec_target_) cap_ = 0;
+        rec_target_ = records;
+        windows_ = windows;
+    }
     // Network weights as the flat FP32 vector (kGuideParams); setting them clears the Adam state.
     int set_params(const float* host, std::string& err);
     int get_params(float* host, std::string& err);
@@ -93,7 +103,9 @@ public:
 
 private:
     float* params_ = nullptr;        // FP32 master weights
-    float* grad_ = nullptr;
+    float* grad_ = nullptr;          // summed gradient (explicit-batch entry point)
+    float* part_ = nullptr;          // per-warpgroup partial gradients of the last training launch
+    int nparts_ = 0;
     float* adam_m_ = nullptr;
     float* adam_v_ = nullptr;
     __nv_bfloat16* bf_ = nullptr;    // BF16 copies (both layouts)
@@ -102,10 +114,13 @@ private:
     float4* rec_ = nullptr;
     float4* batch_ = nullptr;        // compacted training samples (x|w, n, wo, wi)
     int* batch_count_ = nullptr;
-    float* loss_acc_ = nullptr;      // [0] weighted NLL sum, [1] weight sum, [2] raw weight sum
+    float* loss_acc_ = nullptr;      // [0] weighted NLL sum, [1] weight sum, [2] raw weight sum,
+                                     // [4..5] the last Adam step's [0..1]
     int* step_dev_ = nullptr;        // Adam steps taken (device copy: captured graphs advance it)
     size_t cap_ = 0;
     int rec_stride_ = 16, rec_depth_ = 1;
+    int rec_target_ = 1 << 18;       // recorded vertices per wave (about)
+    int windows_ = 4;                // minibatch windows per wave
     size_t rec_cap_ = 0;
     float box_lo_[3] = {0, 0, 0}, box_inv_[3] = {1, 1, 1};
     float lr_ = 2e-3f;

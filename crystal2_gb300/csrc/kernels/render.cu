@@ -1315,7 +1315,7 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
     if (guided) {
         // online training on this wave's recorded vertices (batch build, fused fwd/bwd, Adam)
         begin(C2G_K_TRAIN);
-        guide_.train(st, w.out_L, a.nslots * a.wave_samples, guide_train_steps_);
+        guide_.train(st, w.out_L, a.nslots * a.wave_samples, guide_train_steps_, S.err);
         end();
         launches += 1 + 3 * guide_train_steps_;
     }

@@ -236,6 +236,10 @@ class Context:
         self.check(self._lib.c2g_guide_stats(self._h, C.byref(loss), C.byref(rec), C.byref(steps)))
         return loss.value, rec.value, steps.value
 
+    def guide_batch(self, records_per_wave: int = 1 << 18, windows: int = 4) -> None:
+        """Recorded vertices per guided wave and the minibatch windows its Adam steps take in turn."""
+        self.check(self._lib.c2g_guide_batch(self._h, int(records_per_wave), int(windows)))
+
     def guide_config(self, learning_rate: float = 2e-3, bsdf_fraction: float = 0.5, warmup_waves: int = 2,
                      train_steps: int = 1) -> None:
         self.check(self._lib.c2g_guide_config(self._h, float(learning_rate), float(bsdf_fraction), int(warmup_waves),

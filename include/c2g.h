@@ -225,7 +225,7 @@ int c2g_batch_job_latency(c2g_batch* b, int i, double* ms);
  * No counterpart in the reference, which has no guided integrator; these calls configure and
  * inspect the network the guided path tracer trains online.  The network maps (position in the
  * scene box, shading normal, outgoing direction) to an 8-lobe von Mises-Fisher mixture over
- * directions and the probability c = 0.05 + 0.9 sigmoid(s) of drawing from it rather than from the
+ * directions and the probability c = 0.05 + 0.75 sigmoid(s) of drawing from it rather than from the
  * BSDF; its weights are one flat FP32 vector of C2G_GUIDE_PARAMS values, layer by layer W (inputs x
  * outputs, row-major) then b, for layers 80->64->64->64->48 (outputs 41..47 are padding, kept
  * zero).  Loading a scene discards the network; a guided render creates one. */
@@ -246,9 +246,13 @@ int c2g_guide_gradient(c2g_ctx* ctx, int n, const float* samples, float* grad, d
 /* Training state of the last guided render: weighted NLL of the last batch, its size, Adam steps. */
 int c2g_guide_stats(c2g_ctx* ctx, double* loss, int* records, int* steps);
 /* learning_rate (Adam), bsdf_fraction (initial one-sample MIS probability of the BSDF technique,
- * (0, 1]; the network then learns it per vertex, within [0.05, 0.95]), warmup_waves (guided waves
+ * (0, 1]; the network then learns it per vertex, within [0.2, 0.95]), warmup_waves (guided waves
  * that only train), train_steps (Adam steps per wave). */
 int c2g_guide_config(c2g_ctx* ctx, float learning_rate, float bsdf_fraction, int warmup_waves, int train_steps);
+/* Training batch of a guided wave: about records_per_wave recorded path vertices (every k-th path
+ * records its bounces; default 262144, at least 1024) split into `windows` minibatch windows that
+ * the wave's Adam steps take in turn (default 4, 1..64).  Takes effect at the next guided render. */
+int c2g_guide_batch(c2g_ctx* ctx, int records_per_wave, int windows);
 /* Bounce levels, from the camera hit, whose vertices sample (and train) the guide; deeper vertices
  * use the plain tracer's estimator.  0 = every level; default 2. */
 int c2g_guide_levels(c2g_ctx* ctx, int levels);
