@@ -276,6 +276,9 @@ def run_ours(args) -> None:
     step(0)
     cst = ctx.stats()
     counts = {k: (cst.rays[i], cst.nodes[i], cst.prims[i]) for i, k in ((N.K_EXTEND, "extend"), (N.K_SHADOW, "shadow"), (N.K_MIS, "mis"))}
+    level_paths = [int(v) for v in cst.level_paths[:]]
+    while level_paths and level_paths[-1] == 0:
+        level_paths.pop()
     # timed region (per-launch CUDA events on for the roofline)
     ctx.set_counting(N.COUNT_TIMING)
     clocks = ClockSampler(local)
@@ -287,6 +290,7 @@ def run_ours(args) -> None:
     ev1 = torch.cuda.Event(enable_timing=True)
     kernel_ms = np.zeros(N.K_KINDS)
     kernel_n = np.zeros(N.K_KINDS)
+    level_ms = np.zeros(N.LEVELS)
     launches = 0
     ev0.record(stream)
     for i in range(args.steps):
@@ -294,6 +298,7 @@ def run_ours(args) -> None:
         st = ctx.stats()
         kernel_ms += np.array(st.kernel_ms[:])
         kernel_n += np.array(st.kernel_count[:])
+        level_ms += np.array(st.level_ms[:])
         launches += st.kernel_launches
     ev1.record(stream)
     torch.cuda.synchronize()
@@ -397,6 +402,7 @@ def run_ours(args) -> None:
                         "d2h_bytes_per_step": int(p.width * p.height * 16)},
                 "gpu_launches": int(launches), "roofline": roof, "kernel_share": share,
                 "traversal_per_step": {k: {"rays": v[0], "nodes": v[1], "prims": v[2]} for k, v in counts.items()},
+                "levels": {"paths": level_paths, "ms": [round(float(v) / args.steps, 4) for v in level_ms[:len(level_paths)]]},
                 "clocks": clk, "cpu_baseline": cpu, "guided_equal_time": guided, "batch": batch, "ray_microbench": rays}
         print(json.dumps(line), flush=True)
     if dist:
@@ -481,8 +487,10 @@ def guided_equal_time(args) -> dict:
 def batch_run(args) -> dict:
     """Batched multi-job rendering: `--batch-jobs` seeded jobs (Cornell and many-material variants,
     square resolutions log-uniform in [128, 1024], spp from {16, 64, 256, 1024}, guided or plain)
-    rendered together through replayed CUDA graphs on concurrent streams; the wave size and the
-    stream count are picked by the library's autotuner on a 4-spp trial of every job."""
+    rendered together on one GPU.  The library's coordinate search picks, on a 4-spp trial of every
+    job, the wave size, the mode (0 = the whole batch as one graph launch with device-side wave
+    loops per job; S > 0 = per-job wave graphs on S streams), the traversal variant (two- or
+    four-wide nodes) and the traversal kernels' block size."""
     import numpy as np
     from crystal2_gb300 import Batch, Context, scenes
     from crystal2_gb300 import _native as N
@@ -504,15 +512,19 @@ def batch_run(args) -> dict:
         n_guided += int(guided)
     load_s = time.time() - t0
     t0 = time.time()
-    best = b.autotune(wave_paths=(1 << 19, 1 << 20, 1 << 21, 1 << 22), streams=(1, 2, 4, 8), trial_spp=4)
+    best = b.search(wave_paths=(1 << 20, 1 << 21, 1 << 22, 1 << 23), streams=(0, 8), traversal=(4, 2),
+                    trace_block=(128, 64, 256), trial_spp=4)
     tune_s = time.time() - t0
     st = b.run()
     lat = [b.latency_ms(i) for i in range(len(jobs))]
     out = {"jobs": st.jobs, "guided_jobs": n_guided, "paths": st.paths, "seconds": round(st.seconds, 3),
            "mpaths_per_s": round(st.mpaths_per_s, 2), "latency_p50_ms": round(st.latency_p50_ms, 2),
-           "latency_p99_ms": round(st.latency_p99_ms, 2), "latency_max_ms": round(st.latency_max_ms, 2),
-           "tuned": {"wave_paths": st.wave_paths, "streams": st.streams, "trial_mpaths_per_s": round(best, 2),
-                     "tune_s": round(tune_s, 2)},
+           "latency_p90_ms": round(st.latency_p90_ms, 2), "latency_p99_ms": round(st.latency_p99_ms, 2),
+           "latency_max_ms": round(st.latency_max_ms, 2), "latency_mean_ms": round(st.latency_mean_ms, 2),
+           "latency_rule": "nearest rank over the jobs' completion times from the batch start",
+           "tuned": {"wave_paths": st.wave_paths, "mode": "one graph launch" if st.streams == 0 else f"{st.streams} streams",
+                     "traversal": f"{st.traversal}-wide nodes", "trace_block": st.trace_block,
+                     "trial_mpaths_per_s": round(best, 2), "tune_s": round(tune_s, 2)},
            "graph_launches": st.graph_launches, "scene_load_s": round(load_s, 1),
            "resolutions": [int(c.render_params().width) for c in ctxs],
            "latency_ms": [round(x, 2) for x in lat]}

@@ -56,6 +56,7 @@ class RenderParams(C.Structure):
 
 K_RAYGEN, K_EXTEND, K_SHADE, K_SHADOW, K_MIS, K_ACCUM, K_FILM, K_GUIDE, K_TRAIN = range(9)
 K_KINDS = 10
+LEVELS = 64
 KERNEL_NAMES = ["raygen", "extend", "shade", "shadow", "mis", "accumulate", "film", "guide", "train", "-"]
 COUNT_TRAVERSAL = 1
 COUNT_TIMING = 2
@@ -65,13 +66,22 @@ class Stats(C.Structure):
     _fields_ = [("seconds", C.c_double), ("paths", C.c_double), ("rays", C.c_double * K_KINDS),
                 ("nodes", C.c_double * K_KINDS), ("prims", C.c_double * K_KINDS), ("kernel_ms", C.c_double * K_KINDS),
                 ("kernel_count", C.c_int * K_KINDS),
-                ("kernel_launches", C.c_int), ("waves", C.c_int)]
+                ("kernel_launches", C.c_int), ("waves", C.c_int),
+                ("level_ms", C.c_double * LEVELS), ("level_paths", C.c_double * LEVELS), ("levels", C.c_int)]
 
 
 class BatchStats(C.Structure):
     _fields_ = [("jobs", C.c_int), ("paths", C.c_double), ("seconds", C.c_double), ("mpaths_per_s", C.c_double),
                 ("latency_p50_ms", C.c_double), ("latency_p99_ms", C.c_double), ("latency_max_ms", C.c_double),
-                ("wave_paths", C.c_int), ("streams", C.c_int), ("graph_launches", C.c_int)]
+                ("wave_paths", C.c_int), ("streams", C.c_int), ("graph_launches", C.c_int),
+                ("latency_p90_ms", C.c_double), ("latency_mean_ms", C.c_double), ("traversal", C.c_int),
+                ("trace_block", C.c_int)]
+
+
+class BatchSpace(C.Structure):
+    _fields_ = [("wave_paths", C.POINTER(C.c_int)), ("n_wave_paths", C.c_int), ("streams", C.POINTER(C.c_int)),
+                ("n_streams", C.c_int), ("traversal", C.POINTER(C.c_int)), ("n_traversal", C.c_int),
+                ("trace_block", C.POINTER(C.c_int)), ("n_trace_block", C.c_int)]
 
 
 _P = C.c_void_p
@@ -127,6 +137,8 @@ SIGNATURES = {
     "c2g_batch_add": (_I, [_P, _P, C.POINTER(RenderParams), _IP]),
     "c2g_batch_tune": (_I, [_P, _I, _I]),
     "c2g_batch_autotune": (_I, [_P, _IP, _I, _IP, _I, _I, C.POINTER(C.c_double)]),
+    "c2g_batch_set_trace": (_I, [_P, _I, _I]),
+    "c2g_batch_search": (_I, [_P, C.POINTER(BatchSpace), _I, C.POINTER(C.c_double)]),
     "c2g_batch_run": (_I, [_P, C.POINTER(BatchStats)]),
     "c2g_batch_job_latency": (_I, [_P, _I, C.POINTER(C.c_double)]),
 }

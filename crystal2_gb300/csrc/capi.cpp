@@ -645,7 +645,9 @@ struct c2g_batch {
     std::vector<BatchJob> jobs;
     std::vector<cudaStream_t> streams;
     int wave_paths = 1 << 20;
-    int n_streams = 4;
+    int n_streams = 0;          // 0: every job in one graph launch; > 0: per-job graphs on this many streams
+    int traversal = 4;          // SAH node width of every job's traversal
+    int trace_block = 128;      // threads per block of the traversal kernels
     int captured_wave_paths = -1;
     std::string last_error;
 };
@@ -662,9 +664,18 @@ void drop_graphs(BatchJob& j) {
     j.g_warm = j.g_main = nullptr;
 }
 
+// The batch's traversal variant and block size on every job's context (taken by the next capture).
+void batch_apply_trace(c2g_batch* b) {
+    for (BatchJob& j : b->jobs) {
+        j.ctx->gpu->set_sah_width(b->traversal);
+        j.ctx->gpu->set_trace_block(b->trace_block);
+    }
+}
+
 // Capture every job's wave graphs for the batch's wave size.
 int batch_capture(c2g_batch* b) {
     if (b->captured_wave_paths == b->wave_paths) return C2G_OK;
+    batch_apply_trace(b);
     cudaStream_t st = b->streams.empty() ? nullptr : b->streams[0];
     for (size_t i = 0; i < b->jobs.size(); i++) {
         BatchJob& j = b->jobs[i];
@@ -699,8 +710,109 @@ int batch_streams(c2g_batch* b) {
     return C2G_OK;
 }
 
+void fill_stats(c2g_batch* b, std::vector<double> lat, double paths, float total_ms, int launches, c2g_batch_stats* out) {
+    if (!out) return;
+    std::sort(lat.begin(), lat.end());
+    auto pct = [&](double q) {
+        if (lat.empty()) return 0.0;
+        size_t i = (size_t)std::min<double>((double)lat.size() - 1, std::ceil(q * lat.size()) - 1);
+        return lat[i];
+    };
+    double mean = 0.0;
+    for (double v : lat) mean += v;
+    *out = c2g_batch_stats{};
+    out->jobs = (int)b->jobs.size();
+    out->paths = paths;
+    out->seconds = total_ms * 1e-3;
+    out->mpaths_per_s = total_ms > 0 ? paths / (total_ms * 1e-3) / 1e6 : 0.0;
+    out->latency_p50_ms = pct(0.5);
+    out->latency_p90_ms = pct(0.9);
+    out->latency_p99_ms = pct(0.99);
+    out->latency_max_ms = lat.empty() ? 0.0 : lat.back();
+    out->latency_mean_ms = lat.empty() ? 0.0 : mean / lat.size();
+    out->wave_paths = b->wave_paths;
+    out->streams = b->n_streams;
+    out->graph_launches = launches;
+    out->traversal = b->traversal;
+    out->trace_block = b->trace_block;
+}
+
+// Every job in one graph: per job a chain (sample counter reset, device-side while loops over its
+// waves, completion event), the chains independent of each other, so one cudaGraphLaunch renders the
+// whole batch and the GPU interleaves the jobs' kernels.  `spp_limit` caps every job's samples.
+int batch_pass_graph(c2g_batch* b, int spp_limit, c2g_batch_stats* out) {
+    if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "cudaSetDevice failed");
+    if (cudaDeviceSynchronize() != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "device error before the batch");
+    if (b->streams.empty()) {
+        cudaStream_t st;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "stream creation failed");
+        b->streams.push_back(st);
+    }
+    cudaStream_t st = b->streams[0];
+    batch_apply_trace(b);
+    cudaGraph_t G = nullptr;
+    if (cudaGraphCreate(&G, 0) != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "graph creation failed");
+    double paths = 0.0;
+    int rc = C2G_OK;
+    for (size_t i = 0; i < b->jobs.size() && !rc; i++) {
+        BatchJob& j = b->jobs[i];
+        if (!j.done) cudaEventCreate(&j.done);
+        c2g_render_params q = j.p;
+        if (spp_limit > 0) q.sample_count = std::max(1, std::min(q.sample_count, spp_limit));
+        std::string err;
+        int spw = 0, waves = 0;
+        rc = j.ctx->gpu->append_job(G, nullptr, 0, q, b->wave_paths, j.done, st, *j.ctx->arena, &spw, &waves, err);
+        if (rc) {
+            bfail(b, rc, "job " + std::to_string(i) + ": " + err);
+            break;
+        }
+        j.spw = spw;
+        j.waves = waves;
+        paths += (double)q.width * q.height * q.sample_count;
+    }
+    cudaGraphExec_t exec = nullptr;
+    if (!rc) {
+        cudaError_t e = cudaGraphInstantiate(&exec, G, 0);
+        if (e != cudaSuccess) rc = bfail(b, C2G_ERR_CUDA, std::string("batch graph instantiation: ") + cudaGetErrorString(e));
+    }
+    cudaGraphDestroy(G);
+    if (rc) return rc;
+    cudaEvent_t start, stop;
+    cudaEventCreate(&start);
+    cudaEventCreate(&stop);
+    cudaEventRecord(start, st);
+    cudaError_t e = cudaGraphLaunch(exec, st);
+    cudaEventRecord(stop, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(stop);
+    cudaGraphExecDestroy(exec);
+    if (e != cudaSuccess) {
+        cudaEventDestroy(start);
+        cudaEventDestroy(stop);
+        return bfail(b, C2G_ERR_CUDA, std::string("batch: ") + cudaGetErrorString(e));
+    }
+    float total = 0.f;
+    cudaEventElapsedTime(&total, start, stop);
+    std::vector<double> lat;
+    for (BatchJob& j : b->jobs) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, start, j.done);
+        j.latency_ms = t;
+        lat.push_back(t);
+    }
+    cudaEventDestroy(start);
+    cudaEventDestroy(stop);
+    for (BatchJob& j : b->jobs) {
+        std::string err;
+        rc = j.ctx->gpu->check_device_error(err);
+        if (rc) return bfail(b, rc, err);
+    }
+    fill_stats(b, lat, paths, total, 1, out);
+    return C2G_OK;
+}
+
 // One pass over every job, `spp_limit` samples each (0 = the job's own count).
 int batch_pass(c2g_batch* b, int spp_limit, c2g_batch_stats* out) {
+    if (b->n_streams == 0) return batch_pass_graph(b, spp_limit, out);
     if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "cudaSetDevice failed");
     // work the jobs' contexts queued on their own streams (film clears, renders) comes first
     if (cudaDeviceSynchronize() != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "device error before the batch");
@@ -785,25 +897,7 @@ int batch_pass(c2g_batch* b, int spp_limit, c2g_batch_stats* out) {
         rc = j.ctx->gpu->check_device_error(err);
         if (rc) return bfail(b, rc, err);
     }
-    if (out) {
-        std::sort(lat.begin(), lat.end());
-        auto pct = [&](double q) {
-            if (lat.empty()) return 0.0;
-            size_t i = (size_t)std::min<double>((double)lat.size() - 1, std::ceil(q * lat.size()) - 1);
-            return lat[i];
-        };
-        *out = c2g_batch_stats{};
-        out->jobs = (int)b->jobs.size();
-        out->paths = paths;
-        out->seconds = total * 1e-3;
-        out->mpaths_per_s = total > 0 ? paths / (total * 1e-3) / 1e6 : 0.0;
-        out->latency_p50_ms = pct(0.5);
-        out->latency_p99_ms = pct(0.99);
-        out->latency_max_ms = lat.empty() ? 0.0 : lat.back();
-        out->wave_paths = b->wave_paths;
-        out->streams = ns;
-        out->graph_launches = launches;
-    }
+    fill_stats(b, lat, paths, total, launches, out);
     return C2G_OK;
 }
 }  // namespace
@@ -851,7 +945,7 @@ int c2g_batch_add(c2g_batch* b, c2g_ctx* job, const c2g_render_params* params, i
 
 int c2g_batch_tune(c2g_batch* b, int wave_paths, int streams) {
     if (!b) return C2G_ERR_INVALID;
-    if (wave_paths < 64 || streams < 1 || streams > 32) return bfail(b, C2G_ERR_INVALID, "wave_paths >= 64 and 1 <= streams <= 32");
+    if (wave_paths < 64 || streams < 0 || streams > 32) return bfail(b, C2G_ERR_INVALID, "wave_paths >= 64 and 0 <= streams <= 32");
     if (wave_paths != b->wave_paths) b->captured_wave_paths = -1;
     b->wave_paths = wave_paths;
     b->n_streams = streams;
@@ -882,6 +976,68 @@ int c2g_batch_autotune(c2g_batch* b, const int* wave_paths, int n_wave_paths, co
     c2g_batch_tune(b, bw, bs);
     if (best_mpaths_per_s) *best_mpaths_per_s = best;
     return cudaDeviceSynchronize() == cudaSuccess ? C2G_OK : bfail(b, C2G_ERR_CUDA, "autotune");
+}
+
+int c2g_batch_set_trace(c2g_batch* b, int traversal, int trace_block) {
+    if (!b) return C2G_ERR_INVALID;
+    if ((traversal != 2 && traversal != 4) || (trace_block != 64 && trace_block != 128 && trace_block != 256))
+        return bfail(b, C2G_ERR_INVALID, "traversal 2 or 4, trace_block 64, 128 or 256");
+    if (traversal != b->traversal || trace_block != b->trace_block) b->captured_wave_paths = -1;
+    b->traversal = traversal;
+    b->trace_block = trace_block;
+    return C2G_OK;
+}
+
+int c2g_batch_search(c2g_batch* b, const c2g_batch_space* space, int trial_spp, double* best_mpaths_per_s) {
+    if (!b || !space || trial_spp <= 0) return bfail(b, C2G_ERR_INVALID, "invalid search");
+    if (b->jobs.empty()) return bfail(b, C2G_ERR_STATE, "empty batch");
+    auto bad = [](const int* v, int n) { return n < 0 || (n > 0 && !v); };
+    if (bad(space->wave_paths, space->n_wave_paths) || bad(space->streams, space->n_streams) ||
+        bad(space->traversal, space->n_traversal) || bad(space->trace_block, space->n_trace_block))
+        return bfail(b, C2G_ERR_INVALID, "candidate list without values");
+    struct Cfg { int wave, streams, trav, block; };
+    Cfg cur{b->wave_paths, b->n_streams, b->traversal, b->trace_block};
+    auto apply = [&](const Cfg& c) {
+        int rc = c2g_batch_tune(b, c.wave, c.streams);
+        return rc ? rc : c2g_batch_set_trace(b, c.trav, c.block);
+    };
+    double best = -1.0;
+    auto trial = [&](const Cfg& c, double* rate) {
+        int rc = apply(c);
+        if (rc) return rc;
+        c2g_batch_stats st{};
+        rc = batch_pass(b, trial_spp, &st);
+        if (rc) return rc;
+        *rate = st.mpaths_per_s;
+        return C2G_OK;
+    };
+    int rc = trial(cur, &best);
+    if (rc) return rc;
+    const int* lists[4] = {space->wave_paths, space->streams, space->traversal, space->trace_block};
+    const int counts[4] = {space->n_wave_paths, space->n_streams, space->n_traversal, space->n_trace_block};
+    for (int dim = 0; dim < 4; dim++) {
+        for (int i = 0; i < counts[dim]; i++) {
+            Cfg c = cur;
+            int* field = dim == 0 ? &c.wave : dim == 1 ? &c.streams : dim == 2 ? &c.trav : &c.block;
+            if (*field == lists[dim][i]) continue;
+            *field = lists[dim][i];
+            double r = 0.0;
+            rc = trial(c, &r);
+            if (rc) return rc;
+            if (r > best) { best = r; cur = c; }
+        }
+    }
+    // trials leave samples in the films and train the networks: start the real run clean
+    for (BatchJob& j : b->jobs) {
+        drop_graphs(j);
+        j.ctx->gpu->guide().release(*j.ctx->arena);
+        j.ctx->gpu->film_clear(nullptr);
+    }
+    b->captured_wave_paths = -1;
+    rc = apply(cur);
+    if (rc) return rc;
+    if (best_mpaths_per_s) *best_mpaths_per_s = best;
+    return cudaDeviceSynchronize() == cudaSuccess ? C2G_OK : bfail(b, C2G_ERR_CUDA, "search");
 }
 
 int c2g_batch_run(c2g_batch* b, c2g_batch_stats* stats) {

@@ -96,6 +96,7 @@ struct WaveBuffers {
     int* mis_list = nullptr;
     int* bucket_list = nullptr;  // kBuckets lists of P slots
     int* counters = nullptr;  // [0],[1] path queues, [2] shadow, [3] mis, [8..20) material buckets
+    int* levels = nullptr;    // statistics: paths entering each bounce level (C2G_LEVELS)
     std::vector<void*> owned;
 };
 
@@ -265,7 +266,7 @@ __global__ void k_extend(DevScene S, const float4* __restrict__ qo, const float4
 // is finished writes its hit, appends the slot to its material bucket (all lanes join the keyed
 // append of every round; idle lanes with no key) and takes the next ray.
 template <bool COUNT>
-__global__ void __launch_bounds__(128, C2G_EXTEND_MIN_BLOCKS) k_extend_fetch(DevScene S, const float4* __restrict__ qo, const float4* __restrict__ qd,
+__global__ void __launch_bounds__(256, C2G_EXTEND_MIN_BLOCKS) k_extend_fetch(DevScene S, const float4* __restrict__ qo, const float4* __restrict__ qd,
                                                       float4* hit, const int* qcount, int* zero_a, int* zero_b, int* zero_c,
                                                       int* bucket_cnt, int* bucket_list, int cap, int* fetch,
                                                       unsigned long long* cnt) {
@@ -638,7 +639,7 @@ __global__ void k_shadow(DevScene S, const int* __restrict__ list, const int* co
 // slowest ray of its warp ends (persistent threads with ray replacement).  Same per-ray traversal
 // as trace_any_bvh4, so the same rays are occluded.
 template <bool COUNT>
-__global__ void __launch_bounds__(128, C2G_SHADOW_MIN_BLOCKS) k_shadow_fetch(DevScene S, const int* __restrict__ list, const int* count,
+__global__ void __launch_bounds__(256, C2G_SHADOW_MIN_BLOCKS) k_shadow_fetch(DevScene S, const int* __restrict__ list, const int* count,
                                                       const float4* __restrict__ so, const float4* __restrict__ sd,
                                                       float4* sc, int* fetch, unsigned long long* cnt) {
     const int n = *count;
@@ -1088,27 +1089,45 @@ int GpuScene::film_download(float* rgb_sum, float* weight, float* rgb_sumsq, std
 }
 
 namespace {
-int g_raygen = 0, g_ext = 0, g_ext_c = 0, g_shade = 0, g_sh = 0, g_sh_c = 0, g_mis = 0, g_mis_c = 0, g_acc = 0, g_film = 0;
-int g_shf = 0, g_shf_c = 0, g_exf = 0, g_exf_c = 0;
+int g_raygen = 0, g_shade = 0, g_acc = 0, g_film = 0;
+// Persistent grids of the traversal kernels for one block size (64, 128 or 256 threads).
+struct TraceGrids {
+    int ext, ext_c, sh, sh_c, shf, shf_c, exf, exf_c, mis, mis_c;
+};
+TraceGrids g_trace[3] = {};
+int trace_block_index(int threads) { return threads <= 64 ? 0 : (threads <= 128 ? 1 : 2); }
 void ensure_grids() {
     if (g_raygen) return;
     g_raygen = grid_for((const void*)k_raygen, 256);
-    g_ext = grid_for((const void*)k_extend<false>, 128);
-    g_ext_c = grid_for((const void*)k_extend<true>, 128);
     g_shade = grid_for((const void*)k_shade<MAT_DIFFUSE, false>, 128);
-    g_sh = grid_for((const void*)k_shadow<false>, 128);
-    g_sh_c = grid_for((const void*)k_shadow<true>, 128);
-    g_shf = grid_for((const void*)k_shadow_fetch<false>, 128);
-    g_shf_c = grid_for((const void*)k_shadow_fetch<true>, 128);
-    g_exf = grid_for((const void*)k_extend_fetch<false>, 128);
-    g_exf_c = grid_for((const void*)k_extend_fetch<true>, 128);
-    g_mis = grid_for((const void*)k_mis<false>, 128);
-    g_mis_c = grid_for((const void*)k_mis<true>, 128);
     g_acc = grid_for((const void*)k_accumulate, 256);
     g_film = grid_for((const void*)k_film, 256);
+    for (int i = 0; i < 3; i++) {
+        const int tb = 64 << i;
+        TraceGrids& g = g_trace[i];
+        g.ext = grid_for((const void*)k_extend<false>, tb);
+        g.ext_c = grid_for((const void*)k_extend<true>, tb);
+        g.sh = grid_for((const void*)k_shadow<false>, tb);
+        g.sh_c = grid_for((const void*)k_shadow<true>, tb);
+        g.shf = grid_for((const void*)k_shadow_fetch<false>, tb);
+        g.shf_c = grid_for((const void*)k_shadow_fetch<true>, tb);
+        g.exf = grid_for((const void*)k_extend_fetch<false>, tb);
+        g.exf_c = grid_for((const void*)k_extend_fetch<true>, tb);
+        g.mis = grid_for((const void*)k_mis<false>, tb);
+        g.mis_c = grid_for((const void*)k_mis<true>, tb);
+    }
 }
 
 __global__ void k_advance(int* sample0, int by) { *sample0 += by; }
+__global__ void k_set_int(int* dst, int v) { *dst = v; }
+// The last kernel of a device-side wave loop: advance the sample counter and keep looping while
+// samples of the job remain.
+__global__ void k_advance_loop(int* sample0, int by, int end, cudaGraphConditionalHandle h) {
+    *sample0 += by;
+    cudaGraphSetConditional(h, *sample0 < end ? 1u : 0u);
+}
+// statistics: *total += *count (paths entering a bounce level)
+__global__ void k_level_add(int* total, const int* count) { *total += *count; }
 }  // namespace
 
 size_t GpuScene::default_wave_paths(int K, const DeviceArena& arena) const {
@@ -1179,7 +1198,8 @@ int GpuScene::prepare(const c2g_render_params& p, DeviceArena& arena, WavePlan& 
              (wb_->sh_o = (float4*)A(PK * 16)) && (wb_->sh_d = (float4*)A(PK * 16)) && (wb_->sh_c = (float4*)A(PK * 16)) &&
              (wb_->mis_o = (float4*)A(P * 16)) && (wb_->mis_d = (float4*)A(P * 16)) && (wb_->mis_c = (float4*)A(PK * 16)) &&
              (wb_->mis_hit = (float4*)A(P * 16)) && (wb_->sh_list = (int*)A(PK * 4)) && (wb_->mis_list = (int*)A(P * 4)) &&
-             (wb_->bucket_list = (int*)A(P * 4 * kBuckets)) && (wb_->counters = (int*)A(256));
+             (wb_->bucket_list = (int*)A(P * 4 * kBuckets)) && (wb_->counters = (int*)A(256)) &&
+             (wb_->levels = (int*)A(4 * C2G_LEVELS));
         if (!ok) {
             for (void* q : wb_->owned) arena.free(q);
             wb_->owned.clear();
@@ -1200,13 +1220,15 @@ int GpuScene::prepare(const c2g_render_params& p, DeviceArena& arena, WavePlan& 
 // Enqueue one wave (a.wave_samples samples of every pixel slot) on st: raygen, the bounce levels,
 // the film and (guided) a training step.  begin/end bracket every launch (timing hooks).
 int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideView& gv, bool count, cudaStream_t st,
-                           const std::function<void(int)>& begin, const std::function<void()>& end, int& launches,
-                           std::string& err) {
+                           const std::function<void(int, cudaStream_t)>& begin, const std::function<void(cudaStream_t)>& end,
+                           int& launches, std::string& err, bool advance) {
     const DevScene& S = plan.S;
     const bool guided = plan.guided;
     WaveBuffers& w = *wb_;
     unsigned long long* cnt = sb_->counts;
     launches = 0;
+    const int tb = 64 << trace_block_index(trace_block_);
+    const TraceGrids& TG = g_trace[trace_block_index(trace_block_)];
     const bool overlap = overlap_ && side_stream(err) == C2G_OK;
     // fork: the side stream waits for everything enqueued on st so far; join: st waits for the side
     auto fork = [&](int k) {
@@ -1220,9 +1242,9 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
     int* C = w.counters;
     C2G_CUDA(cudaMemsetAsync(C, 0, 256, st));
     PathRefs buf[2] = {{w.o[0], w.d[0], w.beta[0], w.L[0]}, {w.o[1], w.d[1], w.beta[1], w.L[1]}};
-    begin(C2G_K_RAYGEN);
+    begin(C2G_K_RAYGEN, st);
     k_raygen<<<g_raygen, 256, 0, st>>>(S, a, buf[0], w.out_L, C + 0);
-    end();
+    end(st);
     int cur = 0;
     for (int b = 0; b < plan.levels; b++) {
         int nxt = cur ^ 1;
@@ -1233,31 +1255,33 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
             C2G_CUDA(cudaStreamSynchronize(st));
             if (qn == 0) break;
         }
-        begin(C2G_K_EXTEND);
+        // statistics: the paths entering this level
+        if (count) k_level_add<<<1, 1, 0, st>>>(w.levels + std::min(b, C2G_LEVELS - 1), C + cur);
+        begin(C2G_K_EXTEND, st);
         // bucket sizes and the extension fetch counter C[5] start at zero on every level
         cudaMemsetAsync(C + 5, 0, sizeof(int) * (kCntBucket - 5 + kBuckets), st);
         if (S.tree == C2G_TREE_SAH && S.sah_width == 4) {
             if (count)
-                k_extend_fetch<true><<<g_exf_c, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
+                k_extend_fetch<true><<<TG.exf_c, tb, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
                                                               C + kCntBucket, w.bucket_list, (int)w.P, C + 5, cnt);
             else
-                k_extend_fetch<false><<<g_exf, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
+                k_extend_fetch<false><<<TG.exf, tb, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
                                                                C + kCntBucket, w.bucket_list, (int)w.P, C + 5, cnt);
         } else if (count) {
-            k_extend<true><<<g_ext_c, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
+            k_extend<true><<<TG.ext_c, tb, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
                                                     C + kCntBucket, w.bucket_list, (int)w.P, cnt);
         } else {
-            k_extend<false><<<g_ext, 128, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
+            k_extend<false><<<TG.ext, tb, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
                                                      C + kCntBucket, w.bucket_list, (int)w.P, cnt);
         }
-        end();
+        end(st);
         // the guide serves the first guide_levels_ bounce levels; deeper vertices shade plainly
         const bool glevel = guided && (guide_levels_ <= 0 || b < guide_levels_);
         if (gv.sample && glevel) {
-            begin(C2G_K_GUIDE);
+            begin(C2G_K_GUIDE, st);
             launches += guide_.infer(st, &S, buf[cur].o, buf[cur].d, w.hit, C + kCntBucket, w.bucket_list, (int)w.P,
                                      present_buckets_);
-            end();
+            end(st);
         }
         ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc, w.mis_hit};
         // the material buckets are independent (they append to the shared queues with atomics):
@@ -1266,10 +1290,10 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
         int nb = 0;
         for (int bk = 0; bk < kBuckets; bk++) {
             if (!(present_buckets_ & (1 << bk))) continue;
-            begin(C2G_K_SHADE);
-            launch_shade(bk, g_shade, (overlap && (nb & 1)) ? side_ : st, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list,
-                         (int)w.P, so, gv, glevel);
-            end();
+            const cudaStream_t ss = (overlap && (nb & 1)) ? side_ : st;
+            begin(C2G_K_SHADE, ss);
+            launch_shade(bk, g_shade, ss, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so, gv, glevel);
+            end(ss);
             launches++;
             nb++;
         }
@@ -1278,48 +1302,48 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
         // and outputs; both must finish before k_accumulate
         if (overlap) {
             fork(1);
-            begin(C2G_K_MIS);  // counts the launch (no timing events while overlapping)
-            if (count) k_mis<true><<<g_mis_c, 128, 0, side_>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
-            else k_mis<false><<<g_mis, 128, 0, side_>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
-            end();
+            begin(C2G_K_MIS, side_);
+            if (count) k_mis<true><<<TG.mis_c, tb, 0, side_>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
+            else k_mis<false><<<TG.mis, tb, 0, side_>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
+            end(side_);
         }
-        begin(C2G_K_SHADOW);
+        begin(C2G_K_SHADOW, st);
         if (S.tree == C2G_TREE_SAH && S.sah_width == 4) {
             // four-wide nodes: the dynamic-fetch kernel (fetch counter C[4], zeroed by k_extend)
-            if (count) k_shadow_fetch<true><<<g_shf_c, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, C + 4, cnt);
-            else k_shadow_fetch<false><<<g_shf, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, C + 4, cnt);
+            if (count) k_shadow_fetch<true><<<TG.shf_c, tb, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, C + 4, cnt);
+            else k_shadow_fetch<false><<<TG.shf, tb, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, C + 4, cnt);
         } else if (count) {
-            k_shadow<true><<<g_sh_c, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
+            k_shadow<true><<<TG.sh_c, tb, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
         } else {
-            k_shadow<false><<<g_sh, 128, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
+            k_shadow<false><<<TG.sh, tb, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
         }
-        end();
+        end(st);
         if (overlap) {
             join(1);
         } else {
-            begin(C2G_K_MIS);
-            if (count) k_mis<true><<<g_mis_c, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
-            else k_mis<false><<<g_mis, 128, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
-            end();
+            begin(C2G_K_MIS, st);
+            if (count) k_mis<true><<<TG.mis_c, tb, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
+            else k_mis<false><<<TG.mis, tb, 0, st>>>(S, w.mis_list, C + 3, w.mis_o, w.mis_d, w.mis_hit, cnt);
+            end(st);
         }
-        begin(C2G_K_ACCUM);
+        begin(C2G_K_ACCUM, st);
         k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.mis_hit, w.out_L, C + cur, gv);
-        end();
+        end(st);
         launches += 4;
         cur = nxt;
     }
-    begin(C2G_K_FILM);
+    begin(C2G_K_FILM, st);
     k_film<<<g_film, 256, 0, st>>>(a, w.out_L, sb_->film, sb_->film_m2);
-    end();
+    end(st);
     launches += 2;
     if (guided) {
         // online training on this wave's recorded vertices (batch build, fused fwd/bwd, Adam)
-        begin(C2G_K_TRAIN);
+        begin(C2G_K_TRAIN, st);
         guide_.train(st, w.out_L, a.nslots * a.wave_samples, guide_train_steps_, S.err);
-        end();
+        end(st);
         launches += 1 + 3 * guide_train_steps_;
     }
-    if (a.sample0_dev) {
+    if (a.sample0_dev && advance) {
         k_advance<<<1, 1, 0, st>>>(const_cast<int*>(a.sample0_dev), a.wave_samples);
         launches++;
     }
@@ -1342,31 +1366,39 @@ int GpuScene::set_wave_counter(int sample, cudaStream_t st, DeviceArena& arena, 
     return C2G_OK;
 }
 
-int GpuScene::capture_wave(const c2g_render_params& p, bool guide_sample, cudaStream_t st, DeviceArena& arena,
-                           cudaGraphExec_t* exec, int* wave_samples, std::string& err) {
+// Shared set-up of the captured waves: plan, device sample counter, guide view; one stream.
+int GpuScene::capture_plan(const c2g_render_params& p, bool guide_sample, cudaStream_t st, DeviceArena& arena, WavePlan& plan,
+                           GuideView& gv, std::string& err) {
     if (p.integrator == C2G_INTEGRATOR_DIRECT) {
         err = "batched rendering runs the path tracers (the direct lighting walk synchronises)";
         return C2G_ERR_UNSUPPORTED;
     }
-    WavePlan plan;
     int rc = prepare(p, arena, plan, err);
     if (rc) return rc;
     rc = set_wave_counter(p.sample_begin, st, arena, err);
     if (rc) return rc;
     guide_.prepare_launch();
-    WaveArgs a = plan.a;
-    a.wave_samples = plan.spw;
-    a.sample0 = 0;
-    a.sample0_dev = wave_counter_;
-    const GuideView gv = plan.guided ? guide_.view(true, guide_sample) : GuideView{};
-    auto no_begin = [](int) {};
-    auto no_end = []() {};
-    // batched jobs already overlap across streams; the side-stream branches inside each graph
-    // measured slower there (64-job batch: 770 vs 872 Mpaths/s), so graphs keep one stream
+    plan.a.wave_samples = plan.spw;
+    plan.a.sample0 = 0;
+    plan.a.sample0_dev = wave_counter_;
+    gv = plan.guided ? guide_.view(true, guide_sample) : GuideView{};
+    // batched jobs already overlap each other; the side-stream branches inside each graph measured
+    // slower there (64-job batch: 770 vs 872 Mpaths/s), so graphs keep one stream
     overlap_ = false;
+    return C2G_OK;
+}
+
+int GpuScene::capture_wave(const c2g_render_params& p, bool guide_sample, cudaStream_t st, DeviceArena& arena,
+                           cudaGraphExec_t* exec, int* wave_samples, std::string& err) {
+    WavePlan plan;
+    GuideView gv;
+    int rc = capture_plan(p, guide_sample, st, arena, plan, gv, err);
+    if (rc) return rc;
+    auto no_begin = [](int, cudaStream_t) {};
+    auto no_end = [](cudaStream_t) {};
     C2G_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
     int launches = 0;
-    rc = enqueue_wave(plan, a, gv, false, st, no_begin, no_end, launches, err);
+    rc = enqueue_wave(plan, plan.a, gv, false, st, no_begin, no_end, launches, err);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     if (rc || e != cudaSuccess) {
@@ -1381,6 +1413,85 @@ int GpuScene::capture_wave(const c2g_render_params& p, bool guide_sample, cudaSt
     return C2G_OK;
 }
 
+int GpuScene::capture_wave_loop(const c2g_render_params& p, bool guide_sample, cudaGraph_t body, cudaGraphConditionalHandle h,
+                                int end_sample, cudaStream_t st, DeviceArena& arena, int* wave_samples, std::string& err) {
+    WavePlan plan;
+    GuideView gv;
+    int rc = capture_plan(p, guide_sample, st, arena, plan, gv, err);
+    if (rc) return rc;
+    auto no_begin = [](int, cudaStream_t) {};
+    auto no_end = [](cudaStream_t) {};
+    C2G_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    int launches = 0;
+    rc = enqueue_wave(plan, plan.a, gv, false, st, no_begin, no_end, launches, err, false);
+    if (!rc) k_advance_loop<<<1, 1, 0, st>>>(wave_counter_, plan.spw, end_sample, h);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc) return rc;
+    if (e != cudaSuccess) { err = std::string("stream capture: ") + cudaGetErrorString(e); return C2G_ERR_CUDA; }
+    *wave_samples = plan.spw;
+    return C2G_OK;
+}
+
+void GpuScene::set_trace_block(int threads) { trace_block_ = 64 << trace_block_index(threads); }
+
+int GpuScene::append_job(cudaGraph_t G, const cudaGraphNode_t* deps, int ndeps, const c2g_render_params& p, int wave_paths,
+                         cudaEvent_t done, cudaStream_t st, DeviceArena& arena, int* spw, int* waves, std::string& err) {
+    const int nslots = ((p.width + 7) / 8) * ((p.height + 7) / 8) * 64;
+    // samples per wave: as many as the wave size holds, dividing the job's sample count
+    int s = std::max(1, std::min(p.sample_count, wave_paths / nslots));
+    while (p.sample_count % s) s--;
+    c2g_render_params q = p;
+    q.wave_paths = s * nslots;
+    const bool guided = q.integrator == C2G_INTEGRATOR_GUIDED;
+    const int n_waves = p.sample_count / s;
+    const int warm = guided ? std::min(n_waves, guide_warmup_) : 0;
+    // the counter reset (its address exists once the plan is prepared)
+    {
+        WavePlan plan;
+        int rc = prepare(q, arena, plan, err);
+        if (rc) return rc;
+        rc = set_wave_counter(p.sample_begin, st, arena, err);
+        if (rc) return rc;
+    }
+    cudaGraphNode_t prev = nullptr;
+    {
+        int* counter = wave_counter_;
+        int value = p.sample_begin;
+        void* args[] = {&counter, &value};
+        cudaKernelNodeParams kp{};
+        kp.func = (void*)k_set_int;
+        kp.gridDim = dim3(1);
+        kp.blockDim = dim3(1);
+        kp.kernelParams = args;
+        C2G_CUDA(cudaGraphAddKernelNode(&prev, G, deps, ndeps, &kp));
+    }
+    // one while loop per wave kind: the guided integrator's first waves only train
+    for (int part = 0; part < 2; part++) {
+        const int loop_waves = part == 0 ? warm : n_waves - warm;
+        if (loop_waves <= 0) continue;
+        cudaGraphConditionalHandle h;
+        C2G_CUDA(cudaGraphConditionalHandleCreate(&h, G, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        C2G_CUDA(cudaGraphAddNode(&node, G, &prev, nullptr, 1, &np));
+        const int end = p.sample_begin + (part == 0 ? warm : n_waves) * s;
+        int got = 0;
+        int rc = capture_wave_loop(q, part == 1, np.conditional.phGraph_out[0], h, end, st, arena, &got, err);
+        if (rc) return rc;
+        prev = node;
+    }
+    cudaGraphNode_t ev;
+    C2G_CUDA(cudaGraphAddEventRecordNode(&ev, G, &prev, 1, done));
+    *spw = s;
+    *waves = n_waves;
+    return C2G_OK;
+}
+
 int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_t st, DeviceArena& arena, std::string& err) {
     (void)s;
     WavePlan plan;
@@ -1389,17 +1500,28 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
     const bool guided = plan.guided;
     const bool count = (counting_ & C2G_COUNT_TRAVERSAL) != 0;
     const bool timing = (counting_ & C2G_COUNT_TIMING) != 0;
-    overlap_ = !timing;  // per-kernel timing events need one stream
+    overlap_ = true;  // timing events are recorded on the stream each kernel runs on
     unsigned long long* cnt = sb_->counts;
-    if (count) C2G_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 3 * C2G_K_KINDS, st));
+    if (count) {
+        C2G_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 3 * C2G_K_KINDS, st));
+        C2G_CUDA(cudaMemsetAsync(wb_->levels, 0, sizeof(int) * C2G_LEVELS, st));
+    }
     // per-launch events (timing mode): a pool reused across calls
     struct Ev { cudaEvent_t a, b; int kind; };
     static std::vector<Ev> pool;
     size_t used = 0;
     int kcount[C2G_K_KINDS] = {};
-    auto begin = [&](int kind) {
+    // per-level time: from one extension launch's begin event to the next one (or to the film)
+    std::vector<std::pair<size_t, int>> level_marks;  // (pool index, level)
+    int level = 0;
+    auto begin = [&](int kind, cudaStream_t ks) {
         kcount[kind]++;
         if (!timing) return;
+        if (kind == C2G_K_EXTEND) level_marks.push_back({used, level++});
+        else if (kind == C2G_K_FILM || kind == C2G_K_RAYGEN) {
+            if (kind == C2G_K_FILM) level_marks.push_back({used, -1});  // end of the wave's levels
+            level = 0;
+        }
         if (used == pool.size()) {
             Ev e{};
             cudaEventCreate(&e.a);
@@ -1407,11 +1529,11 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
             pool.push_back(e);
         }
         pool[used].kind = kind;
-        cudaEventRecord(pool[used].a, st);
+        cudaEventRecord(pool[used].a, ks);
     };
-    auto end = [&]() {
+    auto end = [&](cudaStream_t ks) {
         if (!timing) return;
-        cudaEventRecord(pool[used].b, st);
+        cudaEventRecord(pool[used].b, ks);
         used++;
     };
     cudaEvent_t ev0, ev1;
@@ -1450,7 +1572,17 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
         cudaEventElapsedTime(&t, pool[i].a, pool[i].b);
         stats_.kernel_ms[pool[i].kind] += t;
     }
+    for (size_t i = 0; i + 1 < level_marks.size(); i++) {
+        if (level_marks[i].second < 0) continue;
+        float t = 0.f;
+        cudaEventElapsedTime(&t, pool[level_marks[i].first].a, pool[level_marks[i + 1].first].a);
+        stats_.level_ms[std::min(level_marks[i].second, C2G_LEVELS - 1)] += t;
+        stats_.levels = std::max(stats_.levels, level_marks[i].second + 1);
+    }
     if (count) {
+        int lv[C2G_LEVELS];
+        C2G_CUDA(cudaMemcpy(lv, wb_->levels, sizeof(lv), cudaMemcpyDeviceToHost));
+        for (int l = 0; l < C2G_LEVELS; l++) stats_.level_paths[l] = lv[l];
         unsigned long long h[3 * C2G_K_KINDS];
         C2G_CUDA(cudaMemcpy(h, cnt, sizeof(h), cudaMemcpyDeviceToHost));
         for (int k = 0; k < C2G_K_KINDS; k++) {

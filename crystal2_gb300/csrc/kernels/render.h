@@ -106,19 +106,39 @@ public:
     // the samples one launch renders in *wave_samples.
     int capture_wave(const c2g_render_params& p, bool guide_sample, cudaStream_t st, DeviceArena& arena,
                      cudaGraphExec_t* exec, int* wave_samples, std::string& err);
+    // Record one wave of p into `body`, the body graph of a conditional while node of a larger
+    // graph: the wave's kernels (as capture_wave), then one kernel that advances the device sample
+    // counter by the wave's samples and sets the loop's condition `h` to (counter < end_sample), so
+    // the loop renders wave after wave on the device.  Returns the samples per wave.
+    int capture_wave_loop(const c2g_render_params& p, bool guide_sample, cudaGraph_t body, cudaGraphConditionalHandle h,
+                          int end_sample, cudaStream_t st, DeviceArena& arena, int* wave_samples, std::string& err);
+    // Append this scene's job (render parameters p, waves of up to wave_paths paths) to graph G as
+    // one chain: a kernel that resets the device sample counter to p.sample_begin, a device-side
+    // loop over the guided integrator's training-only waves, a loop over the remaining waves, and an
+    // event record node on `done`.  The chain depends on deps[0..ndeps).  *spw / *waves: samples per
+    // wave and the job's wave count.
+    int append_job(cudaGraph_t G, const cudaGraphNode_t* deps, int ndeps, const c2g_render_params& p, int wave_paths,
+                   cudaEvent_t done, cudaStream_t st, DeviceArena& arena, int* spw, int* waves, std::string& err);
     // Device counter the captured graphs read their first sample index from.
     int set_wave_counter(int sample, cudaStream_t st, DeviceArena& arena, std::string& err);
+    int* wave_counter() const { return wave_counter_; }
+    // Threads per block of the traversal kernels (64, 128 or 256); taken by the next render or capture.
+    void set_trace_block(int threads);
+    int trace_block() const { return trace_block_; }
     int guide_warmup() const { return guide_warmup_; }
 
 private:
     int prepare(const c2g_render_params& p, DeviceArena& arena, WavePlan& plan, std::string& err);
     size_t default_wave_paths(int K, const DeviceArena& arena) const;
     int enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideView& gv, bool count, cudaStream_t st,
-                     const std::function<void(int)>& begin, const std::function<void()>& end, int& launches,
-                     std::string& err);
+                     const std::function<void(int, cudaStream_t)>& begin, const std::function<void(cudaStream_t)>& end,
+                     int& launches, std::string& err, bool advance = true);
+    int capture_plan(const c2g_render_params& p, bool guide_sample, cudaStream_t st, DeviceArena& arena, WavePlan& plan,
+                     GuideView& gv, std::string& err);
     DeviceSceneBuffers* sb_;
     int* wave_counter_ = nullptr;  // device sample index of captured wave graphs
     int sah_width_ = 4;            // SAH traversal variant (2 or 4 children per node)
+    int trace_block_ = 128;        // threads per block of the traversal kernels
     WaveBuffers* wb_;
     int counting_ = 0;
     int present_buckets_ = 0;  // material buckets the loaded scene can produce

@@ -247,8 +247,9 @@ class Context:
 
 
 class Batch:
-    """Many jobs (contexts with loaded scenes + render parameters) rendered together on one GPU
-    through replayed CUDA graphs on concurrent streams (c2g_batch_* in include/c2g.h)."""
+    """Many jobs (contexts with loaded scenes + render parameters) rendered together on one GPU:
+    one graph launch with device-side wave loops per job, or per-job graphs on concurrent streams
+    (c2g_batch_* in include/c2g.h)."""
 
     def __init__(self, device: int = 0):
         self._lib = N.load_library()
@@ -281,6 +282,24 @@ class Batch:
         sn = np.ascontiguousarray(streams, np.int32)
         best = C.c_double(0.0)
         rc = self._lib.c2g_batch_autotune(self._h, N.iptr(wp), wp.size, N.iptr(sn), sn.size, int(trial_spp), C.byref(best))
+        if rc:
+            self._raise(rc)
+        return best.value
+
+    def set_trace(self, traversal: int, trace_block: int) -> None:
+        rc = self._lib.c2g_batch_set_trace(self._h, int(traversal), int(trace_block))
+        if rc:
+            self._raise(rc)
+
+    def search(self, wave_paths=(1 << 19, 1 << 20, 1 << 21, 1 << 22), streams=(0, 8), traversal=(4, 2),
+               trace_block=(128, 64, 256), trial_spp: int = 4) -> float:
+        """Coordinate search over wave size, mode (0 = one graph launch), traversal variant and the
+        traversal kernels' block size; returns the best trial rate (Mpaths/s)."""
+        arrs = [np.ascontiguousarray(v, np.int32) for v in (wave_paths, streams, traversal, trace_block)]
+        sp = N.BatchSpace(N.iptr(arrs[0]), arrs[0].size, N.iptr(arrs[1]), arrs[1].size, N.iptr(arrs[2]), arrs[2].size,
+                          N.iptr(arrs[3]), arrs[3].size)
+        best = C.c_double(0.0)
+        rc = self._lib.c2g_batch_search(self._h, C.byref(sp), int(trial_spp), C.byref(best))
         if rc:
             self._raise(rc)
         return best.value

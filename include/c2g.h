@@ -95,6 +95,8 @@ typedef struct {
 #define C2G_COUNT_TRAVERSAL 1  /* rays, nodes visited and prims tested per traversal kernel */
 #define C2G_COUNT_TIMING 2     /* CUDA events around every launch; per-kind device time */
 
+#define C2G_LEVELS 64  /* size of the per-bounce-level arrays (deeper levels add to the last entry) */
+
 typedef struct {
     double seconds;             /* device time of the last c2g_render (CUDA events on its stream) */
     double paths;               /* camera paths traced by the last c2g_render */
@@ -105,6 +107,9 @@ typedef struct {
     int kernel_count[C2G_K_KINDS];        /* launches per kernel kind */
     int kernel_launches;        /* kernels launched by the last c2g_render */
     int waves;                  /* waves of the last c2g_render */
+    double level_ms[C2G_LEVELS];    /* device time per bounce level, summed over waves (C2G_COUNT_TIMING) */
+    double level_paths[C2G_LEVELS]; /* paths entering each bounce level, summed over waves (C2G_COUNT_TRAVERSAL) */
+    int levels;                 /* bounce levels run by the deepest wave */
 } c2g_stats;
 
 /* ---- lifecycle ------------------------------------------------------------------------------ */
@@ -186,23 +191,33 @@ int c2g_probe_l2_read(int device, size_t bytes, int reps, double* gbs);
 /* ---- batched multi-job rendering ---------------------------------------------------------------
  * No counterpart in the reference (one scene per RayTracer).  A batch renders many jobs - each a
  * context with its own loaded scene and its own render parameters (path tracer or guided) - on one
- * GPU: every job's wave is captured once as a CUDA graph that replays wave after wave, the jobs
- * are spread over concurrent streams (longest-first onto the least-loaded stream, shortest-first
- * within a stream), and the films land in each job's context (c2g_film_download).  The wave size
- * and the stream count come from c2g_batch_tune or c2g_batch_autotune.  Jobs' contexts must live
- * as long as the batch; a context belongs to at most one batch. */
+ * GPU, and the films land in each job's context (c2g_film_download).  Two modes:
+ *  - streams = 0 (default): the whole batch is one CUDA graph launched once; per job a chain of a
+ *    sample-counter reset, device-side while loops (conditional graph nodes) that run the job's
+ *    waves one after another, and a completion event; the jobs' chains are independent, so the
+ *    GPU interleaves them;
+ *  - streams = S > 0: every job's wave is captured as its own graph that replays wave after wave,
+ *    jobs spread over S concurrent streams (longest-first onto the least-loaded stream,
+ *    shortest-first within a stream).
+ * The wave size, the mode, the traversal variant and the traversal kernels' block size come from
+ * c2g_batch_tune / c2g_batch_set_trace or the autotuners.  Jobs' contexts must live as long as the
+ * batch; a context belongs to at most one batch. */
 typedef struct c2g_batch c2g_batch;
 typedef struct c2g_batch_stats {
     int jobs;
     double paths;               /* camera paths rendered by the run */
     double seconds;             /* device time from the first launch to the last job's end */
     double mpaths_per_s;
-    double latency_p50_ms;      /* job completion times from the batch start */
+    double latency_p50_ms;      /* job completion times from the batch start (nearest rank) */
     double latency_p99_ms;
     double latency_max_ms;
     int wave_paths;             /* configuration the run used */
     int streams;
     int graph_launches;
+    double latency_p90_ms;
+    double latency_mean_ms;
+    int traversal;              /* SAH node width of the run */
+    int trace_block;            /* threads per block of the traversal kernels */
 } c2g_batch_stats;
 int c2g_batch_create(c2g_batch** out, int device);
 void c2g_batch_destroy(c2g_batch* b);
@@ -210,10 +225,29 @@ const char* c2g_batch_last_error(c2g_batch* b);
 /* Add a job: params->sample_count samples from params->sample_begin; *index = its job index. */
 int c2g_batch_add(c2g_batch* b, c2g_ctx* job, const c2g_render_params* params, int* index);
 /* Fix the configuration: paths per wave (rounded per job so that a wave holds whole samples that
- * divide the job's sample count) and concurrent streams (1..32). */
+ * divide the job's sample count) and the mode: 0 = one graph launch, 1..32 concurrent streams. */
 int c2g_batch_tune(c2g_batch* b, int wave_paths, int streams);
+/* Traversal variant of every job (SAH node width 2 or 4) and threads per block of the traversal
+ * kernels (64, 128 or 256). */
+int c2g_batch_set_trace(c2g_batch* b, int traversal, int trace_block);
+/* Candidate values per dimension of the batch configuration (n_x = 0: keep the current value). */
+typedef struct {
+    const int* wave_paths;
+    int n_wave_paths;
+    const int* streams;         /* 0 = one graph launch */
+    int n_streams;
+    const int* traversal;       /* 2 or 4 */
+    int n_traversal;
+    const int* trace_block;     /* 64, 128, 256 */
+    int n_trace_block;
+} c2g_batch_space;
+/* Coordinate search: starting from the current configuration, each dimension in turn (wave size,
+ * mode, traversal variant, block size) takes its candidate with the best aggregate rate on a trial
+ * pass of every job (trial_spp samples each); films and networks are reset afterwards. */
+int c2g_batch_search(c2g_batch* b, const c2g_batch_space* space, int trial_spp, double* best_mpaths_per_s);
 /* Time each (wave_paths, streams) pair of the candidate lists on a short trial of every job
- * (trial_spp samples each, films and networks reset afterwards), keep the fastest. */
+ * (trial_spp samples each, films and networks reset afterwards), keep the fastest (an exhaustive
+ * search over two dimensions; c2g_batch_search covers all four). */
 int c2g_batch_autotune(c2g_batch* b, const int* wave_paths, int n_wave_paths, const int* streams, int n_streams,
                        int trial_spp, double* best_mpaths_per_s);
 /* Render every job once (films accumulate; clear them with c2g_film_clear between runs). */

@@ -1,5 +1,6 @@
-"""Batched multi-job rendering (c2g_batch_*): replayed wave graphs on concurrent streams render the
-same films as one-job-at-a-time c2g_render calls with the same wave size."""
+"""Batched multi-job rendering (c2g_batch_*): the whole batch as one graph launch with device-side
+wave loops, and replayed per-job wave graphs on concurrent streams, render the same films as
+one-job-at-a-time c2g_render calls with the same wave size."""
 import numpy as np
 import pytest
 
@@ -38,7 +39,8 @@ def _solo(ctx, p, wave_paths):
     return ctx.film()
 
 
-def test_batch_matches_individual_renders(tmp_path):
+@pytest.mark.parametrize("streams", [2, 0])
+def test_batch_matches_individual_renders(tmp_path, streams):
     jobs = [_job(tmp_path, "c1", scenes.cornell, N.INTEGRATOR_PATH, 16, width=32, height=32),
             _job(tmp_path, "c2", scenes.cornell, N.INTEGRATOR_PATH, 12, width=40, height=24),
             _job(tmp_path, "mb", scenes.material_box, N.INTEGRATOR_PATH, 8, width=48, height=48)]
@@ -48,11 +50,13 @@ def test_batch_matches_individual_renders(tmp_path):
     for c, p in jobs:
         c.film_clear()
         b.add(c, p)
-    b.tune(wave_paths, 2)
+    b.tune(wave_paths, streams)
     st = b.run()
     assert st.jobs == 3
     assert st.paths == sum(p.width * p.height * p.sample_count for _, p in jobs)
-    assert st.graph_launches > 3 and st.streams == 2
+    assert st.streams == streams
+    # one launch for the whole batch, or one per wave
+    assert st.graph_launches == 1 if streams == 0 else st.graph_launches > 3
     for (c, p), (s_ref, w_ref) in zip(jobs, solo):
         s, w = c.film()
         assert np.array_equal(w, w_ref)
@@ -93,10 +97,64 @@ def test_batch_rejects_bad_input(tmp_path):
     with pytest.raises(N.C2GError):
         b.add(c, p)          # a context joins a batch once
     with pytest.raises(N.C2GError):
-        b.tune(1 << 20, 0)   # at least one stream
+        b.tune(1 << 20, -1)  # 0 (one graph launch) or 1..32 streams
+    with pytest.raises(N.C2GError):
+        b.set_trace(3, 128)  # node width 2 or 4
+    with pytest.raises(N.C2GError):
+        b.set_trace(4, 96)   # block of 64, 128 or 256 threads
     q = N.RenderParams.from_buffer_copy(p)
     q.sample_count = 0
     c2, _ = _job(tmp_path, "c2", scenes.cornell, N.INTEGRATOR_PATH, 4, width=16, height=16)
     with pytest.raises(N.C2GError):
         b.add(c2, q)         # a job renders at least one sample
     b.close()
+
+
+def test_batch_search_one_launch_guided(tmp_path):
+    """The coordinate search picks a configuration from every dimension's candidates; the chosen one
+    renders a guided and a plain job in one graph launch, the guided job training inside it."""
+    jobs = [_job(tmp_path, "g", scenes.cornell, N.INTEGRATOR_GUIDED, 32, width=32, height=32),
+            _job(tmp_path, "p", scenes.cornell, N.INTEGRATOR_PATH, 32, width=32, height=32),
+            _job(tmp_path, "m", scenes.material_box, N.INTEGRATOR_PATH, 16, width=24, height=24)]
+    b = Batch(0)
+    for c, p in jobs:
+        c.film_clear()
+        b.add(c, p)
+    best = b.search(wave_paths=(2048, 8192), streams=(0, 2), traversal=(4, 2), trace_block=(128, 64, 256), trial_spp=4)
+    assert best > 0
+    b.tune(8192, 0)  # whatever the search chose, run the one-launch mode with its traversal choice
+    st = b.run()
+    assert st.graph_launches == 1 and st.traversal in (2, 4) and st.trace_block in (64, 128, 256)
+    assert jobs[0][0].guide_stats()[2] > 0
+    for c, p in jobs:
+        s, w = c.film()
+        assert np.all(w == p.sample_count)
+    g = jobs[0][0].image().astype(np.float64)
+    pl = jobs[1][0].image().astype(np.float64)
+    assert abs(g.mean() - pl.mean()) < 0.05 * pl.mean()
+    assert st.latency_p50_ms <= st.latency_p90_ms <= st.latency_max_ms
+    b.close()
+
+
+@pytest.mark.parametrize("traversal,block", [(2, 64), (4, 256)])
+def test_batch_trace_settings_keep_films(tmp_path, traversal, block):
+    """Traversal variant and block size change how rays are traced, not what they hit: the films equal
+    the default configuration's."""
+    ref = None
+    for tv, bl in ((4, 128), (traversal, block)):
+        c, p = _job(tmp_path, f"c{tv}{bl}", scenes.material_box, N.INTEGRATOR_PATH, 8, width=32, height=32)
+        b = Batch(0)
+        c.film_clear()
+        b.add(c, p)
+        b.tune(4096, 0)
+        b.set_trace(tv, bl)
+        b.run()
+        s, w = c.film()
+        b.close()
+        if ref is None:
+            ref = (s, w)
+        else:
+            assert np.array_equal(w, ref[1])
+            # the binary and four-wide trees give the same closest hits up to near-ties
+            close = np.isclose(s, ref[0], rtol=1e-4, atol=1e-6)
+            assert close.mean() > 0.98
