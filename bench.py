@@ -459,8 +459,9 @@ def guided_equal_time(args) -> dict:
     # both arms render 8-sample waves (the guided arm trains after every wave)
     plain = progressive(N.INTEGRATOR_PATH, 8)
     ctx.load(cp, sp, tree=N.TREE_SAH)  # a fresh, untrained network
-    ctx.guide_config(args.guided_lr, args.guided_bsdf_fraction, 2, args.guided_train_steps)
+    ctx.guide_config(args.guided_lr, args.guided_bsdf_fraction, args.guided_warmup, args.guided_train_steps)
     ctx.guide_levels(args.guided_levels)
+    ctx.guide_batch(args.guided_records, args.guided_windows)
     guided = progressive(N.INTEGRATOR_GUIDED, 8)
     target = plain[-1][2]
     reach = None
@@ -477,6 +478,8 @@ def guided_equal_time(args) -> dict:
             "guided": {"spp": guided[-1][1], "s": round(guided[-1][0], 3), "relMSE": guided[-1][2],
                        "bsdf_fraction": args.guided_bsdf_fraction, "learning_rate": args.guided_lr,
                        "train_steps_per_wave": args.guided_train_steps, "samples_per_wave": 8,
+                       "records_per_wave": args.guided_records, "minibatch_windows": args.guided_windows,
+                       "warmup_waves": args.guided_warmup,
                        "guided_levels": args.guided_levels,
                        "adam_steps": steps, "last_batch": records, "last_loss": round(loss, 4)},
             "time_to_plain_relMSE_s": None if reach is None else round(reach, 3),
@@ -517,6 +520,18 @@ def batch_run(args) -> dict:
     tune_s = time.time() - t0
     st = b.run()
     lat = [b.latency_ms(i) for i in range(len(jobs))]
+    one = None
+    if st.streams != 0:
+        # the one-launch mode with the same wave size and traversal, from fresh films and networks
+        for c, (_, _, _, guided) in zip(ctxs, jobs):
+            c.film_clear()
+            if guided:
+                c.guide_reset((0.0, 0.0, 0.0), (1.0, 1.0, 1.0), seed=0)
+        b.tune(st.wave_paths, 0)
+        s1 = b.run()
+        one = {"mpaths_per_s": round(s1.mpaths_per_s, 2), "seconds": round(s1.seconds, 3), "graph_launches": s1.graph_launches,
+               "latency_p50_ms": round(s1.latency_p50_ms, 2), "latency_p90_ms": round(s1.latency_p90_ms, 2),
+               "latency_max_ms": round(s1.latency_max_ms, 2), "latency_mean_ms": round(s1.latency_mean_ms, 2)}
     out = {"jobs": st.jobs, "guided_jobs": n_guided, "paths": st.paths, "seconds": round(st.seconds, 3),
            "mpaths_per_s": round(st.mpaths_per_s, 2), "latency_p50_ms": round(st.latency_p50_ms, 2),
            "latency_p90_ms": round(st.latency_p90_ms, 2), "latency_p99_ms": round(st.latency_p99_ms, 2),
@@ -525,7 +540,7 @@ def batch_run(args) -> dict:
            "tuned": {"wave_paths": st.wave_paths, "mode": "one graph launch" if st.streams == 0 else f"{st.streams} streams",
                      "traversal": f"{st.traversal}-wide nodes", "trace_block": st.trace_block,
                      "trial_mpaths_per_s": round(best, 2), "tune_s": round(tune_s, 2)},
-           "graph_launches": st.graph_launches, "scene_load_s": round(load_s, 1),
+           "graph_launches": st.graph_launches, "one_launch_mode": one, "scene_load_s": round(load_s, 1),
            "resolutions": [int(c.render_params().width) for c in ctxs],
            "latency_ms": [round(x, 2) for x in lat]}
     b.close()
@@ -605,9 +620,12 @@ def main() -> int:
     ap.add_argument("--guided-res", default="1920x1080")
     ap.add_argument("--guided-ref-spp", type=int, default=16384)
     ap.add_argument("--guided-seconds", type=float, default=6.0)
-    ap.add_argument("--guided-lr", type=float, default=2e-3)
+    ap.add_argument("--guided-lr", type=float, default=1e-3)
     ap.add_argument("--guided-bsdf-fraction", type=float, default=0.7)
-    ap.add_argument("--guided-train-steps", type=int, default=16)
+    ap.add_argument("--guided-train-steps", type=int, default=64)
+    ap.add_argument("--guided-records", type=int, default=1 << 20, help="recorded vertices per guided wave")
+    ap.add_argument("--guided-windows", type=int, default=16, help="minibatch windows per guided wave")
+    ap.add_argument("--guided-warmup", type=int, default=1, help="guided waves that only train")
     ap.add_argument("--guided-levels", type=int, default=0, help="bounce levels served by the guide (0 = all)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-job measurement")
     ap.add_argument("--sah-width", type=int, default=4, choices=[2, 4], help="SAH traversal variant")

@@ -24,6 +24,10 @@ def main() -> int:
     ap.add_argument("--waves", type=int, default=6)
     ap.add_argument("--spp-per-wave", type=int, default=16)
     ap.add_argument("--guide-levels", type=int, default=2)
+    ap.add_argument("--train-steps", type=int, default=4, help="Adam steps per guided wave")
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--records", type=int, default=1 << 18, help="recorded vertices per guided wave")
+    ap.add_argument("--windows", type=int, default=4, help="minibatch windows per guided wave")
     ap.add_argument("--range", default="capture")
     args = ap.parse_args()
     W, H = (int(v) for v in args.res.split("x"))
@@ -36,8 +40,9 @@ def main() -> int:
         cp, sp = scenes.cornell(d, width=W, height=H, spp=64)
     ctx = Context(0)
     ctx.load(cp, sp, tree=N.TREE_SAH)
-    ctx.guide_config(2e-3, 0.7, 2, 4)
+    ctx.guide_config(args.lr, 0.7, 2, args.train_steps)
     ctx.guide_levels(args.guide_levels)
+    ctx.guide_batch(args.records, args.windows)
     integ = N.INTEGRATOR_GUIDED if args.integrator == "guided" else N.INTEGRATOR_PATH
     slots = ((W + 7) // 8) * ((H + 7) // 8) * 64
 
