@@ -254,6 +254,7 @@ def run_ours(args) -> None:
     ctx = Context(local)
     t0 = time.time()
     ctx.set_traversal(args.sah_width)
+    ctx.set_trace_block(args.trace_block)
     ctx.load(cp, sp, tree=N.TREE_SAH)
     load_s = time.time() - t0
     p = ctx.render_params()
@@ -397,7 +398,8 @@ def run_ours(args) -> None:
                                parallelism=f"replicas x{world}" if world > 1 else "single GPU",
                                l2="inputs larger than L2 (scene + wave state >> 129 MB); no flush",
                                scene_load_s=round(load_s, 2), scale=args.scale,
-                               traversal=f"{args.sah_width}-wide nodes, while-while with leaf postponing"),
+                               traversal=f"{args.sah_width}-wide nodes, while-while with leaf postponing, "
+                                         f"{args.trace_block}-thread blocks"),
                 "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": C.sizeof(p),
                         "d2h_bytes_per_step": int(p.width * p.height * 16)},
                 "gpu_launches": int(launches), "roofline": roof, "kernel_share": share,
@@ -629,6 +631,7 @@ def main() -> int:
     ap.add_argument("--guided-levels", type=int, default=0, help="bounce levels served by the guide (0 = all)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-job measurement")
     ap.add_argument("--sah-width", type=int, default=4, choices=[2, 4], help="SAH traversal variant")
+    ap.add_argument("--trace-block", type=int, default=128, choices=[64, 128, 256], help="traversal kernels' block size")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0: the library default, 2^21)")
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--no-rays", action="store_true", help="skip the ray-intersection microbench")

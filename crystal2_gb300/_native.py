@@ -116,6 +116,7 @@ SIGNATURES = {
     "c2g_get_stats": (_I, [_P, C.POINTER(Stats)]),
     "c2g_set_counting": (_I, [_P, _I]),
     "c2g_set_traversal": (_I, [_P, _I]),
+    "c2g_set_trace_block": (_I, [_P, _I]),
     "c2g_probe_l2_read": (_I, [_I, C.c_size_t, _I, C.POINTER(C.c_double)]),
     "c2g_trace_rays": (_I, [_P, _I, _FP, _FP, _FP, _FP, _IP, _I, _IP, _FP]),
     "c2g_trace_rays_dev": (_I, [_P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),
@@ -138,6 +139,7 @@ SIGNATURES = {
     "c2g_batch_tune": (_I, [_P, _I, _I]),
     "c2g_batch_autotune": (_I, [_P, _IP, _I, _IP, _I, _I, C.POINTER(C.c_double)]),
     "c2g_batch_set_trace": (_I, [_P, _I, _I]),
+    "c2g_batch_set_lanes": (_I, [_P, _I]),
     "c2g_batch_search": (_I, [_P, C.POINTER(BatchSpace), _I, C.POINTER(C.c_double)]),
     "c2g_batch_run": (_I, [_P, C.POINTER(BatchStats)]),
     "c2g_batch_job_latency": (_I, [_P, _I, C.POINTER(C.c_double)]),

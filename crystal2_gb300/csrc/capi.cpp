@@ -434,6 +434,14 @@ int c2g_set_traversal(c2g_ctx* ctx, int width) {
     return C2G_OK;
 }
 
+int c2g_set_trace_block(c2g_ctx* ctx, int threads) {
+    if (!ctx) return C2G_ERR_INVALID;
+    if (threads != 64 && threads != 128 && threads != 256) return fail(ctx, C2G_ERR_INVALID, "trace block is 64, 128 or 256");
+    if (ctx->host_only) return fail(ctx, C2G_ERR_STATE, "host-only context");
+    ctx->gpu->set_trace_block(threads);
+    return C2G_OK;
+}
+
 int c2g_probe_l2_read(int device, size_t bytes, int reps, double* gbs) {
     if (!gbs) return C2G_ERR_INVALID;
     int ndev = 0;
@@ -646,6 +654,7 @@ struct c2g_batch {
     std::vector<cudaStream_t> streams;
     int wave_paths = 1 << 20;
     int n_streams = 0;          // 0: every job in one graph launch; > 0: per-job graphs on this many streams
+    int lanes = 8;              // one-launch mode: chains of jobs that run side by side (0: every job alone)
     int traversal = 4;          // SAH node width of every job's traversal
     int trace_block = 128;      // threads per block of the traversal kernels
     int captured_wave_paths = -1;
@@ -737,9 +746,27 @@ void fill_stats(c2g_batch* b, std::vector<double> lat, double paths, float total
     out->trace_block = b->trace_block;
 }
 
+// Longest job first onto the least-loaded of n queues, shortest first within a queue (the order of
+// the streams mode and of the one-launch mode's lanes).
+std::vector<std::vector<int>> batch_queues(c2g_batch* b, int n) {
+    std::vector<int> order(b->jobs.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return b->jobs[x].paths() > b->jobs[y].paths(); });
+    std::vector<double> load(n, 0.0);
+    std::vector<std::vector<int>> per(n);
+    for (int i : order) {
+        int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[k] += b->jobs[i].paths();
+        per[k].push_back(i);
+    }
+    for (auto& v : per) std::reverse(v.begin(), v.end());
+    return per;
+}
+
 // Every job in one graph: per job a chain (sample counter reset, device-side while loops over its
-// waves, completion event), the chains independent of each other, so one cudaGraphLaunch renders the
-// whole batch and the GPU interleaves the jobs' kernels.  `spp_limit` caps every job's samples.
+// waves, completion event); the jobs of a lane follow each other (shortest first), the lanes run
+// side by side (lanes = 0: every job on its own), so one cudaGraphLaunch renders the whole batch
+// and the GPU interleaves the lanes' kernels.  `spp_limit` caps every job's samples.
 int batch_pass_graph(c2g_batch* b, int spp_limit, c2g_batch_stats* out) {
     if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "cudaSetDevice failed");
     if (cudaDeviceSynchronize() != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "device error before the batch");
@@ -754,21 +781,30 @@ int batch_pass_graph(c2g_batch* b, int spp_limit, c2g_batch_stats* out) {
     if (cudaGraphCreate(&G, 0) != cudaSuccess) return bfail(b, C2G_ERR_CUDA, "graph creation failed");
     double paths = 0.0;
     int rc = C2G_OK;
-    for (size_t i = 0; i < b->jobs.size() && !rc; i++) {
-        BatchJob& j = b->jobs[i];
-        if (!j.done) cudaEventCreate(&j.done);
-        c2g_render_params q = j.p;
-        if (spp_limit > 0) q.sample_count = std::max(1, std::min(q.sample_count, spp_limit));
-        std::string err;
-        int spw = 0, waves = 0;
-        rc = j.ctx->gpu->append_job(G, nullptr, 0, q, b->wave_paths, j.done, st, *j.ctx->arena, &spw, &waves, err);
-        if (rc) {
-            bfail(b, rc, "job " + std::to_string(i) + ": " + err);
-            break;
+    std::vector<std::vector<int>> lanes;
+    if (b->lanes > 0) lanes = batch_queues(b, std::min<int>(b->lanes, (int)b->jobs.size()));
+    else
+        for (size_t i = 0; i < b->jobs.size(); i++) lanes.push_back({(int)i});
+    for (const auto& lane : lanes) {
+        cudaGraphNode_t prev = nullptr;
+        for (int i : lane) {
+            BatchJob& j = b->jobs[i];
+            if (!j.done) cudaEventCreate(&j.done);
+            c2g_render_params q = j.p;
+            if (spp_limit > 0) q.sample_count = std::max(1, std::min(q.sample_count, spp_limit));
+            std::string err;
+            int spw = 0, waves = 0;
+            rc = j.ctx->gpu->append_job(G, prev ? &prev : nullptr, prev ? 1 : 0, q, b->wave_paths, j.done, st, *j.ctx->arena,
+                                        &prev, &spw, &waves, err);
+            if (rc) {
+                bfail(b, rc, "job " + std::to_string(i) + ": " + err);
+                break;
+            }
+            j.spw = spw;
+            j.waves = waves;
+            paths += (double)q.width * q.height * q.sample_count;
         }
-        j.spw = spw;
-        j.waves = waves;
-        paths += (double)q.width * q.height * q.sample_count;
+        if (rc) break;
     }
     cudaGraphExec_t exec = nullptr;
     if (!rc) {
@@ -822,17 +858,7 @@ int batch_pass(c2g_batch* b, int spp_limit, c2g_batch_stats* out) {
     if (rc) return rc;
     const int ns = b->n_streams;
     // longest job first onto the least-loaded stream; shortest first within a stream
-    std::vector<int> order(b->jobs.size());
-    for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
-    std::sort(order.begin(), order.end(), [&](int x, int y) { return b->jobs[x].paths() > b->jobs[y].paths(); });
-    std::vector<double> load(ns, 0.0);
-    std::vector<std::vector<int>> per(ns);
-    for (int i : order) {
-        int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        load[k] += b->jobs[i].paths();
-        per[k].push_back(i);
-    }
-    for (auto& v : per) std::reverse(v.begin(), v.end());
+    std::vector<std::vector<int>> per = batch_queues(b, ns);
     for (BatchJob& j : b->jobs) {
         std::string err;
         rc = j.ctx->gpu->set_wave_counter(j.p.sample_begin, b->streams[0], *j.ctx->arena, err);
@@ -985,6 +1011,13 @@ int c2g_batch_set_trace(c2g_batch* b, int traversal, int trace_block) {
     if (traversal != b->traversal || trace_block != b->trace_block) b->captured_wave_paths = -1;
     b->traversal = traversal;
     b->trace_block = trace_block;
+    return C2G_OK;
+}
+
+int c2g_batch_set_lanes(c2g_batch* b, int lanes) {
+    if (!b) return C2G_ERR_INVALID;
+    if (lanes < 0 || lanes > 256) return bfail(b, C2G_ERR_INVALID, "0 <= lanes <= 256");
+    b->lanes = lanes;
     return C2G_OK;
 }
 

@@ -1436,7 +1436,8 @@ int GpuScene::capture_wave_loop(const c2g_render_params& p, bool guide_sample, c
 void GpuScene::set_trace_block(int threads) { trace_block_ = 64 << trace_block_index(threads); }
 
 int GpuScene::append_job(cudaGraph_t G, const cudaGraphNode_t* deps, int ndeps, const c2g_render_params& p, int wave_paths,
-                         cudaEvent_t done, cudaStream_t st, DeviceArena& arena, int* spw, int* waves, std::string& err) {
+                         cudaEvent_t done, cudaStream_t st, DeviceArena& arena, cudaGraphNode_t* last, int* spw, int* waves,
+                         std::string& err) {
     const int nslots = ((p.width + 7) / 8) * ((p.height + 7) / 8) * 64;
     // samples per wave: as many as the wave size holds, dividing the job's sample count
     int s = std::max(1, std::min(p.sample_count, wave_paths / nslots));
@@ -1487,6 +1488,7 @@ int GpuScene::append_job(cudaGraph_t G, const cudaGraphNode_t* deps, int ndeps, 
     }
     cudaGraphNode_t ev;
     C2G_CUDA(cudaGraphAddEventRecordNode(&ev, G, &prev, 1, done));
+    *last = ev;
     *spw = s;
     *waves = n_waves;
     return C2G_OK;

@@ -115,10 +115,11 @@ public:
     // Append this scene's job (render parameters p, waves of up to wave_paths paths) to graph G as
     // one chain: a kernel that resets the device sample counter to p.sample_begin, a device-side
     // loop over the guided integrator's training-only waves, a loop over the remaining waves, and an
-    // event record node on `done`.  The chain depends on deps[0..ndeps).  *spw / *waves: samples per
-    // wave and the job's wave count.
+    // event record node on `done`.  The chain depends on deps[0..ndeps); *last = its final node.
+    // *spw / *waves: samples per wave and the job's wave count.
     int append_job(cudaGraph_t G, const cudaGraphNode_t* deps, int ndeps, const c2g_render_params& p, int wave_paths,
-                   cudaEvent_t done, cudaStream_t st, DeviceArena& arena, int* spw, int* waves, std::string& err);
+                   cudaEvent_t done, cudaStream_t st, DeviceArena& arena, cudaGraphNode_t* last, int* spw, int* waves,
+                   std::string& err);
     // Device counter the captured graphs read their first sample index from.
     int set_wave_counter(int sample, cudaStream_t st, DeviceArena& arena, std::string& err);
     int* wave_counter() const { return wave_counter_; }

@@ -155,6 +155,10 @@ class Context:
         """SAH traversal variant: 2 (binary nodes) or 4 (four-wide nodes, default)."""
         self.check(self._lib.c2g_set_traversal(self._h, int(width)))
 
+    def set_trace_block(self, threads: int) -> None:
+        """Threads per block of the traversal kernels: 64, 128 (default) or 256."""
+        self.check(self._lib.c2g_set_trace_block(self._h, int(threads)))
+
     # ---- ray queries
     def trace_rays(self, o: np.ndarray, d: np.ndarray, any_hit: bool = False, tmin=None, tmax=None, ignore=None):
         o = np.ascontiguousarray(o, np.float32)
@@ -285,6 +289,12 @@ class Batch:
         if rc:
             self._raise(rc)
         return best.value
+
+    def set_lanes(self, lanes: int) -> None:
+        """One-launch mode: job chains side by side (0 = every job on its own)."""
+        rc = self._lib.c2g_batch_set_lanes(self._h, int(lanes))
+        if rc:
+            self._raise(rc)
 
     def set_trace(self, traversal: int, trace_block: int) -> None:
         rc = self._lib.c2g_batch_set_trace(self._h, int(traversal), int(trace_block))

@@ -182,6 +182,9 @@ int c2g_set_counting(c2g_ctx* ctx, int flags);
 /* SAH-tree traversal variant: 2 (binary nodes) or 4 (four-wide nodes, the default).  Both visit the
  * same leaves; no counterpart in the reference (its BVH is binary). */
 int c2g_set_traversal(c2g_ctx* ctx, int width);
+/* Threads per block of the traversal kernels (64, 128 or 256; default 128); no counterpart in the
+ * reference. */
+int c2g_set_trace_block(c2g_ctx* ctx, int threads);
 
 /* L2 read bandwidth of `device` in GB/s: a `bytes` buffer (keep it well below the L2 size) read
  * `reps` times by every SM with L2-only loads, timed with CUDA events.  No counterpart in the
@@ -194,8 +197,9 @@ int c2g_probe_l2_read(int device, size_t bytes, int reps, double* gbs);
  * GPU, and the films land in each job's context (c2g_film_download).  Two modes:
  *  - streams = 0 (default): the whole batch is one CUDA graph launched once; per job a chain of a
  *    sample-counter reset, device-side while loops (conditional graph nodes) that run the job's
- *    waves one after another, and a completion event; the jobs' chains are independent, so the
- *    GPU interleaves them;
+ *    waves one after another, and a completion event; the jobs are spread over `lanes` chains
+ *    (longest-first onto the least-loaded lane, shortest-first within a lane; default 8,
+ *    c2g_batch_set_lanes) that the GPU runs side by side;
  *  - streams = S > 0: every job's wave is captured as its own graph that replays wave after wave,
  *    jobs spread over S concurrent streams (longest-first onto the least-loaded stream,
  *    shortest-first within a stream).
@@ -230,6 +234,8 @@ int c2g_batch_tune(c2g_batch* b, int wave_paths, int streams);
 /* Traversal variant of every job (SAH node width 2 or 4) and threads per block of the traversal
  * kernels (64, 128 or 256). */
 int c2g_batch_set_trace(c2g_batch* b, int traversal, int trace_block);
+/* One-launch mode: job chains that run side by side (1..256; 0 = every job on its own). */
+int c2g_batch_set_lanes(c2g_batch* b, int lanes);
 /* Candidate values per dimension of the batch configuration (n_x = 0: keep the current value). */
 typedef struct {
     const int* wave_paths;

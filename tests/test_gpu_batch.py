@@ -39,8 +39,8 @@ def _solo(ctx, p, wave_paths):
     return ctx.film()
 
 
-@pytest.mark.parametrize("streams", [2, 0])
-def test_batch_matches_individual_renders(tmp_path, streams):
+@pytest.mark.parametrize("streams,lanes", [(2, None), (0, 8), (0, 1), (0, 0)])
+def test_batch_matches_individual_renders(tmp_path, streams, lanes):
     jobs = [_job(tmp_path, "c1", scenes.cornell, N.INTEGRATOR_PATH, 16, width=32, height=32),
             _job(tmp_path, "c2", scenes.cornell, N.INTEGRATOR_PATH, 12, width=40, height=24),
             _job(tmp_path, "mb", scenes.material_box, N.INTEGRATOR_PATH, 8, width=48, height=48)]
@@ -51,6 +51,8 @@ def test_batch_matches_individual_renders(tmp_path, streams):
         c.film_clear()
         b.add(c, p)
     b.tune(wave_paths, streams)
+    if lanes is not None:
+        b.set_lanes(lanes)  # one chain per job (0), all jobs in one chain (1), or the default 8
     st = b.run()
     assert st.jobs == 3
     assert st.paths == sum(p.width * p.height * p.sample_count for _, p in jobs)
