@@ -221,3 +221,22 @@ def test_new_entry_points_reject_bad_arguments(tmp_path):
     # a host-only context has no device to draw samples on
     assert lib.c2g_sampler_values(ctx.handle, 1, N.iptr(px), N.iptr(px), N.iptr(px), 0, 1, N.fptr(out)) != N.C2G_OK
     assert lib.c2g_sampler_values(ctx.handle, 1, N.iptr(px), N.iptr(px), N.iptr(px), -1, 1, N.fptr(out)) == N.C2G_ERR_INVALID
+
+
+def test_tuning_entry_points_reject_bad_arguments():
+    """Traversal block, guide training batch and batch configuration calls validate their
+    arguments before touching a device: a null handle or an out-of-range value is an error code."""
+    lib = N.load_library()
+    assert lib.c2g_set_trace_block(None, 128) == N.C2G_ERR_INVALID
+    assert lib.c2g_guide_batch(None, 1 << 18, 4) == N.C2G_ERR_INVALID
+    ctx = Context(device=-1)
+    for threads in (0, 32, 96, 512):
+        assert lib.c2g_set_trace_block(ctx.handle, threads) == N.C2G_ERR_INVALID
+    assert lib.c2g_set_trace_block(ctx.handle, 128) == N.C2G_ERR_STATE  # host-only: no device
+    for records, windows in ((0, 4), (1023, 4), (1 << 18, 0), (1 << 18, 65)):
+        assert lib.c2g_guide_batch(ctx.handle, records, windows) == N.C2G_ERR_INVALID
+    assert lib.c2g_guide_batch(ctx.handle, 1 << 18, 4) == N.C2G_ERR_STATE
+    # batch calls on a null batch
+    assert lib.c2g_batch_set_lanes(None, 8) == N.C2G_ERR_INVALID
+    assert lib.c2g_batch_set_trace(None, 4, 128) == N.C2G_ERR_INVALID
+    assert lib.c2g_batch_search(None, None, 4, None) == N.C2G_ERR_INVALID
