@@ -620,6 +620,15 @@ int c2g_guide_batch(c2g_ctx* ctx, int records_per_wave, int windows) {
     return C2G_OK;
 }
 
+int c2g_guide_regularize(c2g_ctx* ctx, float kappa_max, float weight_clamp) {
+    if (!ctx) return C2G_ERR_INVALID;
+    if (!(kappa_max >= 1.f && kappa_max <= c2g::kGuideKappaMax) || !(weight_clamp >= 1.f))
+        return fail(ctx, C2G_ERR_INVALID, "kappa_max in [1, 500], weight_clamp >= 1");
+    if (ctx->host_only) return fail(ctx, C2G_ERR_STATE, "host-only context");
+    ctx->gpu->guide().set_regularisation(kappa_max, weight_clamp);
+    return C2G_OK;
+}
+
 int c2g_guide_config(c2g_ctx* ctx, float learning_rate, float bsdf_fraction, int warmup_waves, int train_steps) {
     if (!ctx) return C2G_ERR_INVALID;
     if (!(learning_rate > 0.f) || !(bsdf_fraction > 0.f && bsdf_fraction <= 1.f) || warmup_waves < 0 || train_steps < 0)

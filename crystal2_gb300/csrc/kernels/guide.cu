@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, co
         if (failed) break;
         const int item = tile * kTcRows + row;
         if (item < total) {
-            if (MODE == 0) pack_lobes(o, out + (size_t)guided_slot(bend, bucket_list, cap, item) * kGuidePacked);
+            if (MODE == 0) pack_lobes(o, out + (size_t)guided_slot(bend, bucket_list, cap, item) * kGuidePacked, net.kappa_max);
             else {
 #pragma unroll
                 for (int k = 0; k < kGuideOut; k++) out[(size_t)item * kGuideOut + k] = o[k];
@@ -404,10 +404,10 @@ static_assert(umma_idesc_mn(64, true, true) == (umma_idesc_bf16(128, 64) | (3u <
 // outputs o (see the oracle for the formulas), each handed to put(k, g_k) as soon as it is known
 // (clamped to [-1e3, 1e3], a non-finite value as 0); returns -log q_mix.
 template <class Put>
-__device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, float w, float pb, Put put) {
+__device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, float w, float pb, float kappa_max, Put put) {
     auto clamped = [](float v) { return isfinite(v) ? fminf(fmaxf(v, -1e3f), 1e3f) : 0.f; };
     Lobe L[kGuideLobes];
-    guide_lobes(o, L);
+    guide_lobes(o, L, kappa_max);
     float p[kGuideLobes], q = 0.f;
 #pragma unroll
     for (int k = 0; k < kGuideLobes; k++) { p[k] = L[k].w * vmf_pdf(L[k], wi); q += p[k]; }
@@ -429,7 +429,7 @@ __device__ __forceinline__ float nll_output_grad(const float* o, float3 wi, floa
         const float dk = 1.f / kap - 2.f * e2 / fmaxf(-expm1f(-2.f * kap), 1e-20f) + (c - 1.f);
         const float kraw = o[5 * k + 3];
         float sig = 1.f / (1.f + __expf(-kraw));
-        if (kap >= kGuideKappaMax) sig = 0.f;
+        if (kap >= kappa_max) sig = 0.f;
         const float3 m = f3(o[5 * k], o[5 * k + 1], o[5 * k + 2]);
         const float len = fmaxf(sqrtf(dot(m, m)), 1e-12f);
         const float3 dm = (wi - L[k].mu * c) * (kap / len);
@@ -582,7 +582,7 @@ __global__ void __launch_bounds__(kTgThreads, 1) k_guide_train_tc(GuideNet net, 
             tc_encode_row<kTgW0>(net, f3(b0), f3(b1), f3(b2), A0, row);
             wi = f3(b3);
             pb = b3.w;
-            w = fminf(b0.w / fmaxf(mean_w, 1e-12f), 20.f);  // normalised, firefly-clamped weight
+            w = fminf(b0.w / fmaxf(mean_w, 1e-12f), net.weight_clamp);  // normalised, firefly-clamped weight
         } else {
             const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
@@ -622,7 +622,7 @@ __global__ void __launch_bounds__(kTgThreads, 1) k_guide_train_tc(GuideNet net, 
         // ---- loss gradient at the outputs (BF16, straight into this row of the delta tile; its
         // padding columns 41..47 stay zero)
         if (valid && w > 0.f) {
-            loss += w * nll_output_grad(o, wi, w, pb, [&](int k, float v) {
+            loss += w * nll_output_grad(o, wi, w, pb, net.kappa_max, [&](int k, float v) {
                 *reinterpret_cast<__nv_bfloat16*>(DO + tc_cm(row, k, kTgWO)) = __float2bfloat16_rn(v);
             });
             wsum += w;
@@ -953,6 +953,8 @@ GuideView GuideTrainer::view(bool record, bool sample) const {
     for (int a = 0; a < 3; a++) { v.net.box_lo[a] = box_lo_[a]; v.net.box_inv[a] = box_inv_[a]; }
     v.net.alpha = alpha_;
     v.net.enabled = sample ? 1 : 0;
+    v.net.kappa_max = kappa_max_;
+    v.net.weight_clamp = weight_clamp_;
     v.out = out_;
     v.rec = rec_;
     v.rec_stride = rec_stride_;

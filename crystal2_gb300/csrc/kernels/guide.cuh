@@ -35,8 +35,8 @@ struct Lobe {
 
 __device__ __forceinline__ float softplusf(float x) { return x > 15.f ? x : log1pf(__expf(x)); }
 
-// Raw outputs (mx, my, mz, kraw, logit) x 8 -> lobes.  kappa = softplus(kraw) + 0.05.
-__device__ __forceinline__ void guide_lobes(const float* out, Lobe* L) {
+// Raw outputs (mx, my, mz, kraw, logit) x 8 -> lobes.  kappa = min(softplus(kraw) + 0.05, kappa_max).
+__device__ __forceinline__ void guide_lobes(const float* out, Lobe* L, float kappa_max) {
     float mx = -INFINITY;
 #pragma unroll
     for (int k = 0; k < kGuideLobes; k++) mx = fmaxf(mx, out[5 * k + 4]);
@@ -46,7 +46,7 @@ __device__ __forceinline__ void guide_lobes(const float* out, Lobe* L) {
         float3 m = f3(out[5 * k], out[5 * k + 1], out[5 * k + 2]);
         float len = sqrtf(dot(m, m));
         L[k].mu = len > 1e-12f ? m * (1.f / len) : f3(0.f, 1.f, 0.f);
-        L[k].kappa = fminf(softplusf(out[5 * k + 3]) + 0.05f, kGuideKappaMax);
+        L[k].kappa = fminf(softplusf(out[5 * k + 3]) + 0.05f, kappa_max);
         L[k].w = __expf(out[5 * k + 4] - mx);
         sum += L[k].w;
     }
@@ -72,12 +72,12 @@ constexpr int kGuidePacked = 52;
 // sharp lobes cannot make the weights larger than 5x the BSDF-only ones).
 __host__ __device__ __forceinline__ float guide_select(float s) { return kGuideSelMin + kGuideSelSpan / (1.f + expf(-s)); }
 
-__device__ __forceinline__ void pack_lobes(const float* out, float* dst) {
+__device__ __forceinline__ void pack_lobes(const float* out, float* dst, float kappa_max) {
     bool finite = true;
 #pragma unroll
     for (int k = 0; k < kGuideOut; k++) finite = finite && isfinite(out[k]);
     Lobe L[kGuideLobes];
-    guide_lobes(out, L);
+    guide_lobes(out, L, kappa_max);
     float4* d4 = reinterpret_cast<float4*>(dst);
 #pragma unroll
     for (int k = 0; k < kGuideLobes; k++) d4[k] = make_float4(L[k].mu.x, L[k].mu.y, L[k].mu.z, L[k].kappa);

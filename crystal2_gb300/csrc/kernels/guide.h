@@ -37,6 +37,8 @@ struct GuideNet {
     float box_lo[3], box_inv[3];
     float alpha;               // probability of drawing the continuation from the BSDF
     int enabled;
+    float kappa_max;           // vMF concentration cap (at most kGuideKappaMax)
+    float weight_clamp;        // training weights clamped at this multiple of their mean
 };
 
 class DeviceArena;
@@ -84,6 +86,11 @@ public:
     GuideStats stats();
     void set_learning_rate(float lr) { lr_ = lr; }
     void set_alpha(float a) { alpha_ = a; }
+    // Regularisation of the mixture: concentration cap and training-weight clamp.
+    void set_regularisation(float kappa_max, float weight_clamp) {
+        kappa_max_ = kappa_max;
+        weight_clamp_ = weight_clamp;
+    }
     // Recorded vertices per wave and minibatch windows (the record buffers are re-sized by the next
     // init()).
     void set_batch(int records, int windows) {
@@ -125,6 +132,8 @@ private:
     float box_lo_[3] = {0, 0, 0}, box_inv_[3] = {1, 1, 1};
     float lr_ = 2e-3f;
     float alpha_ = 0.5f;
+    float kappa_max_ = kGuideKappaMax;
+    float weight_clamp_ = 20.f;
     int steps_ = 0;
     int last_records_ = 0;
     GuideStats last_{};
