@@ -12,7 +12,8 @@ Timing: W untimed warm-up steps, then K steps bracketed by a barrier and device 
 timed with CUDA events on the stream the kernels run on (max over ranks).  The scene (~200 MB of
 BVH/prims) and the wave state (~20 GB) are far larger than the 129 MB L2, so no L2 flush is added.
 `e2e` is the same metric through the public C ABI per step: c2g_render (render parameters from the
-host) plus the film read back to host memory (c2g_film_download), wall-clock timed.
+host) plus the film (rgb sums and weights) read back into pinned host memory (c2g_film_download),
+wall-clock timed.
 
 Multi-GPU: the path does not exchange data; `--gpus N` runs N independent replicas (weak scaling),
 one process per GPU, rendering the same frame; value = all paths / max time.
@@ -312,8 +313,9 @@ def run_ours(args) -> None:
     paths_rank = p.width * p.height * sps * args.steps
     t_max, value = replica_rate(t_local, paths_rank, dist)
     # end to end through the C ABI with host buffers
-    film = np.zeros((p.height, p.width, 3), np.float32)
-    wgt = np.zeros((p.height, p.width), np.float32)
+    # the film read back into pinned host memory (page-locked, as an application streaming frames would)
+    film = torch.zeros((p.height, p.width, 3), dtype=torch.float32, pin_memory=True).numpy()
+    wgt = torch.zeros((p.height, p.width), dtype=torch.float32, pin_memory=True).numpy()
     e2e_steps = max(2, min(args.steps, 4))
     torch.cuda.synchronize()
     if dist:

@@ -72,6 +72,7 @@ struct DeviceSceneBuffers {
     int* fetch = nullptr;                  // ray-query fetch counter
     float4* film = nullptr;                // rgb sum, weight
     float4* film_m2 = nullptr;             // rgb sum of squares
+    float* film_pack = nullptr;            // downloads: rgb (3 floats per pixel) then weights
     int n_lights = 0;
 };
 
@@ -749,6 +750,17 @@ __global__ void k_accumulate(WaveArgs a, PathRefs cur, PathRefs nxt, const int2*
     }
 }
 
+// ---- film download: float4 (rgb, w) per pixel -> rgb triples and weights ----------------------------
+__global__ void k_film_pack(const float4* __restrict__ film, size_t npx, float* rgb, float* w) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npx; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 f = film[i];
+        rgb[3 * i] = f.x;
+        rgb[3 * i + 1] = f.y;
+        rgb[3 * i + 2] = f.z;
+        w[i] = f.w;
+    }
+}
+
 // ---- film: FrameBuffer::AddSample for every sample of the wave, in sample order ------------------
 __global__ void k_film(WaveArgs a, const float4* __restrict__ out_L, float4* film, float4* film_m2) {
     const int stride = gridDim.x * blockDim.x;
@@ -1031,6 +1043,9 @@ int GpuScene::upload(const HostScene& s, int tree, const RefTree* ref, const Sah
     sb_->film_m2 = (float4*)arena.alloc(npx * sizeof(float4), err);
     if (!sb_->film_m2) return C2G_ERR_OOM;
     sb_->owned.push_back(sb_->film_m2);
+    sb_->film_pack = (float*)arena.alloc(npx * 4 * sizeof(float), err);
+    if (!sb_->film_pack) return C2G_ERR_OOM;
+    sb_->owned.push_back(sb_->film_pack);
     C2G_CUDA(cudaMemset(sb_->film, 0, npx * sizeof(float4)));
     C2G_CUDA(cudaMemset(sb_->film_m2, 0, npx * sizeof(float4)));
     sb_->n_lights = S.n_lights;
@@ -1074,16 +1089,25 @@ int GpuScene::check_device_error(std::string& err) {
     return C2G_OK;
 }
 
+// The film in the caller's layout: a kernel packs rgb (and weights) into one device buffer, then
+// one copy per array goes straight into the caller's memory (no host-side repacking).
 int GpuScene::film_download(float* rgb_sum, float* weight, float* rgb_sumsq, std::string& err) {
-    size_t npx = (size_t)film_w_ * film_h_;
+    const size_t npx = (size_t)film_w_ * film_h_;
     if (!sb_->film) { err = "no scene loaded"; return C2G_ERR_STATE; }
-    std::vector<float4> f(npx), m(npx);
-    C2G_CUDA(cudaMemcpy(f.data(), sb_->film, npx * sizeof(float4), cudaMemcpyDeviceToHost));
-    if (rgb_sumsq) C2G_CUDA(cudaMemcpy(m.data(), sb_->film_m2, npx * sizeof(float4), cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < npx; i++) {
-        if (rgb_sum) { rgb_sum[3 * i] = f[i].x; rgb_sum[3 * i + 1] = f[i].y; rgb_sum[3 * i + 2] = f[i].z; }
-        if (weight) weight[i] = f[i].w;
-        if (rgb_sumsq) { rgb_sumsq[3 * i] = m[i].x; rgb_sumsq[3 * i + 1] = m[i].y; rgb_sumsq[3 * i + 2] = m[i].z; }
+    if (!npx) return C2G_OK;
+    const int grid = (int)std::min<size_t>(4096, (npx + 255) / 256);
+    float* rgb = sb_->film_pack;
+    float* w = sb_->film_pack + 3 * npx;
+    if (rgb_sum || weight) {
+        k_film_pack<<<grid, 256>>>(sb_->film, npx, rgb, w);
+        C2G_CUDA(cudaGetLastError());
+        if (rgb_sum) C2G_CUDA(cudaMemcpy(rgb_sum, rgb, 3 * npx * sizeof(float), cudaMemcpyDeviceToHost));
+        if (weight) C2G_CUDA(cudaMemcpy(weight, w, npx * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    if (rgb_sumsq) {
+        k_film_pack<<<grid, 256>>>(sb_->film_m2, npx, rgb, w);
+        C2G_CUDA(cudaGetLastError());
+        C2G_CUDA(cudaMemcpy(rgb_sumsq, rgb, 3 * npx * sizeof(float), cudaMemcpyDeviceToHost));
     }
     return C2G_OK;
 }
