@@ -466,7 +466,7 @@ def guided_equal_time(args) -> dict:
     ctx.guide_config(args.guided_lr, args.guided_bsdf_fraction, args.guided_warmup, args.guided_train_steps)
     ctx.guide_levels(args.guided_levels)
     ctx.guide_batch(args.guided_records, args.guided_windows)
-    ctx.guide_regularize(args.guided_kappa, 20.0)
+    ctx.guide_regularize(args.guided_kappa, 20.0, args.guided_lr_decay)
     guided = progressive(N.INTEGRATOR_GUIDED, 8)
     target = plain[-1][2]
     reach = None
@@ -493,7 +493,7 @@ def guided_equal_time(args) -> dict:
                        "bsdf_fraction": args.guided_bsdf_fraction, "learning_rate": args.guided_lr,
                        "train_steps_per_wave": args.guided_train_steps, "samples_per_wave": 8,
                        "records_per_wave": args.guided_records, "minibatch_windows": args.guided_windows,
-                       "warmup_waves": args.guided_warmup, "kappa_max": args.guided_kappa,
+                       "warmup_waves": args.guided_warmup, "kappa_max": args.guided_kappa, "lr_decay_steps": args.guided_lr_decay,
                        "guided_levels": args.guided_levels,
                        "adam_steps": steps, "last_batch": records, "last_loss": round(loss, 4)},
             "time_to_plain_relMSE_s": None if reach is None else round(reach, 3),
@@ -531,8 +531,8 @@ def batch_run(args) -> dict:
         n_guided += int(guided)
     load_s = time.time() - t0
     t0 = time.time()
-    best = b.search(wave_paths=(1 << 20, 1 << 21, 1 << 22, 1 << 23), streams=(0, 8), traversal=(4, 2),
-                    trace_block=(128, 64, 256), trial_spp=4)
+    best = b.search(wave_paths=(1 << 22, 1 << 23, 1 << 24), streams=(0, 8), traversal=(4, 2),
+                    trace_block=(128, 64, 256), trial_spp=8)
     tune_s = time.time() - t0
     st = b.run()
     lat = [b.latency_ms(i) for i in range(len(jobs))]
@@ -643,6 +643,7 @@ def main() -> int:
     ap.add_argument("--guided-windows", type=int, default=16, help="minibatch windows per guided wave")
     ap.add_argument("--guided-warmup", type=int, default=1, help="guided waves that only train")
     ap.add_argument("--guided-kappa", type=float, default=200.0, help="vMF concentration cap of the guide mixture")
+    ap.add_argument("--guided-lr-decay", type=float, default=0.0, help="Adam steps over which the learning rate halves (0 = constant)")
     ap.add_argument("--guided-levels", type=int, default=0, help="bounce levels served by the guide (0 = all)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-job measurement")
     ap.add_argument("--sah-width", type=int, default=4, choices=[2, 4], help="SAH traversal variant")

@@ -132,7 +132,7 @@ SIGNATURES = {
     "c2g_guide_config": (_I, [_P, C.c_float, C.c_float, _I, _I]),
     "c2g_guide_levels": (_I, [_P, _I]),
     "c2g_guide_batch": (_I, [_P, _I, _I]),
-    "c2g_guide_regularize": (_I, [_P, C.c_float, C.c_float]),
+    "c2g_guide_regularize": (_I, [_P, C.c_float, C.c_float, C.c_float]),
     "c2g_batch_create": (_I, [C.POINTER(_P), _I]),
     "c2g_batch_destroy": (None, [_P]),
     "c2g_batch_last_error": (C.c_char_p, [_P]),

@@ -620,12 +620,12 @@ int c2g_guide_batch(c2g_ctx* ctx, int records_per_wave, int windows) {
     return C2G_OK;
 }
 
-int c2g_guide_regularize(c2g_ctx* ctx, float kappa_max, float weight_clamp) {
+int c2g_guide_regularize(c2g_ctx* ctx, float kappa_max, float weight_clamp, float decay_steps) {
     if (!ctx) return C2G_ERR_INVALID;
-    if (!(kappa_max >= 1.f && kappa_max <= c2g::kGuideKappaMax) || !(weight_clamp >= 1.f))
-        return fail(ctx, C2G_ERR_INVALID, "kappa_max in [1, 500], weight_clamp >= 1");
+    if (!(kappa_max >= 1.f && kappa_max <= c2g::kGuideKappaMax) || !(weight_clamp >= 1.f) || !(decay_steps >= 0.f))
+        return fail(ctx, C2G_ERR_INVALID, "kappa_max in [1, 500], weight_clamp >= 1, decay_steps >= 0");
     if (ctx->host_only) return fail(ctx, C2G_ERR_STATE, "host-only context");
-    ctx->gpu->guide().set_regularisation(kappa_max, weight_clamp);
+    ctx->gpu->guide().set_regularisation(kappa_max, weight_clamp, decay_steps);
     return C2G_OK;
 }
 

@@ -717,12 +717,14 @@ __global__ void __launch_bounds__(kTgThreads, 1) k_guide_train_tc(GuideNet net, 
 // padded output columns stay zero.
 __global__ void k_guide_adam(float* params, const float* __restrict__ part, int nparts, float* m, float* v,
                              __nv_bfloat16* bfw, const float* stats, float lr, float b1, float b2, float eps,
-                             const int* step) {
+                             const int* step, float decay_steps) {
     const float norm = 1.f / fmaxf(stats[1], 1e-12f);
     // bias corrections of Adam step t = *step + 1 (the counter lives on the device so that captured
     // graphs replay correctly; k_guide_tick advances it)
     const float t = (float)(*step + 1);
     const float c1 = 1.f - powf(b1, t), c2 = 1.f - powf(b2, t);
+    // learning rate lr / (1 + t / decay_steps) (decay_steps 0: constant)
+    if (decay_steps > 0.f) lr = lr / (1.f + t / decay_steps);
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < kGuideParams; p += gridDim.x * blockDim.x) {
         int l = 3;
         while (l > 0 && p < guide_w_off(l)) l--;
@@ -941,7 +943,7 @@ void GuideTrainer::train(cudaStream_t st, const float4* out_L, int wave_paths, i
                                                                    std::min(steps, windows_), step_dev_, err);
         steps_++;
         k_guide_adam<<<64, 256, 0, st>>>(params_, part_, nparts_, adam_m_, adam_v_, bf_, loss_acc_, lr_, 0.9f, 0.99f, 1e-8f,
-                                         step_dev_);
+                                         step_dev_, lr_decay_);
         k_guide_tick<<<1, 1, 0, st>>>(step_dev_, loss_acc_);
     }
 }

@@ -86,10 +86,12 @@ public:
     GuideStats stats();
     void set_learning_rate(float lr) { lr_ = lr; }
     void set_alpha(float a) { alpha_ = a; }
-    // Regularisation of the mixture: concentration cap and training-weight clamp.
-    void set_regularisation(float kappa_max, float weight_clamp) {
+    // Regularisation of the mixture: concentration cap, training-weight clamp, learning-rate decay
+    // (lr / (1 + step / decay_steps); 0 = constant).
+    void set_regularisation(float kappa_max, float weight_clamp, float decay_steps) {
         kappa_max_ = kappa_max;
         weight_clamp_ = weight_clamp;
+        lr_decay_ = decay_steps;
     }
     // Recorded vertices per wave and minibatch windows (the record buffers are re-sized by the next
     // init()).
@@ -134,6 +136,7 @@ private:
     float alpha_ = 0.5f;
     float kappa_max_ = kGuideKappaMax;
     float weight_clamp_ = 20.f;
+    float lr_decay_ = 0.f;
     int steps_ = 0;
     int last_records_ = 0;
     GuideStats last_{};

@@ -244,9 +244,10 @@ class Context:
         """Recorded vertices per guided wave and the minibatch windows its Adam steps take in turn."""
         self.check(self._lib.c2g_guide_batch(self._h, int(records_per_wave), int(windows)))
 
-    def guide_regularize(self, kappa_max: float = 500.0, weight_clamp: float = 20.0) -> None:
-        """vMF concentration cap and training-weight clamp (multiple of the mean weight)."""
-        self.check(self._lib.c2g_guide_regularize(self._h, float(kappa_max), float(weight_clamp)))
+    def guide_regularize(self, kappa_max: float = 500.0, weight_clamp: float = 20.0, decay_steps: float = 0.0) -> None:
+        """vMF concentration cap, training-weight clamp (multiple of the mean weight) and learning-rate
+        decay (lr / (1 + step / decay_steps); 0 = constant)."""
+        self.check(self._lib.c2g_guide_regularize(self._h, float(kappa_max), float(weight_clamp), float(decay_steps)))
 
     def guide_config(self, learning_rate: float = 2e-3, bsdf_fraction: float = 0.5, warmup_waves: int = 2,
                      train_steps: int = 1) -> None:

@@ -294,9 +294,10 @@ int c2g_guide_config(c2g_ctx* ctx, float learning_rate, float bsdf_fraction, int
  * the wave's Adam steps take in turn (default 4, 1..64).  Takes effect at the next guided render. */
 int c2g_guide_batch(c2g_ctx* ctx, int records_per_wave, int windows);
 /* Regularisation of the learned mixture: the vMF concentration cap (1..500; default 500, about 2.5
- * degrees of spread) and the clamp of the training weights at a multiple of their mean (>= 1;
- * default 20).  Applies to the next inference and training launches. */
-int c2g_guide_regularize(c2g_ctx* ctx, float kappa_max, float weight_clamp);
+ * degrees of spread), the clamp of the training weights at a multiple of their mean (>= 1;
+ * default 20) and the learning-rate decay: Adam step t uses lr / (1 + t / decay_steps) (>= 0;
+ * default 0 = constant).  Applies to the next inference and training launches. */
+int c2g_guide_regularize(c2g_ctx* ctx, float kappa_max, float weight_clamp, float decay_steps);
 /* Bounce levels, from the camera hit, whose vertices sample (and train) the guide; deeper vertices
  * use the plain tracer's estimator.  0 = every level; default 2. */
 int c2g_guide_levels(c2g_ctx* ctx, int levels);

@@ -112,6 +112,19 @@ def test_batch_rejects_bad_input(tmp_path):
     b.close()
 
 
+@pytest.mark.parametrize("streams", [0, 2])
+def test_batch_rejects_direct_lighting(tmp_path, streams):
+    """The direct lighting integrator walks pass-through hops with a host-side queue check, so it
+    cannot run inside batch graphs: both modes refuse it with an error, not a wrong film."""
+    c, p = _job(tmp_path, "d", scenes.cornell, N.INTEGRATOR_DIRECT, 4, width=16, height=16)
+    b = Batch(0)
+    b.add(c, p)
+    b.tune(4096, streams)
+    with pytest.raises(N.C2GError):
+        b.run()
+    b.close()
+
+
 def test_batch_search_one_launch_guided(tmp_path):
     """The coordinate search picks a configuration from every dimension's candidates; the chosen one
     renders a guided and a plain job in one graph launch, the guided job training inside it."""

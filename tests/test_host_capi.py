@@ -236,9 +236,10 @@ def test_tuning_entry_points_reject_bad_arguments():
     for records, windows in ((0, 4), (1023, 4), (1 << 18, 0), (1 << 18, 65)):
         assert lib.c2g_guide_batch(ctx.handle, records, windows) == N.C2G_ERR_INVALID
     assert lib.c2g_guide_batch(ctx.handle, 1 << 18, 4) == N.C2G_ERR_STATE
-    for kappa, clamp in ((0.5, 20.0), (501.0, 20.0), (100.0, 0.5), (float("nan"), 20.0)):
-        assert lib.c2g_guide_regularize(ctx.handle, kappa, clamp) == N.C2G_ERR_INVALID
-    assert lib.c2g_guide_regularize(ctx.handle, 100.0, 10.0) == N.C2G_ERR_STATE
+    for kappa, clamp, decay in ((0.5, 20.0, 0.0), (501.0, 20.0, 0.0), (100.0, 0.5, 0.0), (float("nan"), 20.0, 0.0),
+                                (100.0, 10.0, -1.0)):
+        assert lib.c2g_guide_regularize(ctx.handle, kappa, clamp, decay) == N.C2G_ERR_INVALID
+    assert lib.c2g_guide_regularize(ctx.handle, 100.0, 10.0, 1000.0) == N.C2G_ERR_STATE
     # batch calls on a null batch
     assert lib.c2g_batch_set_lanes(None, 8) == N.C2G_ERR_INVALID
     assert lib.c2g_batch_set_trace(None, 4, 128) == N.C2G_ERR_INVALID
