@@ -444,8 +444,14 @@ def guided_equal_time(args) -> dict:
     ref = ctx.image().astype(np.float64)
     ref_s = time.perf_counter() - t0
 
+    # relMSE = mean((I - R)^2 / (R^2 + 0.01)), evaluated in FP32 with the weights precomputed
+    # (outside the timed render calls; it only bounds the benchmark's own run time)
+    ref32 = ref.astype(np.float32)
+    inv = (1.0 / (ref32 * ref32 + 1e-2)).astype(np.float32)
+
     def relmse(img):
-        return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+        d = img.astype(np.float32) - ref32
+        return float(np.mean(d * d * inv, dtype=np.float64))
 
     def progressive(integ, wave_spp):
         ctx.film_clear()
@@ -455,7 +461,7 @@ def guided_equal_time(args) -> dict:
             ctx.render(params(integ, s0, 8, wave_spp))
             spent += time.perf_counter() - t
             s0 += 8
-            curve.append((spent, s0, relmse(ctx.image().astype(np.float64))))
+            curve.append((spent, s0, relmse(ctx.image())))
         return curve
 
     ctx.film_clear()
