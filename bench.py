@@ -537,7 +537,7 @@ def batch_run(args) -> dict:
         n_guided += int(guided)
     load_s = time.time() - t0
     t0 = time.time()
-    best = b.search(wave_paths=(1 << 22, 1 << 23, 1 << 24), streams=(0, 8), traversal=(4, 2),
+    best = b.search(wave_paths=(1 << 21, 1 << 22, 1 << 23), streams=(0, 8), traversal=(4, 2),
                     trace_block=(128, 64, 256), trial_spp=8)
     tune_s = time.time() - t0
     st = b.run()
@@ -649,7 +649,7 @@ def main() -> int:
     ap.add_argument("--guided-windows", type=int, default=16, help="minibatch windows per guided wave")
     ap.add_argument("--guided-warmup", type=int, default=1, help="guided waves that only train")
     ap.add_argument("--guided-kappa", type=float, default=200.0, help="vMF concentration cap of the guide mixture")
-    ap.add_argument("--guided-lr-decay", type=float, default=0.0, help="Adam steps over which the learning rate halves (0 = constant)")
+    ap.add_argument("--guided-lr-decay", type=float, default=2000.0, help="Adam steps over which the learning rate halves (0 = constant)")
     ap.add_argument("--guided-levels", type=int, default=0, help="bounce levels served by the guide (0 = all)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-job measurement")
     ap.add_argument("--sah-width", type=int, default=4, choices=[2, 4], help="SAH traversal variant")

@@ -1044,11 +1044,23 @@ int c2g_batch_search(c2g_batch* b, const c2g_batch_space* space, int trial_spp, 
         return rc ? rc : c2g_batch_set_trace(b, c.trav, c.block);
     };
     double best = -1.0;
+    // a candidate whose wave buffers do not fit next to the other jobs' is infeasible: its trial
+    // ends with C2G_ERR_OOM, every job's wave buffers are released and the search goes on
     auto trial = [&](const Cfg& c, double* rate) {
         int rc = apply(c);
         if (rc) return rc;
         c2g_batch_stats st{};
         rc = batch_pass(b, trial_spp, &st);
+        if (rc == C2G_ERR_OOM) {
+            for (BatchJob& j : b->jobs) {
+                drop_graphs(j);
+                j.ctx->gpu->release_wave_buffers(*j.ctx->arena);
+                j.ctx->gpu->guide().release(*j.ctx->arena);  // its per-slot buffers follow the wave size
+            }
+            b->captured_wave_paths = -1;
+            *rate = -1.0;
+            return C2G_OK;
+        }
         if (rc) return rc;
         *rate = st.mpaths_per_s;
         return C2G_OK;

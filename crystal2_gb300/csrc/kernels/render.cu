@@ -1379,6 +1379,13 @@ void GpuScene::set_sah_width(int w) {
     if (sb_->S.tree == C2G_TREE_SAH) sb_->S.sah_width = sb_->S.nodes4 ? sah_width_ : 2;
 }
 
+void GpuScene::release_wave_buffers(DeviceArena& arena) {
+    cudaDeviceSynchronize();
+    for (void* q : wb_->owned) arena.free(q);
+    wb_->owned.clear();
+    *wb_ = WaveBuffers();
+}
+
 int GpuScene::set_wave_counter(int sample, cudaStream_t st, DeviceArena& arena, std::string& err) {
     if (!wave_counter_) {
         wave_counter_ = (int*)arena.alloc(256, err);

@@ -122,6 +122,8 @@ public:
                    std::string& err);
     // Device counter the captured graphs read their first sample index from.
     int set_wave_counter(int sample, cudaStream_t st, DeviceArena& arena, std::string& err);
+    // Free the wave's working buffers (the next render or capture sizes them anew).
+    void release_wave_buffers(DeviceArena& arena);
     int* wave_counter() const { return wave_counter_; }
     // Threads per block of the traversal kernels (64, 128 or 256); taken by the next render or capture.
     void set_trace_block(int threads);
