@@ -173,3 +173,28 @@ def test_batch_trace_settings_keep_films(tmp_path, traversal, block):
             # the binary and four-wide trees give the same closest hits up to near-ties
             close = np.isclose(s, ref[0], rtol=1e-4, atol=1e-6)
             assert close.mean() > 0.98
+
+
+def test_batch_search_skips_wave_sizes_that_do_not_fit(tmp_path):
+    """With a memory cap per context, a wave size whose buffers do not fit fails its trial with
+    C2G_ERR_OOM: the search releases the buffers, keeps the candidate that fits and the batch runs."""
+    jobs = []
+    for i in range(2):
+        cp, sp = scenes.cornell(str(tmp_path / f"c{i}"), width=32, height=32, spp=64)
+        ctx = Context(0, mem_limit_bytes=16 << 20)
+        ctx.load(cp, sp, tree=N.TREE_SAH)
+        p = ctx.render_params()
+        p.sample_begin, p.sample_count = 0, 64
+        jobs.append((ctx, p))
+    b = Batch(0)
+    for c, p in jobs:
+        c.film_clear()
+        b.add(c, p)
+    best = b.search(wave_paths=(4096, 1 << 20), streams=(0,), traversal=(4,), trace_block=(128,), trial_spp=4)
+    assert best > 0
+    st = b.run()
+    assert st.wave_paths == 4096
+    for c, p in jobs:
+        s, w = c.film()
+        assert np.all(w == p.sample_count) and np.isfinite(s).all()
+    b.close()
