@@ -30,7 +30,8 @@ void* DeviceArena::alloc(size_t bytes, std::string& err) {
     if (bytes == 0) bytes = 16;
     bytes = (bytes + 255) & ~size_t(255);
     if (cap_ && used_ + bytes > cap_) {
-        err = "device memory cap exceeded (" + std::to_string(used_ + bytes) + " > " + std::to_string(cap_) + " bytes)";
+        err = "device memory cap exceeded (" + std::to_string(used_) + " in use + " + std::to_string(bytes) + " requested > " +
+              std::to_string(cap_) + " bytes)";
         return nullptr;
     }
     void* p = nullptr;
@@ -104,7 +105,8 @@ struct WaveBuffers {
 GpuScene::GpuScene() : sb_(new DeviceSceneBuffers()), wb_(new WaveBuffers()) {}
 GpuScene::~GpuScene() {
     if (side_) cudaStreamDestroy(side_);
-    for (int k = 0; k < 2; k++) {
+    if (ahead_) cudaStreamDestroy(ahead_);
+    for (int k = 0; k < 3; k++) {
         if (fork_ev_[k]) cudaEventDestroy(fork_ev_[k]);
         if (join_ev_[k]) cudaEventDestroy(join_ev_[k]);
     }
@@ -119,7 +121,12 @@ int GpuScene::side_stream(std::string& err) {
         side_ = nullptr;
         return C2G_ERR_CUDA;
     }
-    for (int k = 0; k < 2; k++)
+    if (cudaStreamCreateWithFlags(&ahead_, cudaStreamNonBlocking) != cudaSuccess) {
+        err = "cannot create the look-ahead stream";
+        ahead_ = nullptr;
+        return C2G_ERR_CUDA;
+    }
+    for (int k = 0; k < 3; k++)
         if (cudaEventCreateWithFlags(&fork_ev_[k], cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&join_ev_[k], cudaEventDisableTiming) != cudaSuccess) {
             err = "cannot create stream events";
@@ -1269,6 +1276,33 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
     begin(C2G_K_RAYGEN, st);
     k_raygen<<<g_raygen, 256, 0, st>>>(S, a, buf[0], w.out_L, C + 0);
     end(st);
+    // Extension of bounce level lv on stream es: closest hits of queue `q`, appended to the material
+    // buckets.  Block 0 zeroes *za, *zb, zb[2] (the queue after the next and the shadow queue with
+    // its fetch counter) and *zc (the MIS queue) - live counters when it runs in order, spare slots
+    // when it runs ahead of the previous level's shadow rays (those are zeroed on st afterwards).
+    auto extend = [&](int q, int* za, int* zb, int* zc, cudaStream_t es) {
+        begin(C2G_K_EXTEND, es);
+        // bucket sizes and the extension fetch counter C[5] start at zero on every level
+        cudaMemsetAsync(C + 5, 0, sizeof(int) * (kCntBucket - 5 + kBuckets), es);
+        if (S.tree == C2G_TREE_SAH && S.sah_width == 4) {
+            if (count)
+                k_extend_fetch<true><<<TG.exf_c, tb, 0, es>>>(S, buf[q].o, buf[q].d, w.hit, C + q, za, zb, zc, C + kCntBucket,
+                                                              w.bucket_list, (int)w.P, C + 5, cnt);
+            else
+                k_extend_fetch<false><<<TG.exf, tb, 0, es>>>(S, buf[q].o, buf[q].d, w.hit, C + q, za, zb, zc, C + kCntBucket,
+                                                               w.bucket_list, (int)w.P, C + 5, cnt);
+        } else if (count) {
+            k_extend<true><<<TG.ext_c, tb, 0, es>>>(S, buf[q].o, buf[q].d, w.hit, C + q, za, zb, zc, C + kCntBucket,
+                                                    w.bucket_list, (int)w.P, cnt);
+        } else {
+            k_extend<false><<<TG.ext, tb, 0, es>>>(S, buf[q].o, buf[q].d, w.hit, C + q, za, zb, zc, C + kCntBucket,
+                                                     w.bucket_list, (int)w.P, cnt);
+        }
+        end(es);
+    };
+    int* const spare = C + 56;  // counter slots no kernel reads
+    static_assert(kCntBucket + kBuckets <= 56, "counter layout");
+    bool ahead_done = false;    // this level's extension was launched during the previous level
     int cur = 0;
     for (int b = 0; b < plan.levels; b++) {
         int nxt = cur ^ 1;
@@ -1281,24 +1315,9 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
         }
         // statistics: the paths entering this level
         if (count) k_level_add<<<1, 1, 0, st>>>(w.levels + std::min(b, C2G_LEVELS - 1), C + cur);
-        begin(C2G_K_EXTEND, st);
-        // bucket sizes and the extension fetch counter C[5] start at zero on every level
-        cudaMemsetAsync(C + 5, 0, sizeof(int) * (kCntBucket - 5 + kBuckets), st);
-        if (S.tree == C2G_TREE_SAH && S.sah_width == 4) {
-            if (count)
-                k_extend_fetch<true><<<TG.exf_c, tb, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
-                                                              C + kCntBucket, w.bucket_list, (int)w.P, C + 5, cnt);
-            else
-                k_extend_fetch<false><<<TG.exf, tb, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
-                                                               C + kCntBucket, w.bucket_list, (int)w.P, C + 5, cnt);
-        } else if (count) {
-            k_extend<true><<<TG.ext_c, tb, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
-                                                    C + kCntBucket, w.bucket_list, (int)w.P, cnt);
-        } else {
-            k_extend<false><<<TG.ext, tb, 0, st>>>(S, buf[cur].o, buf[cur].d, w.hit, C + cur, C + nxt, C + 2, C + 3,
-                                                     C + kCntBucket, w.bucket_list, (int)w.P, cnt);
-        }
-        end(st);
+        const bool pre = ahead_done;
+        if (pre) cudaStreamWaitEvent(st, join_ev_[2], 0);
+        else extend(cur, C + nxt, C + 2, C + 3, st);
         // the guide serves the first guide_levels_ bounce levels; deeper vertices shade plainly
         const bool glevel = guided && (guide_levels_ <= 0 || b < guide_levels_);
         if (gv.sample && glevel) {
@@ -1322,6 +1341,18 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
             nb++;
         }
         if (overlap) join(0);
+        // The next level's queue is complete: its extension runs ahead on the third stream, beside
+        // this level's shadow and MIS rays and accumulation (none of which reads the hits or the
+        // buckets it writes).  Not for direct lighting, whose walk checks the queue on the host.
+        ahead_done = false;
+        if (overlap && a.integrator != C2G_INTEGRATOR_DIRECT && b + 1 < plan.levels) {
+            cudaEventRecord(fork_ev_[2], st);
+            cudaStreamWaitEvent(ahead_, fork_ev_[2], 0);
+            extend(nxt, spare, spare + 1, spare + 4, ahead_);
+            cudaEventRecord(join_ev_[2], ahead_);
+            ahead_done = true;
+            launches++;
+        }
         // MIS rays (closest hit + emitter test) beside the shadow rays (any hit): disjoint inputs
         // and outputs; both must finish before k_accumulate
         if (overlap) {
@@ -1353,7 +1384,13 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
         begin(C2G_K_ACCUM, st);
         k_accumulate<<<g_acc, 256, 0, st>>>(a, buf[cur], buf[nxt], w.acc, w.sh_c, w.mis_c, w.mis_hit, w.out_L, C + cur, gv);
         end(st);
-        launches += 4;
+        if (ahead_done) {
+            // the counters the look-ahead extension left alone: the queue after the next level, the
+            // shadow and MIS queues and the shadow fetch counter
+            cudaMemsetAsync(C + cur, 0, sizeof(int), st);
+            cudaMemsetAsync(C + 2, 0, 3 * sizeof(int), st);
+        }
+        launches += pre ? 3 : 4;
         cur = nxt;
     }
     begin(C2G_K_FILM, st);

@@ -155,7 +155,10 @@ private:
     // off while per-kernel timing events are recorded and in the graphs batched jobs replay.
     bool overlap_ = true;
     cudaStream_t side_ = nullptr;
-    cudaEvent_t fork_ev_[2] = {nullptr, nullptr}, join_ev_[2] = {nullptr, nullptr};
+    // Third stream of a wave: the next bounce level's extension starts on it as soon as this level's
+    // shading has filled the next queue, beside this level's shadow and MIS rays and accumulation.
+    cudaStream_t ahead_ = nullptr;
+    cudaEvent_t fork_ev_[3] = {nullptr, nullptr, nullptr}, join_ev_[3] = {nullptr, nullptr, nullptr};
     int side_stream(std::string& err);
     float box_lo_[3] = {0, 0, 0}, box_hi_[3] = {1, 1, 1};  // scene bounds (network input range)
     c2g_stats stats_{};

@@ -249,7 +249,10 @@ typedef struct {
 } c2g_batch_space;
 /* Coordinate search: starting from the current configuration, each dimension in turn (wave size,
  * mode, traversal variant, block size) takes its candidate with the best aggregate rate on a trial
- * pass of every job (trial_spp samples each); films and networks are reset afterwards. */
+ * pass of every job (trial_spp samples each); films and networks are reset afterwards.  A candidate
+ * whose trial runs out of device memory is skipped.  A trial's waves hold at most trial_spp samples
+ * per pixel, so with trial_spp below a job's sample count the full run may need more memory than
+ * its trial did. */
 int c2g_batch_search(c2g_batch* b, const c2g_batch_space* space, int trial_spp, double* best_mpaths_per_s);
 /* Time each (wave_paths, streams) pair of the candidate lists on a short trial of every job
  * (trial_spp samples each, films and networks reset afterwards), keep the fastest (an exhaustive

@@ -180,17 +180,19 @@ def test_batch_search_skips_wave_sizes_that_do_not_fit(tmp_path):
     C2G_ERR_OOM: the search releases the buffers, keeps the candidate that fits and the batch runs."""
     jobs = []
     for i in range(2):
-        cp, sp = scenes.cornell(str(tmp_path / f"c{i}"), width=32, height=32, spp=64)
-        ctx = Context(0, mem_limit_bytes=16 << 20)
+        cp, sp = scenes.cornell(str(tmp_path / f"c{i}"), width=32, height=32, spp=256)
+        ctx = Context(0, mem_limit_bytes=64 << 20)
         ctx.load(cp, sp, tree=N.TREE_SAH)
         p = ctx.render_params()
-        p.sample_begin, p.sample_count = 0, 64
+        p.sample_begin, p.sample_count = 0, 256
         jobs.append((ctx, p))
     b = Batch(0)
     for c, p in jobs:
         c.film_clear()
         b.add(c, p)
-    best = b.search(wave_paths=(4096, 1 << 20), streams=(0,), traversal=(4,), trace_block=(128,), trial_spp=4)
+    # 4096 paths per wave fit (about 2 MB of wave buffers per job); 2^20 do not (256 samples of 1024
+    # pixel slots: about 100 MB)
+    best = b.search(wave_paths=(4096, 1 << 20), streams=(0,), traversal=(4,), trace_block=(128,), trial_spp=256)
     assert best > 0
     st = b.run()
     assert st.wave_paths == 4096
