@@ -1320,7 +1320,7 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
         else extend(cur, C + nxt, C + 2, C + 3, st);
         // the guide serves the first guide_levels_ bounce levels; deeper vertices shade plainly
         const bool glevel = guided && (guide_levels_ <= 0 || b < guide_levels_);
-        if (gv.sample && glevel) {
+        if (gv.sample && glevel && !pre) {
             begin(C2G_K_GUIDE, st);
             launches += guide_.infer(st, &S, buf[cur].o, buf[cur].d, w.hit, C + kCntBucket, w.bucket_list, (int)w.P,
                                      present_buckets_);
@@ -1349,9 +1349,17 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
             cudaEventRecord(fork_ev_[2], st);
             cudaStreamWaitEvent(ahead_, fork_ev_[2], 0);
             extend(nxt, spare, spare + 1, spare + 4, ahead_);
+            launches++;
+            // the next level's guide inference needs only its rays and hits: it follows on the
+            // same stream (this level's shading has read its mixtures already)
+            if (gv.sample && guided && (guide_levels_ <= 0 || b + 1 < guide_levels_)) {
+                begin(C2G_K_GUIDE, ahead_);
+                launches += guide_.infer(ahead_, &S, buf[nxt].o, buf[nxt].d, w.hit, C + kCntBucket, w.bucket_list, (int)w.P,
+                                         present_buckets_);
+                end(ahead_);
+            }
             cudaEventRecord(join_ev_[2], ahead_);
             ahead_done = true;
-            launches++;
         }
         // MIS rays (closest hit + emitter test) beside the shadow rays (any hit): disjoint inputs
         // and outputs; both must finish before k_accumulate
