@@ -60,6 +60,7 @@ LEVELS = 64
 KERNEL_NAMES = ["raygen", "extend", "shade", "shadow", "mis", "accumulate", "film", "guide", "train", "-"]
 COUNT_TRAVERSAL = 1
 COUNT_TIMING = 2
+COUNT_SERIAL = 4
 
 
 class Stats(C.Structure):

@@ -1578,7 +1578,9 @@ int GpuScene::render(const HostScene& s, const c2g_render_params& p, cudaStream_
     const bool guided = plan.guided;
     const bool count = (counting_ & C2G_COUNT_TRAVERSAL) != 0;
     const bool timing = (counting_ & C2G_COUNT_TIMING) != 0;
-    overlap_ = true;  // timing events are recorded on the stream each kernel runs on
+    // timing events are recorded on the stream each kernel runs on; C2G_COUNT_SERIAL keeps every
+    // kernel on st, so that their times are exclusive
+    overlap_ = (counting_ & C2G_COUNT_SERIAL) == 0;
     unsigned long long* cnt = sb_->counts;
     if (count) {
         C2G_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 3 * C2G_K_KINDS, st));

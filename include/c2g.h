@@ -94,6 +94,7 @@ typedef struct {
 /* Counting / timing switches of c2g_set_counting. */
 #define C2G_COUNT_TRAVERSAL 1  /* rays, nodes visited and prims tested per traversal kernel */
 #define C2G_COUNT_TIMING 2     /* CUDA events around every launch; per-kind device time */
+#define C2G_COUNT_SERIAL 4     /* one stream: no side or look-ahead stream, so per-kind times are exclusive */
 
 #define C2G_LEVELS 64  /* size of the per-bounce-level arrays (deeper levels add to the last entry) */
 
