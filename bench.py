@@ -256,7 +256,6 @@ def run_ours(args) -> None:
     t0 = time.time()
     ctx.set_traversal(args.sah_width)
     ctx.set_trace_block(args.trace_block)
-    ctx.set_shadow_sort(args.shadow_sort)
     ctx.load(cp, sp, tree=N.TREE_SAH)
     load_s = time.time() - t0
     p = ctx.render_params()
@@ -670,7 +669,6 @@ def main() -> int:
     ap.add_argument("--no-batch", action="store_true", help="skip the batched multi-job measurement")
     ap.add_argument("--sah-width", type=int, default=4, choices=[2, 4], help="SAH traversal variant")
     ap.add_argument("--trace-block", type=int, default=128, choices=[64, 128, 256], help="traversal kernels' block size")
-    ap.add_argument("--shadow-sort", type=int, default=0, help="bounce levels whose shadow rays are binned before tracing")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0: the library default, 2^21)")
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--no-rays", action="store_true", help="skip the ray-intersection microbench")

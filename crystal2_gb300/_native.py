@@ -118,7 +118,6 @@ SIGNATURES = {
     "c2g_set_counting": (_I, [_P, _I]),
     "c2g_set_traversal": (_I, [_P, _I]),
     "c2g_set_trace_block": (_I, [_P, _I]),
-    "c2g_set_shadow_sort": (_I, [_P, _I]),
     "c2g_probe_l2_read": (_I, [_I, C.c_size_t, _I, C.POINTER(C.c_double)]),
     "c2g_trace_rays": (_I, [_P, _I, _FP, _FP, _FP, _FP, _IP, _I, _IP, _FP]),
     "c2g_trace_rays_dev": (_I, [_P, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P]),

@@ -442,14 +442,6 @@ int c2g_set_trace_block(c2g_ctx* ctx, int threads) {
     return C2G_OK;
 }
 
-int c2g_set_shadow_sort(c2g_ctx* ctx, int levels) {
-    if (!ctx) return C2G_ERR_INVALID;
-    if (levels < 0) return fail(ctx, C2G_ERR_INVALID, "levels >= 0");
-    if (ctx->host_only) return fail(ctx, C2G_ERR_STATE, "host-only context");
-    ctx->gpu->set_shadow_sort(levels);
-    return C2G_OK;
-}
-
 int c2g_probe_l2_read(int device, size_t bytes, int reps, double* gbs) {
     if (!gbs) return C2G_ERR_INVALID;
     int ndev = 0;

@@ -99,9 +99,6 @@ struct WaveBuffers {
     int* bucket_list = nullptr;  // kBuckets lists of P slots
     int* counters = nullptr;  // [0],[1] path queues, [2] shadow, [3] mis, [8..20) material buckets
     int* levels = nullptr;    // statistics: paths entering each bounce level (C2G_LEVELS)
-    int* sh_key = nullptr;    // shadow-ray binning: bin of each shadow ray (light, origin cell)
-    int* sh_perm = nullptr;   //   shadow rays in bin order
-    int* sh_bins = nullptr;   //   bin sizes, then bin cursors
     std::vector<void*> owned;
 };
 
@@ -645,55 +642,6 @@ __global__ void k_shadow(DevScene S, const int* __restrict__ list, const int* co
     if (COUNT) flush_counts(cnt, C2G_K_SHADOW, rays, tc);
 }
 
-// ---- shadow-ray binning: rays of one light from one cell of the scene box traced together -------
-constexpr int kShadowCellBits = 4;                          // per axis
-constexpr int kShadowCells = 1 << (3 * kShadowCellBits);    // 4096 cells
-__device__ __forceinline__ unsigned cell_bits(float v) {
-    const float c = fminf(fmaxf(v, 0.f), 0.999999f) * (float)(1 << kShadowCellBits);
-    return (unsigned)c;
-}
-// bins: light-major, Morton order of the origin's cell within a light
-__global__ void k_shadow_key(const float4* __restrict__ so, const int* __restrict__ list, const int* count, int K, float3 lo,
-                             float3 inv, int* key, int* bins) {
-    const int n = *count;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 o = so[i];
-        const unsigned x = cell_bits((o.x - lo.x) * inv.x), y = cell_bits((o.y - lo.y) * inv.y), z = cell_bits((o.z - lo.z) * inv.z);
-        unsigned m = 0;
-#pragma unroll
-        for (int b = 0; b < kShadowCellBits; b++)
-            m |= (((x >> b) & 1u) << (3 * b)) | (((y >> b) & 1u) << (3 * b + 1)) | (((z >> b) & 1u) << (3 * b + 2));
-        const int k = (list[i] % K) * kShadowCells + (int)m;
-        key[i] = k;
-        atomicAdd(bins + k, 1);
-    }
-}
-// exclusive prefix sum of the bin sizes (one block)
-__global__ void __launch_bounds__(1024) k_shadow_scan(int* bins, int nb) {
-    __shared__ int part[1024];
-    const int per = (nb + 1023) / 1024, lo = threadIdx.x * per, hi = min(nb, lo + per);
-    int s = 0;
-    for (int i = lo; i < hi; i++) s += bins[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const int v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    int run = part[threadIdx.x] - s;
-    for (int i = lo; i < hi; i++) {
-        const int c = bins[i];
-        bins[i] = run;
-        run += c;
-    }
-}
-__global__ void k_shadow_scatter(const int* __restrict__ key, const int* count, int* bins, int* perm) {
-    const int n = *count;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) perm[atomicAdd(bins + key[i], 1)] = i;
-}
-
 // Four-wide any-hit traversal with dynamic ray fetch: a lane whose ray is finished takes the next
 // ray from a global counter at the end of every while-while round, instead of idling until the
 // slowest ray of its warp ends (persistent threads with ray replacement).  Same per-ray traversal
@@ -701,8 +649,7 @@ __global__ void k_shadow_scatter(const int* __restrict__ key, const int* count, 
 template <bool COUNT>
 __global__ void __launch_bounds__(256, C2G_SHADOW_MIN_BLOCKS) k_shadow_fetch(DevScene S, const int* __restrict__ list, const int* count,
                                                       const float4* __restrict__ so, const float4* __restrict__ sd,
-                                                      float4* sc, int* fetch, unsigned long long* cnt,
-                                                      const int* __restrict__ perm) {
+                                                      float4* sc, int* fetch, unsigned long long* cnt) {
     const int n = *count;
     TraceCounters tc{0, 0};
     unsigned rays = 0;
@@ -714,10 +661,9 @@ __global__ void __launch_bounds__(256, C2G_SHADOW_MIN_BLOCKS) k_shadow_fetch(Dev
     Bvh4AnyState st;
     while (true) {
         const bool need = ray < 0 && !exhausted;
-        int idx = warp_fetch(fetch, need, n);
+        const int idx = warp_fetch(fetch, need, n);
         if (need) {
             if (idx >= 0) {
-                if (perm) idx = __ldg(perm + idx);  // binned order: rays of one light from one cell together
                 const float4 o = so[idx], d = sd[idx];
                 r = make_rayq(f3(o), f3(d));
                 tmax = d.w;
@@ -1284,8 +1230,7 @@ int GpuScene::prepare(const c2g_render_params& p, DeviceArena& arena, WavePlan& 
              (wb_->mis_o = (float4*)A(P * 16)) && (wb_->mis_d = (float4*)A(P * 16)) && (wb_->mis_c = (float4*)A(PK * 16)) &&
              (wb_->mis_hit = (float4*)A(P * 16)) && (wb_->sh_list = (int*)A(PK * 4)) && (wb_->mis_list = (int*)A(P * 4)) &&
              (wb_->bucket_list = (int*)A(P * 4 * kBuckets)) && (wb_->counters = (int*)A(256)) &&
-             (wb_->levels = (int*)A(4 * C2G_LEVELS)) && (wb_->sh_key = (int*)A(PK * 4)) && (wb_->sh_perm = (int*)A(PK * 4)) &&
-             (wb_->sh_bins = (int*)A(4 * (size_t)a.K * kShadowCells));
+             (wb_->levels = (int*)A(4 * C2G_LEVELS));
         if (!ok) {
             for (void* q : wb_->owned) arena.free(q);
             wb_->owned.clear();
@@ -1428,22 +1373,8 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
         begin(C2G_K_SHADOW, st);
         if (S.tree == C2G_TREE_SAH && S.sah_width == 4) {
             // four-wide nodes: the dynamic-fetch kernel (fetch counter C[4], zeroed by k_extend)
-            const int* perm = nullptr;
-            if (b < shadow_sort_levels_) {
-                // bin the level's shadow rays by (light, origin cell) and trace them in bin order
-                const float3 lo = make_float3(box_lo_[0], box_lo_[1], box_lo_[2]);
-                const float3 inv = make_float3(1.f / std::max(box_hi_[0] - box_lo_[0], 1e-20f), 1.f / std::max(box_hi_[1] - box_lo_[1], 1e-20f),
-                                               1.f / std::max(box_hi_[2] - box_lo_[2], 1e-20f));
-                const int nb = a.K * kShadowCells;
-                cudaMemsetAsync(w.sh_bins, 0, sizeof(int) * nb, st);
-                k_shadow_key<<<g_acc, 256, 0, st>>>(w.sh_o, w.sh_list, C + 2, a.K, lo, inv, w.sh_key, w.sh_bins);
-                k_shadow_scan<<<1, 1024, 0, st>>>(w.sh_bins, nb);
-                k_shadow_scatter<<<g_acc, 256, 0, st>>>(w.sh_key, C + 2, w.sh_bins, w.sh_perm);
-                perm = w.sh_perm;
-                launches += 3;
-            }
-            if (count) k_shadow_fetch<true><<<TG.shf_c, tb, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, C + 4, cnt, perm);
-            else k_shadow_fetch<false><<<TG.shf, tb, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, C + 4, cnt, perm);
+            if (count) k_shadow_fetch<true><<<TG.shf_c, tb, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, C + 4, cnt);
+            else k_shadow_fetch<false><<<TG.shf, tb, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, C + 4, cnt);
         } else if (count) {
             k_shadow<true><<<TG.sh_c, tb, 0, st>>>(S, w.sh_list, C + 2, w.sh_o, w.sh_d, w.sh_c, cnt);
         } else {

@@ -128,9 +128,6 @@ public:
     // Threads per block of the traversal kernels (64, 128 or 256); taken by the next render or capture.
     void set_trace_block(int threads);
     int trace_block() const { return trace_block_; }
-    // Bounce levels (from the camera hit) whose shadow rays are binned by (light, origin cell) before
-    // they are traced.
-    void set_shadow_sort(int levels) { shadow_sort_levels_ = levels < 0 ? 0 : levels; }
     int guide_warmup() const { return guide_warmup_; }
 
 private:
@@ -145,7 +142,6 @@ private:
     int* wave_counter_ = nullptr;  // device sample index of captured wave graphs
     int sah_width_ = 4;            // SAH traversal variant (2 or 4 children per node)
     int trace_block_ = 128;        // threads per block of the traversal kernels
-    int shadow_sort_levels_ = 0;   // bounce levels whose shadow rays are binned before tracing
     WaveBuffers* wb_;
     int counting_ = 0;
     int present_buckets_ = 0;  // material buckets the loaded scene can produce

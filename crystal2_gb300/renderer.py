@@ -155,10 +155,6 @@ class Context:
         """SAH traversal variant: 2 (binary nodes) or 4 (four-wide nodes, default)."""
         self.check(self._lib.c2g_set_traversal(self._h, int(width)))
 
-    def set_shadow_sort(self, levels: int) -> None:
-        """Bounce levels whose shadow rays are binned by (light, origin cell) before tracing."""
-        self.check(self._lib.c2g_set_shadow_sort(self._h, int(levels)))
-
     def set_trace_block(self, threads: int) -> None:
         """Threads per block of the traversal kernels: 64, 128 (default) or 256."""
         self.check(self._lib.c2g_set_trace_block(self._h, int(threads)))

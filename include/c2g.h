@@ -186,10 +186,6 @@ int c2g_set_traversal(c2g_ctx* ctx, int width);
 /* Threads per block of the traversal kernels (64, 128 or 256; default 128); no counterpart in the
  * reference. */
 int c2g_set_trace_block(c2g_ctx* ctx, int threads);
-/* Bounce levels, from the camera hit, whose shadow rays are binned by (light, cell of the origin in
- * the scene box) before the four-wide any-hit kernel traces them (default 0); the answers are the
- * same.  No counterpart in the reference. */
-int c2g_set_shadow_sort(c2g_ctx* ctx, int levels);
 
 /* L2 read bandwidth of `device` in GB/s: a `bytes` buffer (keep it well below the L2 size) read
  * `reps` times by every SM with L2-only loads, timed with CUDA events.  No counterpart in the

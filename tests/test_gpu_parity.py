@@ -157,24 +157,6 @@ def test_traversal_variants_agree(accel, tmp_path):
         assert close.mean() >= 0.999
 
 
-@pytest.mark.parametrize("accel", ["BVH", "Brute"])
-def test_binned_shadow_rays_match(accel, tmp_path):
-    """Shadow rays traced in (light, origin cell) bin order get the same answers: the films with the
-    binning on 0, 1 and 3 bounce levels are bit-identical, on the scene with every shape kind, under
-    both any-hit semantics (the shadow leak of the BVH semantics included)."""
-    cp, sp = scenes.material_box(str(tmp_path / accel), width=40, height=40, spp=4, accel=accel)
-    ctx = _ctx(cp, sp, N.TREE_SAH)
-    films = []
-    for levels in (0, 1, 3):
-        ctx.set_shadow_sort(levels)
-        p = ctx.render_params()
-        ctx.film_clear()
-        ctx.render(p)
-        films.append(ctx.film()[0])
-    assert np.array_equal(films[0], films[1])
-    assert np.array_equal(films[0], films[2])
-
-
 def test_axis_aligned_shadow_leak_is_reproduced(tmp_path):
     """The BVH shadow test hands the object-box-clipped interval to the triangle test
     (BVH.cpp:132-134): an axis-aligned wall blocks a shadow ray only when the matrix-inverse t
