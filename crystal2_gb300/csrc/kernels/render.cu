@@ -106,7 +106,7 @@ GpuScene::GpuScene() : sb_(new DeviceSceneBuffers()), wb_(new WaveBuffers()) {}
 GpuScene::~GpuScene() {
     if (side_) cudaStreamDestroy(side_);
     if (ahead_) cudaStreamDestroy(ahead_);
-    for (int k = 0; k < 3; k++) {
+    for (int k = 0; k < 4; k++) {
         if (fork_ev_[k]) cudaEventDestroy(fork_ev_[k]);
         if (join_ev_[k]) cudaEventDestroy(join_ev_[k]);
     }
@@ -126,7 +126,7 @@ int GpuScene::side_stream(std::string& err) {
         ahead_ = nullptr;
         return C2G_ERR_CUDA;
     }
-    for (int k = 0; k < 3; k++)
+    for (int k = 0; k < 4; k++)
         if (cudaEventCreateWithFlags(&fork_ev_[k], cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&join_ev_[k], cudaEventDisableTiming) != cudaSuccess) {
             err = "cannot create stream events";
@@ -1328,19 +1328,27 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
         }
         ShadeOut so{buf[nxt], C + nxt, w.sh_o, w.sh_d, w.sh_c, w.mis_o, w.mis_d, w.mis_c, w.sh_list, w.mis_list, C + 2, C + 3, w.acc, w.mis_hit};
         // the material buckets are independent (they append to the shared queues with atomics):
-        // with overlap every second present bucket shades on the side stream
-        if (overlap) fork(0);
+        // with overlap the present buckets take the three streams in turn
+        if (overlap) {
+            fork(0);
+            cudaEventRecord(fork_ev_[3], st);
+            cudaStreamWaitEvent(ahead_, fork_ev_[3], 0);
+        }
         int nb = 0;
         for (int bk = 0; bk < kBuckets; bk++) {
             if (!(present_buckets_ & (1 << bk))) continue;
-            const cudaStream_t ss = (overlap && (nb & 1)) ? side_ : st;
+            const cudaStream_t ss = !overlap ? st : (nb % 3 == 1 ? side_ : (nb % 3 == 2 ? ahead_ : st));
             begin(C2G_K_SHADE, ss);
             launch_shade(bk, g_shade, ss, S, a, buf[cur], w.hit, C + kCntBucket, w.bucket_list, (int)w.P, so, gv, glevel);
             end(ss);
             launches++;
             nb++;
         }
-        if (overlap) join(0);
+        if (overlap) {
+            join(0);
+            cudaEventRecord(join_ev_[3], ahead_);
+            cudaStreamWaitEvent(st, join_ev_[3], 0);
+        }
         // The next level's queue is complete: its extension runs ahead on the third stream, beside
         // this level's shadow and MIS rays and accumulation (none of which reads the hits or the
         // buckets it writes).  Not for direct lighting, whose walk checks the queue on the host.

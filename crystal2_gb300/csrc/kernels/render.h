@@ -158,7 +158,7 @@ private:
     // Third stream of a wave: the next bounce level's extension starts on it as soon as this level's
     // shading has filled the next queue, beside this level's shadow and MIS rays and accumulation.
     cudaStream_t ahead_ = nullptr;
-    cudaEvent_t fork_ev_[3] = {nullptr, nullptr, nullptr}, join_ev_[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t fork_ev_[4] = {nullptr, nullptr, nullptr, nullptr}, join_ev_[4] = {nullptr, nullptr, nullptr, nullptr};
     int side_stream(std::string& err);
     float box_lo_[3] = {0, 0, 0}, box_hi_[3] = {1, 1, 1};  // scene bounds (network input range)
     c2g_stats stats_{};
