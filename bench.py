@@ -431,8 +431,9 @@ def run_ours(args) -> None:
 def guided_equal_time(args) -> dict:
     """Equal-time error of the guided path tracer against the plain one on the slit-lit glossy room.
 
-    Both arms render the same frame progressively in chunks of 8 spp, one wave of 8 samples per
-    chunk (the guided arm takes `--guided-train-steps` Adam steps after each wave), for the same
+    Both arms render the same frame progressively in chunks of `--guided-wave` spp (16: the plain
+    tracer's fastest wave size on this scene), one wave per chunk (the guided arm takes
+    `--guided-train-steps` Adam steps after each wave), for the same
     budget of render time (the c2g_render calls only; the error is evaluated outside the timer).  relMSE = mean((I - R)^2 / (R^2 + 0.01))
     against a plain reference of `--guided-ref-spp` samples from a disjoint sample range.
     Reported: both errors at the budget, the time the guided arm needs to reach the plain arm's
@@ -468,27 +469,29 @@ def guided_equal_time(args) -> dict:
         d = img.astype(np.float32) - ref32
         return float(np.mean(d * d * inv, dtype=np.float64))
 
+    ws = args.guided_wave
+
     def progressive(integ, wave_spp):
         ctx.film_clear()
         s0, spent, curve = 0, 0.0, []
         while spent < args.guided_seconds:
             t = time.perf_counter()
-            ctx.render(params(integ, s0, 8, wave_spp))
+            ctx.render(params(integ, s0, wave_spp, wave_spp))
             spent += time.perf_counter() - t
-            s0 += 8
+            s0 += wave_spp
             curve.append((spent, s0, relmse(ctx.image())))
         return curve
 
     ctx.film_clear()
     ctx.render(params(N.INTEGRATOR_PATH, 0, 4))  # first-launch costs out of the way
     # both arms render 8-sample waves (the guided arm trains after every wave)
-    plain = progressive(N.INTEGRATOR_PATH, 8)
+    plain = progressive(N.INTEGRATOR_PATH, ws)
     ctx.load(cp, sp, tree=N.TREE_SAH)  # a fresh, untrained network
     ctx.guide_config(args.guided_lr, args.guided_bsdf_fraction, args.guided_warmup, args.guided_train_steps)
     ctx.guide_levels(args.guided_levels)
     ctx.guide_batch(args.guided_records, args.guided_windows)
     ctx.guide_regularize(args.guided_kappa, 20.0, args.guided_lr_decay)
-    guided = progressive(N.INTEGRATOR_GUIDED, 8)
+    guided = progressive(N.INTEGRATOR_GUIDED, ws)
     target = plain[-1][2]
     reach = None
     for (t0_, _, e0), (t1_, _, e1) in zip(guided, guided[1:]):
@@ -498,21 +501,21 @@ def guided_equal_time(args) -> dict:
     if reach is None and guided and guided[0][2] <= target:
         reach = guided[0][0]
     loss, records, steps = ctx.guide_stats()
-    # one timed 8-spp wave of each arm (the trained network): device time per kernel kind
+    # one timed wave of each arm (the trained network): device time per kernel kind
     wave_ms = {}
     ctx.set_counting(N.COUNT_TIMING)
     for name, integ in (("plain", N.INTEGRATOR_PATH), ("guided", N.INTEGRATOR_GUIDED)):
-        ctx.render(params(integ, 1 << 20, 8, 8))
+        ctx.render(params(integ, 1 << 20, ws, ws))
         st = ctx.stats()
         wave_ms[name] = {"total": round(st.seconds * 1e3, 2),
                          **{N.KERNEL_NAMES[k]: round(st.kernel_ms[k], 2) for k in range(N.K_KINDS) if st.kernel_count[k] > 0}}
     ctx.set_counting(0)
     return {"scene": f"slit_room {W}x{H} (524k-triangle heightfield, GGX a U(0.1,0.3), slit-lit), max depth 12",
             "reference_spp": args.guided_ref_spp, "reference_s": round(ref_s, 2), "budget_s": args.guided_seconds,
-            "plain": {"spp": plain[-1][1], "s": round(plain[-1][0], 3), "relMSE": target, "samples_per_wave": 8},
+            "plain": {"spp": plain[-1][1], "s": round(plain[-1][0], 3), "relMSE": target, "samples_per_wave": ws},
             "guided": {"spp": guided[-1][1], "s": round(guided[-1][0], 3), "relMSE": guided[-1][2],
                        "bsdf_fraction": args.guided_bsdf_fraction, "learning_rate": args.guided_lr,
-                       "train_steps_per_wave": args.guided_train_steps, "samples_per_wave": 8,
+                       "train_steps_per_wave": args.guided_train_steps, "samples_per_wave": ws,
                        "records_per_wave": args.guided_records, "minibatch_windows": args.guided_windows,
                        "warmup_waves": args.guided_warmup, "kappa_max": args.guided_kappa, "lr_decay_steps": args.guided_lr_decay,
                        "guided_levels": args.guided_levels,
@@ -520,7 +523,7 @@ def guided_equal_time(args) -> dict:
             "time_to_plain_relMSE_s": None if reach is None else round(reach, 3),
             "time_ratio": None if reach is None else round(reach / plain[-1][0], 3),
             "equal_time_relMSE_ratio": round(guided[-1][2] / target, 3),
-            "wave_ms": wave_ms, "wave_ms_note": "one 8-spp wave per arm with per-launch CUDA events; kernels on the "
+            "wave_ms": wave_ms, "wave_ms_note": "one wave per arm with per-launch CUDA events; kernels on the "
                                                 "side stream overlap, so the kinds can sum past the total"}
 
 
@@ -659,9 +662,10 @@ def main() -> int:
     ap.add_argument("--guided-seconds", type=float, default=6.0)
     ap.add_argument("--guided-lr", type=float, default=1e-3)
     ap.add_argument("--guided-bsdf-fraction", type=float, default=0.7)
-    ap.add_argument("--guided-train-steps", type=int, default=64)
-    ap.add_argument("--guided-records", type=int, default=1 << 20, help="recorded vertices per guided wave")
-    ap.add_argument("--guided-windows", type=int, default=16, help="minibatch windows per guided wave")
+    ap.add_argument("--guided-train-steps", type=int, default=128)
+    ap.add_argument("--guided-records", type=int, default=1 << 21, help="recorded vertices per guided wave")
+    ap.add_argument("--guided-windows", type=int, default=32, help="minibatch windows per guided wave")
+    ap.add_argument("--guided-wave", type=int, default=16, help="samples per pixel per wave, both arms (plain's fastest)")
     ap.add_argument("--guided-warmup", type=int, default=1, help="guided waves that only train")
     ap.add_argument("--guided-kappa", type=float, default=200.0, help="vMF concentration cap of the guide mixture")
     ap.add_argument("--guided-lr-decay", type=float, default=2000.0, help="Adam steps over which the learning rate halves (0 = constant)")
