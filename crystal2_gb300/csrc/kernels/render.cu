@@ -1276,10 +1276,11 @@ int GpuScene::enqueue_wave(const WavePlan& plan, const WaveArgs& a, const GuideV
     begin(C2G_K_RAYGEN, st);
     k_raygen<<<g_raygen, 256, 0, st>>>(S, a, buf[0], w.out_L, C + 0);
     end(st);
-    // Extension of bounce level lv on stream es: closest hits of queue `q`, appended to the material
-    // buckets.  Block 0 zeroes *za, *zb, zb[2] (the queue after the next and the shadow queue with
-    // its fetch counter) and *zc (the MIS queue) - live counters when it runs in order, spare slots
-    // when it runs ahead of the previous level's shadow rays (those are zeroed on st afterwards).
+    // Extension of the paths in queue q on stream es: closest hits, appended to the material buckets.
+    // Block 0 zeroes *za (the count of the queue this level's shading fills), *zb and zb[2] (the
+    // shadow queue and its fetch counter) and *zc (the MIS queue): the live counters when it runs in
+    // order, spare slots when it runs ahead beside the previous level's shadow rays (the live ones
+    // are then zeroed on st after that level's accumulation).
     auto extend = [&](int q, int* za, int* zb, int* zc, cudaStream_t es) {
         begin(C2G_K_EXTEND, es);
         // bucket sizes and the extension fetch counter C[5] start at zero on every level
