@@ -31,29 +31,32 @@ __host__ __device__ constexpr bool bucket_guided(int b) {
 }
 
 // ---- inference on the fifth-generation tensor cores (tcgen05) -----------------------------------
-// Two kernels.  k_guide_encode (one thread per guided vertex, full occupancy) reconstructs the
-// surface, encodes (x, n, wo) and writes the row as BF16 into 128-row operand tiles in global
-// memory, already in the tensor core's shared-memory layout.  k_guide_mlp_tc streams those tiles
-// into shared memory with the bulk-copy engine and runs the four layers: two warpgroups per CTA
-// share the staged weights; per warpgroup and tile one thread issues K/16 tcgen05.mma (M = 128,
-// N = 64 or 48, BF16 operands from shared-memory descriptors, FP32 accumulator in 64 tensor-memory
-// columns) and commits them to an mbarrier; every thread then reads its row (tcgen05.ld), adds the
-// bias, applies ReLU and writes BF16 for the next layer, or packs the mixture after the last.  The
-// next tile's copy starts as soon as layer 0 has consumed the input buffer.
+// Two kernels.  k_guide_record (one thread per guided vertex, full occupancy) reconstructs the
+// surface and writes the vertex's network input as a compact record of 9 floats (x, n, wo), 36 B,
+// records of consecutive work items back to back.  k_guide_mlp_tc streams 128-record tiles into
+// shared memory with the bulk-copy engine; every thread frequency-encodes its own row into the
+// BF16 operand tile, already in the tensor core's shared-memory layout, and the warpgroup runs the
+// four layers: two warpgroups per CTA share the staged weights; per warpgroup and tile one thread
+// issues K/16 tcgen05.mma (M = 128, N = 64 or 48, BF16 operands from shared-memory descriptors,
+// FP32 accumulator in 64 tensor-memory columns) and commits them to an mbarrier; every thread then
+// reads its row (tcgen05.ld), adds the bias, applies ReLU and writes BF16 for the next layer over
+// the operand tile (the layer that read it has completed), or packs the mixture after the last.
+// The next tile's record copy starts as soon as the current tile is encoded.
 // Operand layout: K-major 8-row x 16-byte core matrices without swizzle; element (r, k) of a
 // K-column operand sits at (r / 8) * 16K + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2 bytes, so one
 // K=16 step spans two core matrices 128 B apart (descriptor LBO), 8-row groups 16K bytes apart (SBO).
 constexpr int kTcRows = 128;
 constexpr int kTcGroups = 2;                            // warpgroups per CTA
 constexpr int kTcThreads = kTcRows * kTcGroups;
-constexpr int kTcTileBytes = kTcRows * kGuideIn * 2;    // one staged input tile: 20480 B
-// staging bytes for n vertices: whole 128-row tiles
-constexpr size_t stage_bytes(size_t n) { return (n + kTcRows - 1) / kTcRows * (size_t)kTcTileBytes; }
+constexpr int kTcRecFloats = 9;                         // network input record: x, n, wo
+constexpr int kTcRecBytes = kTcRows * kTcRecFloats * 4;   // one tile of records: 4608 B
+constexpr int kTcTileBytes = kTcRows * kGuideIn * 2;    // one BF16 operand tile: 20480 B
+// record bytes for n vertices: whole 128-row tiles
+constexpr size_t stage_bytes(size_t n) { return (n + kTcRows - 1) / kTcRows * (size_t)kTcRecBytes; }
 __host__ __device__ constexpr int tc_w_off(int l) { return l == 0 ? 0 : tc_w_off(l - 1) + guide_n(l - 1) * guide_k(l - 1) * 2; }
-constexpr int kTcActBytes = kTcRows * kGuideHidden * 2;
-constexpr int kTcGroupBytes = kTcTileBytes + kTcActBytes;  // input tile + hidden activations
+constexpr int kTcGroupBytes = kTcTileBytes + kTcRecBytes;  // operand tile (input, then hidden activations) + records
 __host__ __device__ constexpr int tc_in(int g) { return tc_w_off(4) + g * kTcGroupBytes; }
-__host__ __device__ constexpr int tc_act(int g) { return tc_in(g) + kTcTileBytes; }
+__host__ __device__ constexpr int tc_rec(int g) { return tc_in(g) + kTcTileBytes; }
 constexpr int kTcBias = tc_w_off(4) + kTcGroups * kTcGroupBytes;
 constexpr int kTcBiasN = 3 * kGuideHidden + kGuideOutPad;
 constexpr int kTcBar = kTcBias + kTcBiasN * 4;          // per warpgroup: MMA-done and input-full mbarriers
@@ -62,8 +65,9 @@ constexpr size_t kTcSmem = (size_t)kTcTmemSlot + 8;
 constexpr uint32_t kTcColsPerGroup = 64;
 constexpr uint32_t kTcCols = kTcColsPerGroup * kTcGroups;  // tensor-memory columns per CTA (power of 2)
 constexpr uint32_t kTcWaitPolls = 1u << 22;
-static_assert(tc_in(0) % 128 == 0 && tc_act(0) % 128 == 0 && kTcGroupBytes % 128 == 0 && kTcBar % 8 == 0,
-              "operand and barrier alignment");
+static_assert(tc_in(0) % 128 == 0 && tc_rec(0) % 16 == 0 && kTcGroupBytes % 128 == 0 && kTcBar % 8 == 0,
+              "operand, bulk-copy and barrier alignment");
+static_assert(kTcRecBytes % 16 == 0 && (32 * kTcRecFloats * 4) % 16 == 0, "record tiles and warp chunks are 16-byte multiples");
 
 __device__ __forceinline__ int tc_cm(int r, int k, int K) { return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2; }
 
@@ -124,43 +128,47 @@ __device__ __forceinline__ void guided_bucket_ends(const int* bucket_cnt, int ma
     }
 }
 
-// MODE 0: the guided buckets' vertices; MODE 1: explicit inputs xnw (9 floats each).  Rows past the
-// last item of the last tile are zero.
-template <int MODE>
-__global__ void __launch_bounds__(256) k_guide_encode(DevScene S, GuideNet net, const float4* __restrict__ ray_o,
+// The guided buckets' vertices -> network input records (x, n, wo; kTcRecFloats floats each, work
+// item i at floats [9 i, 9 i + 9)).  Each warp assembles its 32 consecutive records in shared
+// memory and writes them as one contiguous 1152-byte run of float4 stores.
+__global__ void __launch_bounds__(256) k_guide_record(DevScene S, const float4* __restrict__ ray_o,
                                                      const float4* __restrict__ ray_d, const float4* __restrict__ hits,
                                                      const int* bucket_cnt, const int* __restrict__ bucket_list, int cap,
-                                                     int mask, const float* __restrict__ xnw, int n_in,
-                                                     unsigned char* stage) {
+                                                     int mask, float* rec) {
     __shared__ int bend[kBuckets];
-    if (MODE == 0 && threadIdx.x == 0) guided_bucket_ends(bucket_cnt, mask, bend);
+    __shared__ __align__(16) float chunk[8][32 * kTcRecFloats];
+    if (threadIdx.x == 0) guided_bucket_ends(bucket_cnt, mask, bend);
     __syncthreads();
-    const int total = MODE == 0 ? bend[kBuckets - 1] : n_in;
-    const int padded = (total + kTcRows - 1) / kTcRows * kTcRows;
+    const int total = bend[kBuckets - 1];
+    const int padded = (total + 31) & ~31;  // whole warps (the record buffer holds whole tiles)
+    const int lane = threadIdx.x & 31;
+    float* mine = chunk[threadIdx.x >> 5];
     for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < padded; item += gridDim.x * blockDim.x) {
-        unsigned char* tile = stage + (size_t)(item / kTcRows) * kTcTileBytes;
-        const int r = item % kTcRows;
+        float v[kTcRecFloats] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (item < total) {
-            if (MODE == 0) {
-                const int slot = guided_slot(bend, bucket_list, cap, item);
-                const float4 o4 = ray_o[slot], d4 = ray_d[slot], h4 = hits[slot];
-                Hit h{h4.x, h4.y, h4.z, __float_as_int(h4.w)};
-                Surface sf;
-                make_surface(S, f3(o4), f3(d4), h, sf);
-                tc_encode_row(net, sf.pos, sf.N, -f3(d4), tile, r);
-            } else {
-                const float* v = xnw + (size_t)9 * item;
-                tc_encode_row(net, f3(v[0], v[1], v[2]), f3(v[3], v[4], v[5]), f3(v[6], v[7], v[8]), tile, r);
-            }
-        } else {
-            const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int k = 0; k < kGuideIn; k += 8) tc_store8(tile, r, k, kGuideIn, z);
+            const int slot = guided_slot(bend, bucket_list, cap, item);
+            const float4 o4 = ray_o[slot], d4 = ray_d[slot], h4 = hits[slot];
+            Hit h{h4.x, h4.y, h4.z, __float_as_int(h4.w)};
+            Surface sf;
+            make_surface(S, f3(o4), f3(d4), h, sf);
+            v[0] = sf.pos.x; v[1] = sf.pos.y; v[2] = sf.pos.z;
+            v[3] = sf.N.x; v[4] = sf.N.y; v[5] = sf.N.z;
+            v[6] = -d4.x; v[7] = -d4.y; v[8] = -d4.z;
         }
+#pragma unroll
+        for (int k = 0; k < kTcRecFloats; k++) mine[lane * kTcRecFloats + k] = v[k];
+        __syncwarp();
+        // the warp's items are item - lane .. item - lane + 31 (32-aligned): one contiguous run
+        float4* dst = reinterpret_cast<float4*>(rec + (size_t)(item - lane) * kTcRecFloats);
+        const float4* src = reinterpret_cast<const float4*>(mine);
+        for (int q = lane; q < 32 * kTcRecFloats / 4; q += 32) dst[q] = src[q];
+        __syncwarp();
     }
 }
 
-// MODE 0: packed mixtures per queue slot; MODE 1: raw outputs (kGuideOut floats per input).
+// Input: records (kTcRecFloats floats per work item, whole 128-row tiles; rows past the last item
+// are not read).  MODE 0: the guided buckets' vertices, packed mixtures per queue slot; MODE 1:
+// n_in explicit inputs, raw outputs (kGuideOut floats per input).
 template <int MODE>
 __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, const unsigned char* __restrict__ stage,
                                                                const int* bucket_cnt, const int* __restrict__ bucket_list,
@@ -202,26 +210,38 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, co
     const uint32_t tmem = *tslot + grp * kTcColsPerGroup;             // this warpgroup's columns
     const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's 32 lanes
     unsigned char* IN = smem + tc_in(grp);
-    unsigned char* ACT = smem + tc_act(grp);
+    const float* REC = reinterpret_cast<const float*>(smem + tc_rec(grp));
     const int bar_id = 1 + grp;
     const int total = MODE == 0 ? bend[kBuckets - 1] : n_in;
     const int tiles = (total + kTcRows - 1) / kTcRows;
     const int tstride = gridDim.x * kTcGroups;
     int tile = blockIdx.x * kTcGroups + grp;
-    // phases of the two barriers, and whether a tile copy / an MMA group is outstanding (the same
+    // phases of the two barriers, and whether a record copy / an MMA group is outstanding (the same
     // in every thread of the warpgroup: issue decisions are uniform)
     uint32_t ph_mma = 0, ph_in = 0;
     bool copy_pending = false, mma_pending = false, failed = false;
     if (tile < tiles) {
         if (row == 0) {
-            mbar_arrive_expect_tx(bar_in, kTcTileBytes);
-            bulk_g2s(smem_u32(IN), stage + (size_t)tile * kTcTileBytes, kTcTileBytes, bar_in);
+            mbar_arrive_expect_tx(bar_in, kTcRecBytes);
+            bulk_g2s(smem_u32(REC), stage + (size_t)tile * kTcRecBytes, kTcRecBytes, bar_in);
         }
         copy_pending = true;
     }
     for (; tile < tiles && !failed; tile += tstride) {
         bool ok = mbar_wait(bar_in, ph_in, kTcWaitPolls);
         if (ok) { ph_in ^= 1u; copy_pending = false; }
+        const int item = tile * kTcRows + row;
+        // this thread's row of the operand tile (the previous tile's last layer has completed)
+        if (ok) {
+            if (item < total) {
+                const float* v = REC + row * kTcRecFloats;  // 9-float stride: conflict-free
+                tc_encode_row(net, f3(v[0], v[1], v[2]), f3(v[3], v[4], v[5]), f3(v[6], v[7], v[8]), IN, row);
+            } else {
+                const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int k = 0; k < kGuideIn; k += 8) tc_store8(IN, row, k, kGuideIn, z);
+            }
+        }
         float o[kGuideOutPad];
 #pragma unroll
         for (int l = 0; l < kGuideLayers; l++) {
@@ -231,26 +251,25 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, co
             if (wg_sync_or(bar_id, !ok)) { failed = true; break; }
             if (row == 0) {
                 tc_fence_after();
-                const uint32_t a0 = smem_u32(l == 0 ? IN : ACT), b0 = smem_u32(smem + tc_w_off(l));
+                const uint32_t a0 = smem_u32(IN), b0 = smem_u32(smem + tc_w_off(l));
                 const uint32_t idesc = umma_idesc_bf16(kTcRows, N);
                 for (int kk = 0; kk < K / 16; kk++)
                     umma_bf16(tmem, umma_desc(a0 + kk * 256, 128, K * 16), umma_desc(b0 + kk * 256, 128, K * 16), idesc, kk > 0);
                 umma_commit(bar_mma);
+                if (l == 0 && tile + tstride < tiles) {
+                    // every row of this tile is encoded: fetch the next tile's records behind the layers
+                    mbar_arrive_expect_tx(bar_in, kTcRecBytes);
+                    bulk_g2s(smem_u32(REC), stage + (size_t)(tile + tstride) * kTcRecBytes, kTcRecBytes, bar_in);
+                }
             }
+            if (l == 0 && tile + tstride < tiles) copy_pending = true;
             mma_pending = true;
             ok = mbar_wait(bar_mma, ph_mma, kTcWaitPolls);
             if (ok) { ph_mma ^= 1u; mma_pending = false; }
             if (wg_sync_or(bar_id, !ok)) { failed = true; break; }
             tc_fence_after();
-            if (l == 0 && tile + tstride < tiles) {
-                // layer 0 has consumed the input tile: fetch the next one behind layers 1-3
-                if (row == 0) {
-                    mbar_arrive_expect_tx(bar_in, kTcTileBytes);
-                    bulk_g2s(smem_u32(IN), stage + (size_t)(tile + tstride) * kTcTileBytes, kTcTileBytes, bar_in);
-                }
-                copy_pending = true;
-            }
             if (l < kGuideLayers - 1) {
+                // the next layer's operand over this one's (its MMAs have completed)
 #pragma unroll
                 for (int c = 0; c < kGuideHidden; c += 32) {
                     uint32_t r[32];
@@ -262,7 +281,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, co
                         float v[8];
 #pragma unroll
                         for (int j = 0; j < 8; j++) v[j] = fmaxf(__uint_as_float(r[q + j]) + bias[l * kGuideHidden + c + q + j], 0.f);
-                        tc_store8(ACT, row, c + q, kGuideHidden, v);
+                        tc_store8(IN, row, c + q, kGuideHidden, v);
                     }
                 }
             } else {
@@ -275,7 +294,6 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, co
             }
         }
         if (failed) break;
-        const int item = tile * kTcRows + row;
         if (item < total) {
             if (MODE == 0) pack_lobes(o, out + (size_t)guided_slot(bend, bucket_list, cap, item) * kGuidePacked, net.kappa_max);
             else {
@@ -903,7 +921,7 @@ void GuideTrainer::prepare_launch() {
     g_infer_grid = std::max(1, sms * std::max(1, per));
     g_train_grid = std::max(1, sms);
     int per_enc = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_enc, k_guide_encode<0>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_enc, k_guide_record, 256, 0);
     g_encode_grid = std::max(1, sms * std::max(1, per_enc));
 }
 
@@ -917,8 +935,7 @@ int GuideTrainer::infer(cudaStream_t st, const void* Sv, const float4* ray_o, co
     if (!mask) return 0;
     const DevScene& S = *static_cast<const DevScene*>(Sv);
     const GuideNet net = view(false, false).net;
-    k_guide_encode<0><<<g_encode_grid, 256, 0, st>>>(S, net, ray_o, ray_d, hits, bucket_cnt, bucket_list, cap, mask, nullptr, 0,
-                                                     stage_);
+    k_guide_record<<<g_encode_grid, 256, 0, st>>>(S, ray_o, ray_d, hits, bucket_cnt, bucket_list, cap, mask, (float*)stage_);
     k_guide_mlp_tc<0><<<grid, kTcThreads, kTcSmem, st>>>(net, stage_, bucket_cnt, bucket_list, cap, mask, 0, out_, S.err);
     return 2;
 }
@@ -988,21 +1005,19 @@ int GuideTrainer::get_params(float* host, std::string& err) {
 int GuideTrainer::eval(DeviceArena& arena, const float* host_xnw, int n, float* host_out, std::string& err) {
     if (!params_) { err = "guide network not initialised"; return C2G_ERR_STATE; }
     if (n <= 0) return C2G_OK;
-    float* din = (float*)arena.alloc((size_t)n * 9 * 4, err);
+    // the inputs are already records (9 floats each); the buffer holds whole tiles
+    float* din = (float*)arena.alloc(stage_bytes((size_t)n), err);
     float* dout = (float*)arena.alloc((size_t)n * kGuideOut * 4, err);
-    unsigned char* dstage = (unsigned char*)arena.alloc(stage_bytes((size_t)n), err);
     int* derr = (int*)arena.alloc(16, err);
     int rc = C2G_OK;
-    if (!din || !dout || !dstage || !derr) rc = C2G_ERR_OOM;
+    if (!din || !dout || !derr) rc = C2G_ERR_OOM;
     if (!rc) {
         cudaMemcpy(din, host_xnw, (size_t)n * 9 * 4, cudaMemcpyHostToDevice);
         cudaMemset(derr, 0, 16);
         prepare_launch();
         const GuideNet net = view(false, false).net;
-        k_guide_encode<1><<<std::min(g_encode_grid, (n + 255) / 256), 256>>>(DevScene{}, net, nullptr, nullptr, nullptr, nullptr,
-                                                                           nullptr, 0, 0, din, n, dstage);
         const int blocks = std::min(g_infer_grid, (n + kTcThreads - 1) / kTcThreads);
-        k_guide_mlp_tc<1><<<blocks, kTcThreads, kTcSmem>>>(net, dstage, nullptr, nullptr, 0, 0, n, dout, derr);
+        k_guide_mlp_tc<1><<<blocks, kTcThreads, kTcSmem>>>(net, (const unsigned char*)din, nullptr, nullptr, 0, 0, n, dout, derr);
         int h = 0;
         if (cudaDeviceSynchronize() != cudaSuccess) { err = cudaGetErrorString(cudaGetLastError()); rc = C2G_ERR_CUDA; }
         else if (cudaMemcpy(&h, derr, 4, cudaMemcpyDeviceToHost) == cudaSuccess && h) {
@@ -1012,7 +1027,6 @@ int GuideTrainer::eval(DeviceArena& arena, const float* host_xnw, int n, float* 
     }
     if (din) arena.free(din);
     if (dout) arena.free(dout);
-    if (dstage) arena.free(dstage);
     if (derr) arena.free(derr);
     return rc;
 }

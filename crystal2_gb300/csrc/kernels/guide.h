@@ -119,7 +119,7 @@ private:
     float* adam_v_ = nullptr;
     __nv_bfloat16* bf_ = nullptr;    // BF16 copies (both layouts)
     float* out_ = nullptr;           // per-slot outputs
-    unsigned char* stage_ = nullptr; // encoded inputs, 128-row BF16 operand tiles (160 B per vertex)
+    unsigned char* stage_ = nullptr; // network input records of the guided vertices (x, n, wo: 36 B per vertex)
     float4* rec_ = nullptr;
     float4* batch_ = nullptr;        // compacted training samples (x|w, n, wo, wi)
     int* batch_count_ = nullptr;

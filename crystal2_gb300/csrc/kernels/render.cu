@@ -232,6 +232,10 @@ __global__ void k_raygen(DevScene S, WaveArgs a, PathRefs out, float4* out_L, in
 #ifndef C2G_SHADOW_MIN_BLOCKS
 #define C2G_SHADOW_MIN_BLOCKS 1
 #endif
+// Minimum resident 128-thread blocks per SM of the shading kernels (their register budget).
+#ifndef C2G_SHADE_MIN_BLOCKS
+#define C2G_SHADE_MIN_BLOCKS 4
+#endif
 
 // ---- extend: closest hit of each queued path ray ------------------------------------------------
 // Per-kernel-kind traversal counters: cnt[3 * kind + {0: rays, 1: nodes, 2: prims}].
@@ -333,7 +337,7 @@ struct ShadeOut {
 };
 
 template <int MT, bool G>
-__global__ void __launch_bounds__(128, 4) k_shade(DevScene S, WaveArgs a, PathRefs cur, const float4* __restrict__ hits,
+__global__ void __launch_bounds__(128, C2G_SHADE_MIN_BLOCKS) k_shade(DevScene S, WaveArgs a, PathRefs cur, const float4* __restrict__ hits,
                                                 const int* bucket_cnt, const int* __restrict__ bucket_list, int cap, ShadeOut out,
                                                 GuideView gv) {
     const int n = bucket_cnt[MT];
