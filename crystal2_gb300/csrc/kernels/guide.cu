@@ -23,12 +23,6 @@ namespace c2g {
 namespace {
 __device__ __forceinline__ float luminance(float3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
 
-// Bucket ids whose hits are guided: the non-specular materials whose BSDF sampling routine returns
-// the exact density of the directions it draws (the mixture pdf needs it at guide-drawn directions).
-__host__ __device__ constexpr bool bucket_guided(int b) {
-    return b == MAT_DIFFUSE || b == MAT_MICRO_GGX || b == MAT_MICRO_BECKMANN || b == MAT_PLASTIC_GGX ||
-           b == MAT_PLASTIC_BECKMANN || b == MAT_ORENNAYAR;
-}
 
 // ---- inference on the fifth-generation tensor cores (tcgen05) -----------------------------------
 // Two kernels.  k_guide_record (one thread per guided vertex, full occupancy) reconstructs the
@@ -167,12 +161,12 @@ __global__ void __launch_bounds__(256) k_guide_record(DevScene S, const float4* 
 }
 
 // Input: records (kTcRecFloats floats per work item, whole 128-row tiles; rows past the last item
-// are not read).  MODE 0: the guided buckets' vertices, packed mixtures per queue slot; MODE 1:
-// n_in explicit inputs, raw outputs (kGuideOut floats per input).
+// are not read).  MODE 0: the guided buckets' vertices, packed mixtures per work item (field-major,
+// out_stride float4 per field); MODE 1: n_in explicit inputs, raw outputs (kGuideOut floats each).
 template <int MODE>
 __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, const unsigned char* __restrict__ stage,
-                                                               const int* bucket_cnt, const int* __restrict__ bucket_list,
-                                                               int cap, int mask, int n_in, float* out, int* err) {
+                                                               const int* bucket_cnt, int mask, int n_in, float* out,
+                                                               int out_stride, int* err) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int grp = threadIdx.x / kTcRows, row = threadIdx.x - grp * kTcRows, warp = threadIdx.x >> 5;
     float* bias = reinterpret_cast<float*>(smem + kTcBias);
@@ -295,7 +289,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, co
         }
         if (failed) break;
         if (item < total) {
-            if (MODE == 0) pack_lobes(o, out + (size_t)guided_slot(bend, bucket_list, cap, item) * kGuidePacked, net.kappa_max);
+            if (MODE == 0) pack_lobes(o, reinterpret_cast<float4*>(out) + item, out_stride, net.kappa_max);
             else {
 #pragma unroll
                 for (int k = 0; k < kGuideOut; k++) out[(size_t)item * kGuideOut + k] = o[k];
@@ -936,7 +930,7 @@ int GuideTrainer::infer(cudaStream_t st, const void* Sv, const float4* ray_o, co
     const DevScene& S = *static_cast<const DevScene*>(Sv);
     const GuideNet net = view(false, false).net;
     k_guide_record<<<g_encode_grid, 256, 0, st>>>(S, ray_o, ray_d, hits, bucket_cnt, bucket_list, cap, mask, (float*)stage_);
-    k_guide_mlp_tc<0><<<grid, kTcThreads, kTcSmem, st>>>(net, stage_, bucket_cnt, bucket_list, cap, mask, 0, out_, S.err);
+    k_guide_mlp_tc<0><<<grid, kTcThreads, kTcSmem, st>>>(net, stage_, bucket_cnt, mask, 0, out_, (int)cap_, S.err);
     return 2;
 }
 
@@ -975,6 +969,7 @@ GuideView GuideTrainer::view(bool record, bool sample) const {
     v.net.kappa_max = kappa_max_;
     v.net.weight_clamp = weight_clamp_;
     v.out = out_;
+    v.out_stride = (int)cap_;
     v.rec = rec_;
     v.rec_stride = rec_stride_;
     v.rec_depth = rec_depth_;
@@ -1017,7 +1012,7 @@ int GuideTrainer::eval(DeviceArena& arena, const float* host_xnw, int n, float* 
         prepare_launch();
         const GuideNet net = view(false, false).net;
         const int blocks = std::min(g_infer_grid, (n + kTcThreads - 1) / kTcThreads);
-        k_guide_mlp_tc<1><<<blocks, kTcThreads, kTcSmem>>>(net, (const unsigned char*)din, nullptr, nullptr, 0, 0, n, dout, derr);
+        k_guide_mlp_tc<1><<<blocks, kTcThreads, kTcSmem>>>(net, (const unsigned char*)din, nullptr, 0, n, dout, 0, derr);
         int h = 0;
         if (cudaDeviceSynchronize() != cudaSuccess) { err = cudaGetErrorString(cudaGetLastError()); rc = C2G_ERR_CUDA; }
         else if (cudaMemcpy(&h, derr, 4, cudaMemcpyDeviceToHost) == cudaSuccess && h) {

@@ -61,26 +61,54 @@ __device__ __forceinline__ float vmf_pdf(const Lobe& l, float3 w) {
     return l.kappa / (2.f * kPiF * (-expm1f(-2.f * l.kappa))) * __expf(l.kappa * (c - 1.f));
 }
 
+// Bucket ids whose hits are guided: the non-specular materials whose BSDF sampling routine returns
+// the exact density of the directions it draws (the mixture pdf needs it at guide-drawn directions).
+__host__ __device__ constexpr bool bucket_guided(int b) {
+    return b == MAT_DIFFUSE || b == MAT_MICRO_GGX || b == MAT_MICRO_BECKMANN || b == MAT_PLASTIC_GGX ||
+           b == MAT_PLASTIC_BECKMANN || b == MAT_ORENNAYAR;
+}
+
+// Work item of the guided vertices that sits at position `pos` of bucket MT's list: the guided
+// buckets' lists back to back in bucket order (the order inference runs over them).
+template <int MT>
+__device__ __forceinline__ int guided_item(const int* bucket_cnt, int pos) {
+    int base = 0;
+#pragma unroll
+    for (int b = 0; b < MT; b++)
+        if (bucket_guided(b)) base += __ldg(bucket_cnt + b);
+    return base + pos;
+}
+
 // ---- packed mixture (inference output, read by the shading kernels) ---------------------------
-// Per slot kGuidePacked floats: 8 float4 (mean direction, concentration), the 8 lobe weights, the 8
-// products weight x vMF normaliser, and the probability c of drawing from the mixture rather than
-// the BSDF.  A non-finite network output is flagged by a NaN first weight.
+// Per guided work item kGuidePacked floats as 13 float4 fields: 8 (mean direction, concentration),
+// the 8 lobe weights (fields 8-9), the 8 products weight x vMF normaliser (10-11), and the
+// probability c of drawing from the mixture rather than the BSDF (12.x).  A non-finite network
+// output is flagged by a NaN first weight.  Field-major: field f of item j is float4 f * stride + j
+// (stride: the wave's path capacity), so a warp's 32 consecutive items read and write each field
+// as one contiguous 512-byte run.
 constexpr int kGuidePacked = 52;
+constexpr int kGuideFields = kGuidePacked / 4;
+struct PackedMix {
+    const float4* p;   // field 0 of this item
+    int s;             // field stride in float4
+    __device__ __forceinline__ float4 f(int k) const { return __ldg(p + (size_t)k * s); }
+};
 
 // Technique selection: c = 0.05 + 0.75 sigmoid(s) keeps both techniques in use; at least a fifth
 // of the continuations follow the BSDF (a defensive mixture: a mixture that trained onto a few
 // sharp lobes cannot make the weights larger than 5x the BSDF-only ones).
 __host__ __device__ __forceinline__ float guide_select(float s) { return kGuideSelMin + kGuideSelSpan / (1.f + expf(-s)); }
 
-__device__ __forceinline__ void pack_lobes(const float* out, float* dst, float kappa_max) {
+// d4: field 0 of the item; stride: the field stride in float4.
+__device__ __forceinline__ void pack_lobes(const float* out, float4* d4, int stride, float kappa_max) {
     bool finite = true;
 #pragma unroll
     for (int k = 0; k < kGuideOut; k++) finite = finite && isfinite(out[k]);
     Lobe L[kGuideLobes];
     guide_lobes(out, L, kappa_max);
-    float4* d4 = reinterpret_cast<float4*>(dst);
+    const size_t s = (size_t)stride;
 #pragma unroll
-    for (int k = 0; k < kGuideLobes; k++) d4[k] = make_float4(L[k].mu.x, L[k].mu.y, L[k].mu.z, L[k].kappa);
+    for (int k = 0; k < kGuideLobes; k++) d4[k * s] = make_float4(L[k].mu.x, L[k].mu.y, L[k].mu.z, L[k].kappa);
     float w[kGuideLobes], wc[kGuideLobes];
 #pragma unroll
     for (int k = 0; k < kGuideLobes; k++) {
@@ -88,42 +116,45 @@ __device__ __forceinline__ void pack_lobes(const float* out, float* dst, float k
         wc[k] = L[k].w * L[k].kappa / (2.f * kPiF * (-expm1f(-2.f * L[k].kappa)));
     }
     if (!finite) w[0] = __int_as_float(0x7fc00000);
-    d4[8] = make_float4(w[0], w[1], w[2], w[3]);
-    d4[9] = make_float4(w[4], w[5], w[6], w[7]);
-    d4[10] = make_float4(wc[0], wc[1], wc[2], wc[3]);
-    d4[11] = make_float4(wc[4], wc[5], wc[6], wc[7]);
-    d4[12] = make_float4(guide_select(out[40]), 0.f, 0.f, 0.f);
+    d4[8 * s] = make_float4(w[0], w[1], w[2], w[3]);
+    d4[9 * s] = make_float4(w[4], w[5], w[6], w[7]);
+    d4[10 * s] = make_float4(wc[0], wc[1], wc[2], wc[3]);
+    d4[11 * s] = make_float4(wc[4], wc[5], wc[6], wc[7]);
+    d4[12 * s] = make_float4(guide_select(out[40]), 0.f, 0.f, 0.f);
 }
 
-// Probability of drawing the continuation from the mixture (vs the BSDF).
-__device__ __forceinline__ float packed_select(const float4* p) { return __ldg(p + 12).x; }
+__device__ __forceinline__ float f4_at(const float4& v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w)); }
 
-__device__ __forceinline__ bool packed_valid(const float4* p) { return isfinite(__ldg(p + 8).x); }
+// Probability of drawing the continuation from the mixture (vs the BSDF).
+__device__ __forceinline__ float packed_select(const PackedMix& p) { return p.f(12).x; }
+
+__device__ __forceinline__ bool packed_valid(const PackedMix& p) { return isfinite(p.f(8).x); }
 
 // Mixture density at the unit direction w.  Kept out of line: the shading kernel calls it per
 // light and per continuation, and one copy keeps its instruction footprint small.
-static __device__ __noinline__ float packed_pdf(const float4* p, float3 w) {
-    const float* wc = reinterpret_cast<const float*>(p + 10);
+static __device__ __noinline__ float packed_pdf(const PackedMix p, float3 w) {
+    const float4 wc0 = p.f(10), wc1 = p.f(11);
     float s = 0.f;
 #pragma unroll
     for (int k = 0; k < kGuideLobes; k++) {
-        const float4 m = __ldg(p + k);
-        s += __ldg(wc + k) * __expf(m.w * (m.x * w.x + m.y * w.y + m.z * w.z - 1.f));
+        const float4 m = p.f(k);
+        const float wc = k < 4 ? f4_at(wc0, k) : f4_at(wc1, k - 4);
+        s += wc * __expf(m.w * (m.x * w.x + m.y * w.y + m.z * w.z - 1.f));
     }
     return s;
 }
 
 // Sample: lobe by weight with u0, then the vMF around its mean (w = cos theta by inversion).
-static __device__ __noinline__ float3 packed_sample(const float4* p, float u0, float u1, float u2) {
-    const float* wt = reinterpret_cast<const float*>(p + 8);
+static __device__ __noinline__ float3 packed_sample(const PackedMix p, float u0, float u1, float u2) {
+    const float4 w0 = p.f(8), w1 = p.f(9);
     int k = kGuideLobes - 1;
     float acc = 0.f;
 #pragma unroll
     for (int i = 0; i < kGuideLobes; i++) {
-        acc += __ldg(wt + i);
+        acc += i < 4 ? f4_at(w0, i) : f4_at(w1, i - 4);
         if (u0 < acc) { k = i; break; }
     }
-    const float4 l = __ldg(p + k);
+    const float4 l = p.f(k);
     const float kappa = l.w;
     const float e = __expf(-2.f * kappa);
     float cw = 1.f + __logf(fmaxf(u1 + (1.f - u1) * e, 1e-30f)) / kappa;

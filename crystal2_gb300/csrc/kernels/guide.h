@@ -46,7 +46,8 @@ class DeviceArena;
 // Per-wave view handed to the shading kernels.
 struct GuideView {
     GuideNet net;
-    const float* out;      // per queue slot: the packed mixture (kGuidePacked floats, guide.cuh)
+    const float* out;      // per guided work item: the packed mixture (kGuidePacked floats, field-major, guide.cuh)
+    int out_stride;        // its field stride in float4 (the wave's path capacity)
     float4* rec;           // training records, 4 float4 per (recorded path, bounce)
     int rec_stride;        // every rec_stride-th path id records its vertices
     int rec_depth;         // records per recorded path (= max depth)

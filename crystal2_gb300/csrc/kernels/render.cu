@@ -440,7 +440,8 @@ __global__ void __launch_bounds__(128, C2G_SHADE_MIN_BLOCKS) k_shade(DevScene S,
         // technique of direct lighting (no separate MIS ray); light samples are weighted against the
         // mixture pdf.  Before the network is trained alpha = 1.
         const bool gvert = G && do_nee && !direct && (bx.flags & BXDF_SPECULAR) == 0;
-        const float4* lobes = reinterpret_cast<const float4*>(gv.out + (size_t)i * kGuidePacked);
+        const PackedMix lobes{reinterpret_cast<const float4*>(gv.out) + (G ? guided_item<MT>(bucket_cnt, base + (int)threadIdx.x) : 0),
+                              gv.out_stride};
         float alpha = 1.f;
         const float detM = gvert ? fabsf(dot(fr.T, cross(fr.N, fr.B))) : 1.f;
         if (gvert && gv.sample) {
