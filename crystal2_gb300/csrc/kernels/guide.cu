@@ -44,16 +44,25 @@ constexpr int kTcGroups = 2;                            // warpgroups per CTA
 constexpr int kTcThreads = kTcRows * kTcGroups;
 constexpr int kTcRecFloats = 9;                         // network input record: x, n, wo
 constexpr int kTcRecBytes = kTcRows * kTcRecFloats * 4;   // one tile of records: 4608 B
-constexpr int kTcTileBytes = kTcRows * kGuideIn * 2;    // one BF16 operand tile: 20480 B
+// Every layer runs with K = 80: the 80 inputs of layer 0, or a layer's 64 inputs then 16 more
+// columns.  Two columns of every operand row hold 1.0 (inputs 78-79 of layer 0, whose features are
+// the encoding's two zeros; columns 64-65 of the hidden activations) and the matching weight
+// columns the bias split into two BF16 halves (hi = bf16(b), lo = bf16(b - hi)), so the MMA adds
+// the bias to within FP32 rounding and the epilogues only apply ReLU.
+constexpr int kTcK = kGuideIn;
+static_assert(kTcK >= kGuideHidden + 2 && kTcK % 16 == 0, "room for the bias columns");
+__host__ __device__ constexpr int tc_bias_col(int l) { return l == 0 ? kGuideIn - 2 : kGuideHidden; }
+constexpr int kTcTileBytes = kTcRows * kTcK * 2;        // one BF16 operand tile: 20480 B
 // record bytes for n vertices: whole 128-row tiles
 constexpr size_t stage_bytes(size_t n) { return (n + kTcRows - 1) / kTcRows * (size_t)kTcRecBytes; }
+// weights of layer l, K-major: K = guide_k(l) (training kernel) or kTcK (inference kernel)
 __host__ __device__ constexpr int tc_w_off(int l) { return l == 0 ? 0 : tc_w_off(l - 1) + guide_n(l - 1) * guide_k(l - 1) * 2; }
+__host__ __device__ constexpr int tc_wi_off(int l) { return l == 0 ? 0 : tc_wi_off(l - 1) + guide_n(l - 1) * kTcK * 2; }
 constexpr int kTcGroupBytes = kTcTileBytes + kTcRecBytes;  // operand tile (input, then hidden activations) + records
-__host__ __device__ constexpr int tc_in(int g) { return tc_w_off(4) + g * kTcGroupBytes; }
+__host__ __device__ constexpr int tc_in(int g) { return tc_wi_off(4) + g * kTcGroupBytes; }
 __host__ __device__ constexpr int tc_rec(int g) { return tc_in(g) + kTcTileBytes; }
-constexpr int kTcBias = tc_w_off(4) + kTcGroups * kTcGroupBytes;
-constexpr int kTcBiasN = 3 * kGuideHidden + kGuideOutPad;
-constexpr int kTcBar = kTcBias + kTcBiasN * 4;          // per warpgroup: MMA-done and input-full mbarriers
+constexpr int kTcBiasN = 3 * kGuideHidden + kGuideOutPad;   // (the training kernel's bias table)
+constexpr int kTcBar = tc_wi_off(4) + kTcGroups * kTcGroupBytes;  // per warpgroup: MMA-done and input-full mbarriers
 constexpr int kTcTmemSlot = kTcBar + 16 * kTcGroups;
 constexpr size_t kTcSmem = (size_t)kTcTmemSlot + 8;
 constexpr uint32_t kTcColsPerGroup = 64;
@@ -79,8 +88,9 @@ __device__ __forceinline__ void tc_store8(unsigned char* base, int r, int k0, in
 // eight values at a time: position p in the scene box as sin/cos(pi 2^f p), f = 0..11 per axis
 // (one exactly reduced sincospif, then the double-angle recurrence sin 2u = 2 sin u cos u,
 // cos 2u = (cos u - sin u)(cos u + sin u), whose absolute error grows about 2x per octave: ~1e-4 at
-// 2^11, far below BF16 resolution), the shading normal, the outgoing direction, two zeros.
-template <int W = kGuideIn>
+// 2^11, far below BF16 resolution), the shading normal, the outgoing direction, two zeros (two
+// ones with BIAS_COLS: the inference kernel's bias columns).
+template <int W = kGuideIn, bool BIAS_COLS = false>
 __device__ __forceinline__ void tc_encode_row(const GuideNet& g, float3 x, float3 n, float3 wo, unsigned char* base, int r) {
     const float p[3] = {(x.x - g.box_lo[0]) * g.box_inv[0], (x.y - g.box_lo[1]) * g.box_inv[1], (x.z - g.box_lo[2]) * g.box_inv[2]};
     float chunk[8];
@@ -104,7 +114,8 @@ __device__ __forceinline__ void tc_encode_row(const GuideNet& g, float3 x, float
             c = c2;
         }
     }
-    const float tail[8] = {n.x, n.y, n.z, wo.x, wo.y, wo.z, 0.f, 0.f};
+    const float one = BIAS_COLS ? 1.f : 0.f;
+    const float tail[8] = {n.x, n.y, n.z, wo.x, wo.y, wo.z, one, one};
     tc_store8(base, r, 72, W, tail);
 }
 
@@ -169,23 +180,27 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, co
                                                                int out_stride, int* err) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int grp = threadIdx.x / kTcRows, row = threadIdx.x - grp * kTcRows, warp = threadIdx.x >> 5;
-    float* bias = reinterpret_cast<float*>(smem + kTcBias);
     const uint32_t bar_mma = smem_u32(smem + kTcBar + 16 * grp), bar_in = bar_mma + 8;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kTcTmemSlot);
-    // weights -> core-matrix layout; biases
+    // weights -> core-matrix layout with K = kTcK: the layer's weights (wt: N x K, K contiguous),
+    // the two bias halves in the bias columns, zeros after them
 #pragma unroll
     for (int l = 0; l < kGuideLayers; l++) {
-        const int K = guide_k(l), N = guide_n(l), vpr = K / 8;
-        const uint4* src = reinterpret_cast<const uint4*>(net.bf + guide_bf_off(l));  // wt: N x K, K contiguous
-        for (int i = threadIdx.x; i < N * vpr; i += kTcThreads) {
-            const int nn = i / vpr, c = i - nn * vpr;
-            *reinterpret_cast<uint4*>(smem + tc_w_off(l) + tc_cm(nn, 8 * c, K)) = src[i];
+        const int K = guide_k(l), N = guide_n(l), bc = tc_bias_col(l);
+        const __nv_bfloat16* wt = net.bf + guide_bf_off(l);
+        for (int i = threadIdx.x; i < N * (kTcK / 8); i += kTcThreads) {
+            const int nn = i / (kTcK / 8), c = i - nn * (kTcK / 8);
+            const float b = net.params[guide_b_off(l) + nn];
+            const __nv_bfloat16 bh = __float2bfloat16_rn(b);
+            const __nv_bfloat16 bl = __float2bfloat16_rn(b - __bfloat162float(bh));
+            __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int k = 8 * c + j;
+                v[j] = k < bc ? wt[nn * K + k] : (k == bc ? bh : (k == bc + 1 ? bl : __float2bfloat16_rn(0.f)));
+            }
+            *reinterpret_cast<uint4*>(smem + tc_wi_off(l) + tc_cm(nn, 8 * c, kTcK)) = *reinterpret_cast<const uint4*>(v);
         }
-    }
-    for (int i = threadIdx.x; i < kTcBiasN; i += kTcThreads) {
-        const int l = i < 3 * kGuideHidden ? i / kGuideHidden : 3;
-        const int j = i - l * kGuideHidden;
-        bias[i] = net.params[guide_b_off(l) + j];
     }
     __shared__ int bend[kBuckets];
     if (threadIdx.x == 0) {
@@ -229,26 +244,27 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, co
         if (ok) {
             if (item < total) {
                 const float* v = REC + row * kTcRecFloats;  // 9-float stride: conflict-free
-                tc_encode_row(net, f3(v[0], v[1], v[2]), f3(v[3], v[4], v[5]), f3(v[6], v[7], v[8]), IN, row);
+                tc_encode_row<kTcK, true>(net, f3(v[0], v[1], v[2]), f3(v[3], v[4], v[5]), f3(v[6], v[7], v[8]), IN, row);
             } else {
                 const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-                for (int k = 0; k < kGuideIn; k += 8) tc_store8(IN, row, k, kGuideIn, z);
+                for (int k = 0; k < kTcK; k += 8) tc_store8(IN, row, k, kTcK, z);
             }
         }
         float o[kGuideOutPad];
 #pragma unroll
         for (int l = 0; l < kGuideLayers; l++) {
-            const int K = guide_k(l), N = guide_n(l);
+            const int N = guide_n(l);
             fence_async_smem();
             tc_fence_before();
             if (wg_sync_or(bar_id, !ok)) { failed = true; break; }
             if (row == 0) {
                 tc_fence_after();
-                const uint32_t a0 = smem_u32(IN), b0 = smem_u32(smem + tc_w_off(l));
+                const uint32_t a0 = smem_u32(IN), b0 = smem_u32(smem + tc_wi_off(l));
                 const uint32_t idesc = umma_idesc_bf16(kTcRows, N);
-                for (int kk = 0; kk < K / 16; kk++)
-                    umma_bf16(tmem, umma_desc(a0 + kk * 256, 128, K * 16), umma_desc(b0 + kk * 256, 128, K * 16), idesc, kk > 0);
+                for (int kk = 0; kk < kTcK / 16; kk++)
+                    umma_bf16(tmem, umma_desc(a0 + kk * 256, 128, kTcK * 16), umma_desc(b0 + kk * 256, 128, kTcK * 16), idesc,
+                              kk > 0);
                 umma_commit(bar_mma);
                 if (l == 0 && tile + tstride < tiles) {
                     // every row of this tile is encoded: fetch the next tile's records behind the layers
@@ -263,7 +279,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, co
             if (wg_sync_or(bar_id, !ok)) { failed = true; break; }
             tc_fence_after();
             if (l < kGuideLayers - 1) {
-                // the next layer's operand over this one's (its MMAs have completed)
+                // the next layer's operand over this one's (its MMAs have completed): ReLU, BF16
 #pragma unroll
                 for (int c = 0; c < kGuideHidden; c += 32) {
                     uint32_t r[32];
@@ -272,11 +288,20 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, co
                     tmem_wait();
 #pragma unroll
                     for (int q = 0; q < 32; q += 8) {
-                        float v[8];
-#pragma unroll
-                        for (int j = 0; j < 8; j++) v[j] = fmaxf(__uint_as_float(r[q + j]) + bias[l * kGuideHidden + c + q + j], 0.f);
-                        tc_store8(IN, row, c + q, kGuideHidden, v);
+                        uint4 u;
+                        u.x = pack_bf16_relu(__uint_as_float(r[q + 0]), __uint_as_float(r[q + 1]));
+                        u.y = pack_bf16_relu(__uint_as_float(r[q + 2]), __uint_as_float(r[q + 3]));
+                        u.z = pack_bf16_relu(__uint_as_float(r[q + 4]), __uint_as_float(r[q + 5]));
+                        u.w = pack_bf16_relu(__uint_as_float(r[q + 6]), __uint_as_float(r[q + 7]));
+                        *reinterpret_cast<uint4*>(IN + tc_cm(row, c + q, kTcK)) = u;
                     }
+                }
+                if (l == 0) {
+                    // the hidden layers' bias columns (1, 1) and zeros over the rest of the input
+                    const float t0[8] = {1.f, 1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                    const float t1[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                    tc_store8(IN, row, kGuideHidden, kTcK, t0);
+                    tc_store8(IN, row, kGuideHidden + 8, kTcK, t1);
                 }
             } else {
                 uint32_t r[kGuideOutPad];
@@ -284,7 +309,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_guide_mlp_tc(GuideNet net, co
                 for (int c = 0; c < kGuideOutPad; c += 16) tmem_ld16(trow + c, r + c);
                 tmem_wait();
 #pragma unroll
-                for (int j = 0; j < kGuideOutPad; j++) o[j] = __uint_as_float(r[j]) + bias[3 * kGuideHidden + j];
+                for (int j = 0; j < kGuideOutPad; j++) o[j] = __uint_as_float(r[j]);
             }
         }
         if (failed) break;

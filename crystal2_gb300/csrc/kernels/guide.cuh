@@ -25,6 +25,13 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
 }
+// ReLU and BF16 rounding of two values in one conversion (negative values become +0; a NaN stays
+// a NaN, so a non-finite layer still marks the mixture invalid).
+__device__ __forceinline__ uint32_t pack_bf16_relu(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
 
 // ---- the directional mixture -----------------------------------------------------------------
 struct Lobe {
