@@ -492,14 +492,30 @@ def guided_equal_time(args) -> dict:
     ctx.guide_batch(args.guided_records, args.guided_windows)
     ctx.guide_regularize(args.guided_kappa, 20.0, args.guided_lr_decay)
     guided = progressive(N.INTEGRATOR_GUIDED, ws)
+    def time_to(curve, err):
+        """Render time at which a progressive curve first reaches err (linear in between)."""
+        for (t0_, _, e0), (t1_, _, e1) in zip(curve, curve[1:]):
+            if e1 <= err:
+                return t0_ + (t1_ - t0_) * ((e0 - err) / (e0 - e1) if e0 > e1 else 1.0)
+        if curve and curve[0][2] <= err:
+            return curve[0][0]
+        return None
+
     target = plain[-1][2]
-    reach = None
-    for (t0_, _, e0), (t1_, _, e1) in zip(guided, guided[1:]):
-        if e1 <= target:
-            reach = t0_ + (t1_ - t0_) * ((e0 - target) / (e0 - e1) if e0 > e1 else 1.0)
+    reach = time_to(guided, target)
+    # the same ratio at earlier points of plain's curve: the time the guided arm needs to reach the
+    # error plain had after t seconds, over t
+    checkpoints = []
+    for t in (2.0, 4.0, 6.0, 8.0, 10.0, 15.0, 20.0):
+        if t > plain[-1][0]:
             break
-    if reach is None and guided and guided[0][2] <= target:
-        reach = guided[0][0]
+        before = [p for p in plain if p[0] <= t]
+        if not before:
+            continue
+        t_p, spp_p, err_p = before[-1]
+        r = time_to(guided, err_p)
+        checkpoints.append({"plain_s": round(t_p, 2), "plain_spp": spp_p, "relMSE": err_p,
+                            "time_ratio": None if r is None else round(r / t_p, 3)})
     loss, records, steps = ctx.guide_stats()
     # one timed wave of each arm (the trained network): device time per kernel kind
     wave_ms = {}
@@ -522,6 +538,7 @@ def guided_equal_time(args) -> dict:
                        "adam_steps": steps, "last_batch": records, "last_loss": round(loss, 4)},
             "time_to_plain_relMSE_s": None if reach is None else round(reach, 3),
             "time_ratio": None if reach is None else round(reach / plain[-1][0], 3),
+            "time_ratio_curve": checkpoints,
             "equal_time_relMSE_ratio": round(guided[-1][2] / target, 3),
             "wave_ms": wave_ms, "wave_ms_note": "one wave per arm with per-launch CUDA events; kernels on the "
                                                 "side stream overlap, so the kinds can sum past the total"}
@@ -659,7 +676,7 @@ def main() -> int:
     ap.add_argument("--no-guided", action="store_true", help="skip the guided-vs-plain equal-time measurement")
     ap.add_argument("--guided-res", default="1920x1080")
     ap.add_argument("--guided-ref-spp", type=int, default=16384)
-    ap.add_argument("--guided-seconds", type=float, default=6.0)
+    ap.add_argument("--guided-seconds", type=float, default=10.0, help="render time per arm of the guided leg")
     ap.add_argument("--guided-lr", type=float, default=1e-3)
     ap.add_argument("--guided-bsdf-fraction", type=float, default=0.7)
     ap.add_argument("--guided-train-steps", type=int, default=128)
