@@ -31,10 +31,11 @@ __device__ __forceinline__ float luminance(float3 c) { return 0.2126f * c.x + 0.
 // shared memory with the bulk-copy engine; every thread frequency-encodes its own row into the
 // BF16 operand tile, already in the tensor core's shared-memory layout, and the warpgroup runs the
 // four layers: two warpgroups per CTA share the staged weights; per warpgroup and tile one thread
-// issues K/16 tcgen05.mma (M = 128, N = 64 or 48, BF16 operands from shared-memory descriptors,
-// FP32 accumulator in 64 tensor-memory columns) and commits them to an mbarrier; every thread then
-// reads its row (tcgen05.ld), adds the bias, applies ReLU and writes BF16 for the next layer over
-// the operand tile (the layer that read it has completed), or packs the mixture after the last.
+// issues K/16 tcgen05.mma (M = 128, N = 64 or 48, K = 80 with the bias folded in below, BF16
+// operands from shared-memory descriptors, FP32 accumulator in 64 tensor-memory columns) and
+// commits them to an mbarrier; every thread then reads its row (tcgen05.ld), applies ReLU and
+// writes BF16 for the next layer over the operand tile (the layer that read it has completed), or
+// packs the mixture after the last.
 // The next tile's record copy starts as soon as the current tile is encoded.
 // Operand layout: K-major 8-row x 16-byte core matrices without swizzle; element (r, k) of a
 // K-column operand sits at (r / 8) * 16K + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2 bytes, so one
