@@ -428,6 +428,34 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
 
 
+def time_to_error(curve, err):
+    """Render time at which a progressive error curve [(seconds, spp, relMSE), ...] first reaches
+    err, interpolated linearly between the two waves around it; None if it never does."""
+    if curve and curve[0][2] <= err:
+        return curve[0][0]
+    for (t0_, _, e0), (t1_, _, e1) in zip(curve, curve[1:]):
+        if e1 <= err:  # here e0 > err >= e1
+            return t0_ + (t1_ - t0_) * (e0 - err) / (e0 - e1)
+    return None
+
+
+def time_ratio_curve(plain, guided, points=(2.0, 4.0, 6.0, 8.0, 10.0, 15.0, 20.0)):
+    """At each point t of plain's curve (its last wave ending by t): the time the guided curve needs
+    to reach the error plain had then, over plain's time."""
+    out = []
+    for t in points:
+        if not plain or t > plain[-1][0]:
+            break
+        before = [p for p in plain if p[0] <= t]
+        if not before:
+            continue
+        t_p, spp_p, err_p = before[-1]
+        r = time_to_error(guided, err_p)
+        out.append({"plain_s": round(t_p, 2), "plain_spp": spp_p, "relMSE": err_p,
+                    "time_ratio": None if r is None else round(r / t_p, 3)})
+    return out
+
+
 def guided_equal_time(args) -> dict:
     """Equal-time error of the guided path tracer against the plain one on the slit-lit glossy room.
 
@@ -492,30 +520,9 @@ def guided_equal_time(args) -> dict:
     ctx.guide_batch(args.guided_records, args.guided_windows)
     ctx.guide_regularize(args.guided_kappa, 20.0, args.guided_lr_decay)
     guided = progressive(N.INTEGRATOR_GUIDED, ws)
-    def time_to(curve, err):
-        """Render time at which a progressive curve first reaches err (linear in between)."""
-        for (t0_, _, e0), (t1_, _, e1) in zip(curve, curve[1:]):
-            if e1 <= err:
-                return t0_ + (t1_ - t0_) * ((e0 - err) / (e0 - e1) if e0 > e1 else 1.0)
-        if curve and curve[0][2] <= err:
-            return curve[0][0]
-        return None
-
     target = plain[-1][2]
-    reach = time_to(guided, target)
-    # the same ratio at earlier points of plain's curve: the time the guided arm needs to reach the
-    # error plain had after t seconds, over t
-    checkpoints = []
-    for t in (2.0, 4.0, 6.0, 8.0, 10.0, 15.0, 20.0):
-        if t > plain[-1][0]:
-            break
-        before = [p for p in plain if p[0] <= t]
-        if not before:
-            continue
-        t_p, spp_p, err_p = before[-1]
-        r = time_to(guided, err_p)
-        checkpoints.append({"plain_s": round(t_p, 2), "plain_spp": spp_p, "relMSE": err_p,
-                            "time_ratio": None if r is None else round(r / t_p, 3)})
+    reach = time_to_error(guided, target)
+    checkpoints = time_ratio_curve(plain, guided)
     loss, records, steps = ctx.guide_stats()
     # one timed wave of each arm (the trained network): device time per kernel kind
     wave_ms = {}
